@@ -1,0 +1,69 @@
+"""Packing helpers for the golden fixtures.
+
+Spectral fields in NHQG's rfft2 layout ``(levels, Nx, Nx//2+1)`` are stored
+packed to the 2/3-rule band: rows ``kx in [0..K] + [Nx-K..Nx-1]`` (fftfreq
+order) and columns ``ky in [0..K]`` with ``K = Nx//3``.  Every state the
+reference produces from a band-limited input is exactly zero outside that
+rectangle, and ``make_golden.py`` asserts it before packing.
+"""
+
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+
+GOLDEN_DIR = Path(__file__).parent
+
+
+def band_rows(Nx: int) -> np.ndarray:
+    K = Nx // 3
+    return np.concatenate([np.arange(K + 1), np.arange(Nx - K, Nx)])
+
+
+def pack(field: np.ndarray, Nx: int) -> np.ndarray:
+    K = Nx // 3
+    rows = band_rows(Nx)
+    return np.ascontiguousarray(field[:, rows, : K + 1])
+
+
+def out_of_band_max(field: np.ndarray, Nx: int) -> float:
+    K = Nx // 3
+    rows = band_rows(Nx)
+    keep = np.zeros(field.shape[1:], dtype=bool)
+    keep[np.ix_(rows, np.arange(K + 1))] = True
+    rest = field[:, ~keep]
+    return float(np.max(np.abs(rest))) if rest.size else 0.0
+
+
+def unpack(packed: np.ndarray, Nx: int) -> np.ndarray:
+    K = Nx // 3
+    Nk = Nx // 2 + 1
+    out = np.zeros((packed.shape[0], Nx, Nk), dtype=packed.dtype)
+    out[:, band_rows(Nx), : K + 1] = packed
+    return out
+
+
+def load_case(name: str) -> tuple[dict, dict]:
+    """Return (config dict, arrays dict with spectral fields unpacked)."""
+    with np.load(GOLDEN_DIR / f"{name}.npz") as z:
+        meta = json.loads(str(z["meta"]))
+        Nx = meta["cfg"]["Nx"]
+        arrays = {}
+        for key in z.files:
+            if key == "meta":
+                continue
+            a = z[key]
+            if key.endswith("__packed"):
+                arrays[key[: -len("__packed")]] = unpack(a, Nx)
+            else:
+                arrays[key] = a
+    return meta, arrays
+
+
+def state_from(arrays: dict, prefix: str):
+    return tuple(arrays[f"{prefix}.{f}"] for f in ("q_hat", "w_hat", "th_hat", "th_bar"))
+
+
+CASES = ("prod16", "fixed16", "jac16", "polar16", "radix24", "legacy16")

@@ -1,0 +1,96 @@
+"""Pin the CPU oracle against golden vectors produced by the reference source.
+
+The fixtures in ``tests/golden`` hold the unmodified reference's outputs
+(``tests/golden/make_golden.py``).  The oracle restates the same algorithm in
+NumPy with different operation order (GEMM vs einsum, SciPy vs NumPy FFT), so
+agreement is to round-off, not bitwise.
+"""
+
+import numpy as np
+import pytest
+
+import fixtures
+import oracle
+from oracle.nhqg_oracle import OracleConfig, OracleState
+from _util import assert_state_close, rel_l2
+
+TOL = 1e-12
+
+
+def _grid(meta, arrays):
+    cfg = dict(meta["cfg"])
+    cfg.pop("_override_eta_sponge", None)
+    grid = oracle.make_grid(OracleConfig(**cfg))
+    if meta.get("override_eta_sponge"):
+        grid = grid.replace(eta_hat=arrays["grid.eta_hat"][0], sponge_phys=arrays["grid.sponge_phys"])
+    return grid
+
+
+def _state(arrays, prefix):
+    return OracleState(*fixtures.state_from(arrays, prefix))
+
+
+@pytest.fixture(scope="module", params=fixtures.CASES)
+def case(request):
+    meta, arrays = fixtures.load_case(request.param)
+    return request.param, meta, arrays, _grid(meta, arrays)
+
+
+def _base(grid, meta):
+    if meta["split"]:
+        return grid.replace(thermal_closure="fixed_conduction", mean_exchange_discretization="legacy")
+    return grid
+
+
+def test_initial_state(case):
+    name, meta, arrays, grid = case
+    s0 = oracle.theta_perturbation_state(grid, seed=meta["seed"])
+    assert_state_close(s0, _state(arrays, "s0"), TOL, th_bar_abs=0.0)
+
+
+def test_explicit_rhs(case):
+    name, meta, arrays, grid = case
+    E = oracle.explicit_rhs_dispatch(_state(arrays, "r"), _base(grid, meta))
+    assert_state_close(E, _state(arrays, "E"), TOL, th_bar_abs=1e-14)
+
+
+def test_implicit_tendency(case):
+    name, meta, arrays, grid = case
+    I = oracle.implicit_tendency(_state(arrays, "r"), _base(grid, meta))
+    assert_state_close(I, _state(arrays, "I"), TOL, th_bar_abs=1e-12)
+
+
+def test_implicit_solve(case):
+    name, meta, arrays, grid = case
+    r = _state(arrays, "r")
+    base = _base(grid, meta)
+    q, w, th = oracle.imex_implicit_solve(r.q_hat, r.w_hat, r.th_hat, base)
+    tb = oracle.imex_mean_temp_solve(r.th_bar, base)
+    assert_state_close((q, w, th, tb), _state(arrays, "solve"), TOL, th_bar_abs=1e-13)
+
+
+def test_corrector(case):
+    name, meta, arrays, grid = case
+    if not meta["split"]:
+        pytest.skip("no SBP2 corrector in this recipe")
+    alpha = grid.gamma_imex * grid.dt
+    out = oracle.apply_balanced_sbp2_corrector(_state(arrays, "r"), grid, alpha)
+    assert_state_close(out, _state(arrays, "corr"), TOL, th_bar_abs=1e-14)
+
+
+def test_steps(case):
+    name, meta, arrays, grid = case
+    s = _state(arrays, "r")
+    s = oracle.imex_step(s, grid)
+    assert_state_close(s, _state(arrays, "r1"), TOL, th_bar_abs=1e-14)
+    for _ in range(4):
+        s = oracle.imex_step(s, grid)
+    assert_state_close(s, _state(arrays, "r5"), 1e-11, th_bar_abs=1e-13)
+
+
+def test_seeded_trajectory(case):
+    name, meta, arrays, grid = case
+    s = _state(arrays, "s0")
+    for _ in range(meta["n_steps"]):
+        s = oracle.imex_step(s, grid)
+    assert_state_close(s, _state(arrays, "sN"), 1e-11, th_bar_abs=1e-16)
