@@ -1,0 +1,157 @@
+/*
+ * nhqg_gpu.h -- C ABI of the GB300 (sm_103a) NHQG time-step engine.
+ *
+ * The engine advances the nonhydrostatic quasi-geostrophic state of
+ * ksr-ocean/NHQG with the ARS(2,2,2) IMEX step: 2/3-rule dealiased
+ * horizontal products (flux or Jacobian form), Chebyshev / Dirichlet-Galerkin
+ * vertical transforms, per-|k|^2-shell implicit solves with buoyancy
+ * elimination, and the balanced SBP2 mean-temperature corrector.
+ *
+ * Conventions
+ *   - Spectral fields are complex128 stored as interleaved (re, im) doubles in
+ *     the reference layout (levels, Nx, Nx/2+1), ky contiguous, kx in fftfreq
+ *     order; q_hat has Nz+1 levels (Chebyshev), w_hat / th_hat have Nz-1
+ *     (Galerkin), th_bar is Nz+1 doubles.  Pointers passed to the compute
+ *     entry points are DEVICE pointers; the caller owns them.
+ *   - Every call is ordered on the given CUDA stream (passed as void*, NULL =
+ *     legacy default stream) and never synchronises the host.
+ *   - Every entry point returns an nhqg_status; device-side conditions (a
+ *     state that is not band-limited, a bounded wait that ran out) are latched
+ *     in the context and read with nhqg_get_device_status after the stream
+ *     has been synchronised.
+ *   - A context is used by one host thread at a time; separate contexts may
+ *     run concurrently on separate streams.
+ */
+#ifndef NHQG_GPU_H
+#define NHQG_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum nhqg_status {
+  NHQG_OK = 0,
+  NHQG_ERR_BAD_ARG = 1,          /* null pointer, inconsistent sizes */
+  NHQG_ERR_UNSUPPORTED = 2,      /* configuration outside the GPU path */
+  NHQG_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+  NHQG_ERR_DEVICE_TIMEOUT = 4,   /* a bounded device wait ran out */
+  NHQG_ERR_NOT_BAND_LIMITED = 5  /* input had content outside the 2/3 band */
+} nhqg_status;
+
+enum { NHQG_ADV_FLUX = 0, NHQG_ADV_JACOBIAN = 1 };
+enum { NHQG_CLOSURE_FIXED_CONDUCTION = 0, NHQG_CLOSURE_EVOLVE_MEAN = 1 };
+enum { NHQG_EXCHANGE_LEGACY = 0, NHQG_EXCHANGE_BALANCED_SBP2 = 1,
+       NHQG_EXCHANGE_BALANCED_SBP2_PC = 2 };
+enum { NHQG_WBC_DIRICHLET = 0, NHQG_WBC_NEUMANN = 1 };
+
+/*
+ * Host-side description of a Grid (nhqg/grid.py:29-141 Grid fields, built by
+ * make_grid, nhqg/grid.py:439-789).  All arrays are HOST float64 row-major in
+ * the reference's shapes; they are copied to the device by nhqg_ctx_create
+ * and may be freed afterwards.  P = Nz+1, G = Nz-1, Nk = Nx/2+1.
+ */
+typedef struct nhqg_grid_desc {
+  int Nx, Nz;
+  int advection;          /* NHQG_ADV_* (nonlinear_advection) */
+  int thermal_closure;    /* NHQG_CLOSURE_* */
+  int exchange;           /* NHQG_EXCHANGE_* (mean_exchange_discretization) */
+  int w_bc_top;           /* NHQG_WBC_* */
+  int substeps;           /* sbp_corrector_substeps */
+  int n_shells;           /* number of matrices in shell_inv */
+  double dt, gamma_imex, Ra_sigma, sigma, beta, eps_sq;
+  const double *kx, *ky;                       /* (Nx,), (Nk,) */
+  const double *inv_denom;                     /* (Nx,Nk) */
+  const double *diss_rate_q, *diss_rate_w, *diss_rate_th;  /* (Nx,Nk) */
+  const double *inv_alpha_q, *inv_alpha_th;    /* (Nx,Nk) */
+  const int *shell_of_mode;                    /* (Nx,Nk) row of shell_inv, or -1 */
+  const double *shell_inv;                     /* (n_shells,G,G) imex_inv rows */
+  const double *eta_hat;                       /* (Nx,Nk) complex or NULL */
+  const double *eta_phys;                      /* (Nx,Nx) irfft2(eta_hat), or NULL */
+  const double *sponge_phys;                   /* (Nx,Nx) or NULL */
+  const double *V, *V_inv;                     /* (P,P) */
+  const double *w_stencil;                     /* (P,G) */
+  const double *G_Z;                           /* (P,P) */
+  const double *proj_dirichlet;                /* (P,P) */
+  const double *sbp_D1, *sbp_L;                /* (P,P) */
+  const double *cgl_to_sbp, *sbp_to_cgl;       /* (P,P) */
+  const double *mean_solve;                    /* (P,P) inverse of the tau'd
+                                                  1-D mean operator (legacy
+                                                  evolve_mean), else NULL */
+} nhqg_grid_desc;
+
+typedef struct nhqg_ctx nhqg_ctx;
+
+/* Device-resident state in the reference layout (nhqg/solver.py:33-38). */
+typedef struct nhqg_state {
+  void *q_hat;     /* (Nz+1, Nx, Nk) complex128 */
+  void *w_hat;     /* (Nz-1, Nx, Nk) complex128 */
+  void *th_hat;    /* (Nz-1, Nx, Nk) complex128 */
+  double *th_bar;  /* (Nz+1,) float64 */
+} nhqg_state;
+
+/* Create a context: validates the configuration, uploads the tables.
+ * Replaces the jit closure over the Grid in the reference drivers
+ * (scripts/benchmark.py:39-45: jax.jit(lambda s: imex_step(s, grid))). */
+int nhqg_ctx_create(const nhqg_grid_desc *desc, nhqg_ctx **out);
+int nhqg_ctx_destroy(nhqg_ctx *ctx);
+
+/* n_steps applications of imex_step (nhqg/solver.py:1228-1242, including
+ * sanitize_state), in place.  The input must be band-limited (every state
+ * that sanitize_state, make_initial_state, run or imex_step produced is). */
+int nhqg_step(nhqg_ctx *ctx, nhqg_state *state, int n_steps, void *stream);
+
+/* explicit_rhs (nhqg/solver.py:510-599) at `in`, written to `out`.
+ * closure/exchange select the Grid flavour the reference call would see
+ * (the split steppers evaluate it on the fixed_conduction/legacy base grid,
+ * nhqg/solver.py:1172-1175). */
+int nhqg_explicit_rhs(nhqg_ctx *ctx, const nhqg_state *in, nhqg_state *out,
+                      int thermal_closure, int exchange, void *stream);
+
+/* implicit_tendency (nhqg/solver.py:615-641). */
+int nhqg_implicit_tendency(nhqg_ctx *ctx, const nhqg_state *in, nhqg_state *out,
+                           int thermal_closure, void *stream);
+
+/* imex_implicit_solve (nhqg/solver.py:691-738) of (R.q_hat, R.w_hat,
+ * R.th_hat) and imex_mean_temp_solve (nhqg/solver.py:741-758) of R.th_bar. */
+int nhqg_implicit_solve(nhqg_ctx *ctx, const nhqg_state *rhs, nhqg_state *out,
+                        int thermal_closure, void *stream);
+
+/* _apply_balanced_sbp2_corrector (nhqg/solver.py:909-950) with total_dt. */
+int nhqg_sbp2_corrector(nhqg_ctx *ctx, const nhqg_state *in, nhqg_state *out,
+                        double total_dt, void *stream);
+
+/* triple_conservative_flux_divergence_23 / triple_jacobian_23
+ * (nhqg/spectral.py:331-358) on `levels` planes (Nx, Nk) complex128 each:
+ * inputs psi, q, w, th; outputs Aq, Aw, Ath (masked). advection = NHQG_ADV_*. */
+int nhqg_triple_advection_23(nhqg_ctx *ctx, int advection, int levels,
+                             const void *psi, const void *q, const void *w,
+                             const void *th, void *Aq, void *Aw, void *Ath,
+                             void *stream);
+
+/* sponge_product_23 (nhqg/spectral.py:53-60) with the context's sponge. */
+int nhqg_sponge_product_23(nhqg_ctx *ctx, int levels, const void *f, void *out,
+                           void *stream);
+
+/* sanitize_state (nhqg/solver.py:128-146), in place: Hermitian projection
+ * of the ky=0 column and the 2/3 band limit. */
+int nhqg_sanitize(nhqg_ctx *ctx, nhqg_state *state, void *stream);
+
+/* imex_mean_temp_solve (nhqg/solver.py:741-758) of R_th_bar (Nz+1 doubles,
+ * device) into out. */
+int nhqg_mean_temp_solve(nhqg_ctx *ctx, const double *R_th_bar, double *out,
+                         int thermal_closure, void *stream);
+
+/* Latched device-side status of the last calls (after a stream sync);
+ * reset = 1 clears it. */
+int nhqg_get_device_status(nhqg_ctx *ctx, int reset);
+
+/* Number of kernel launches the last compute call issued (bench accounting). */
+int nhqg_last_launch_count(const nhqg_ctx *ctx);
+
+/* Engine build identification string (static storage). */
+const char *nhqg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NHQG_GPU_H */

@@ -1,0 +1,679 @@
+// C ABI of the NHQG GB300 engine: context creation (table upload), the
+// ARS(2,2,2) step orchestration and the per-operator entry points.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "engine.h"
+#include "nhqg_gpu.h"
+
+using namespace nhqg;
+
+struct nhqg_ctx {
+  Params p{};
+  Tables t{};
+  Work w{};
+  std::vector<void*> allocs;
+  int launches = 0;
+  // named compact work fields
+  double2 *q0, *w0, *t0, *Qn, *Wn, *Tn, *Aq, *Aw, *At, *E1q, *E1w, *E1t, *Rq, *Rt, *rhs;
+  double2 *Q1, *W1, *T1p, *T1, *Q2, *W2, *T2p, *T2, *Wcgl, *Wsbp, *Tsbp, *Tcgl;
+  // 1-D vectors [P]
+  double *tb0, *tb1p, *tb1, *tb2p, *tb2, *E1tb, *E2tb, *Itb, *flux, *dtb;
+};
+
+namespace {
+
+#define CK(call)                                  \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess) return NHQG_ERR_CUDA;  \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(nhqg_ctx* c, T** ptr, size_t n) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T) + 16);
+  if (e != cudaSuccess) return e;
+  c->allocs.push_back(p);
+  *ptr = static_cast<T*>(p);
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t upload(nhqg_ctx* c, T** ptr, const T* host, size_t n) {
+  cudaError_t e = dalloc(c, ptr, n);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*ptr, host, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void free_all(nhqg_ctx* c) {
+  for (void* p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+}
+
+struct CSR {
+  std::vector<int> ptr, col;
+  std::vector<double> val;
+};
+CSR to_csr(const double* A, int n) {
+  CSR s;
+  s.ptr.push_back(0);
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < n; ++j) {
+      const double v = A[(size_t)i * n + j];
+      if (v != 0.0) { s.col.push_back(j); s.val.push_back(v); }
+    }
+    s.ptr.push_back((int)s.col.size());
+  }
+  if (s.col.empty()) { s.col.push_back(0); s.val.push_back(0.0); }
+  return s;
+}
+
+int full_index(const Dims& d, int r, int c) { return full_row(r, d.K, d.Nx) * d.Nk + c; }
+
+}  // namespace
+
+extern "C" {
+
+const char* nhqg_version(void) { return "nhqg_gb300 0.1 (sm_103a, FP64 plain path)"; }
+
+int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
+  if (!g || !out) return NHQG_ERR_BAD_ARG;
+  *out = nullptr;
+  if (g->Nx < 8 || g->Nx % 2 != 0 || g->Nz < 4 || g->Nz + 1 > 1024) return NHQG_ERR_UNSUPPORTED;
+  FftPlan plan = make_fft_plan(g->Nx);
+  if (plan.npass <= 0) return NHQG_ERR_UNSUPPORTED;
+  if (g->advection != NHQG_ADV_FLUX && g->advection != NHQG_ADV_JACOBIAN) return NHQG_ERR_UNSUPPORTED;
+  if (g->exchange < NHQG_EXCHANGE_LEGACY || g->exchange > NHQG_EXCHANGE_BALANCED_SBP2_PC)
+    return NHQG_ERR_UNSUPPORTED;
+  if (g->thermal_closure == NHQG_CLOSURE_EVOLVE_MEAN && g->exchange == NHQG_EXCHANGE_LEGACY &&
+      !g->mean_solve)
+    return NHQG_ERR_BAD_ARG;
+  if (!g->kx || !g->ky || !g->inv_denom || !g->diss_rate_q || !g->diss_rate_w || !g->diss_rate_th ||
+      !g->inv_alpha_q || !g->inv_alpha_th || !g->shell_of_mode || !g->shell_inv || !g->V ||
+      !g->V_inv || !g->w_stencil || !g->G_Z || !g->proj_dirichlet || !g->sbp_D1 || !g->sbp_L ||
+      !g->cgl_to_sbp || !g->sbp_to_cgl)
+    return NHQG_ERR_BAD_ARG;
+  if (g->eta_hat && !g->eta_phys) return NHQG_ERR_BAD_ARG;
+
+  nhqg_ctx* c = new (std::nothrow) nhqg_ctx();
+  if (!c) return NHQG_ERR_BAD_ARG;
+  Params& p = c->p;
+  p.d = make_dims(g->Nx, g->Nz);
+  p.plan = plan;
+  p.advection = g->advection;
+  p.closure = g->thermal_closure;
+  p.exchange = g->exchange;
+  p.wbc = g->w_bc_top;
+  p.substeps = g->substeps > 0 ? g->substeps : 1;
+  p.dt = g->dt; p.gamma_imex = g->gamma_imex; p.Ra_sigma = g->Ra_sigma; p.sigma = g->sigma;
+  p.beta = g->beta; p.eps_sq = g->eps_sq;
+  p.has_eta = g->eta_hat != nullptr;
+  p.has_sponge = g->sponge_phys != nullptr;
+  const Dims& d = p.d;
+  const int P = d.P, G = d.G, N = d.Nz, M = d.M;
+  int rc = NHQG_OK;
+  auto fail = [&](int code) { free_all(c); delete c; return code; };
+#define UP(dst, src, n) \
+  if (upload(c, &(dst), (src), (n)) != cudaSuccess) return fail(NHQG_ERR_CUDA)
+
+  // ---- w stencil structure ----
+  std::vector<double> wa, wb;
+  if (g->w_bc_top == NHQG_WBC_DIRICHLET) {
+    for (int n = 0; n < G; ++n) {
+      if (g->w_stencil[(size_t)n * G + n] != -1.0 || g->w_stencil[(size_t)(n + 2) * G + n] != 1.0)
+        return fail(NHQG_ERR_UNSUPPORTED);
+    }
+  } else if (g->w_bc_top == NHQG_WBC_NEUMANN) {
+    wa.resize(G);
+    wb.resize(G);
+    for (int n = 0; n < G; ++n) {
+      if (g->w_stencil[(size_t)n * G + n] != 1.0) return fail(NHQG_ERR_UNSUPPORTED);
+      wa[n] = g->w_stencil[(size_t)(n + 1) * G + n];
+      wb[n] = g->w_stencil[(size_t)(n + 2) * G + n];
+    }
+  } else {
+    return fail(NHQG_ERR_UNSUPPORTED);
+  }
+
+  // ---- per-mode compact tables ----
+  std::vector<double> kx(M), ky(M), idn(M), iaq(M), iat(M), drq(M), drw(M), drt(M);
+  std::vector<double2> eta;
+  if (p.has_eta) eta.resize(M);
+  std::vector<int> shell(M);
+  for (int r = 0; r < d.Mr; ++r) {
+    for (int cc = 0; cc < d.Mc; ++cc) {
+      const int m = r * d.Mc + cc;
+      const int f = full_index(d, r, cc);
+      kx[m] = g->kx[full_row(r, d.K, d.Nx)];
+      ky[m] = g->ky[cc];
+      idn[m] = g->inv_denom[f];
+      iaq[m] = g->inv_alpha_q[f];
+      iat[m] = g->inv_alpha_th[f];
+      drq[m] = g->diss_rate_q[f];
+      drw[m] = g->diss_rate_w[f];
+      drt[m] = g->diss_rate_th[f];
+      if (p.has_eta) eta[m] = make_double2(g->eta_hat[2 * (size_t)f], g->eta_hat[2 * (size_t)f + 1]);
+      shell[m] = g->shell_of_mode[f];
+      if (shell[m] < 0 || shell[m] >= g->n_shells) return fail(NHQG_ERR_BAD_ARG);
+    }
+  }
+  Tables& t = c->t;
+  UP(t.kx, kx.data(), M); UP(t.ky, ky.data(), M); UP(t.inv_denom, idn.data(), M);
+  UP(t.inv_aq, iaq.data(), M); UP(t.inv_at, iat.data(), M);
+  UP(t.drq, drq.data(), M); UP(t.drw, drw.data(), M); UP(t.drt, drt.data(), M);
+  if (p.has_eta) {
+    UP(t.eta, eta.data(), M);
+    UP(t.eta_phys, g->eta_phys, (size_t)d.Nx * d.Nx);
+  }
+  if (p.has_sponge) UP(t.sponge, g->sponge_phys, (size_t)d.Nx * d.Nx);
+  UP(t.kx_full, g->kx, d.Nx);
+  UP(t.ky_full, g->ky, d.Nk);
+  UP(t.inv_denom_full, g->inv_denom, (size_t)d.Nx * d.Nk);
+  if (p.wbc == NHQG_WBC_NEUMANN) { UP(t.wst_a, wa.data(), G); UP(t.wst_b, wb.data(), G); }
+
+  // ---- FFT tables ----
+  {
+    std::vector<double2> tw(d.Nx);
+    for (int k = 0; k < d.Nx; ++k) {
+      // exp(-2 pi i k / Nx), argument reduced to the first octant for accuracy
+      const long num = k, den = d.Nx;
+      const double ang = 2.0 * M_PI * (double)num / (double)den;
+      double cs = std::cos(ang), sn = std::sin(ang);
+      if (4 * k == d.Nx) { cs = 0.0; sn = 1.0; }
+      if (2 * k == d.Nx) { cs = -1.0; sn = 0.0; }
+      if (4 * k == 3 * d.Nx) { cs = 0.0; sn = -1.0; }
+      tw[k] = make_double2(cs, -sn);
+    }
+    std::vector<int> perm(d.Nx);
+    make_fft_perm(plan, perm.data());
+    UP(t.tw, tw.data(), d.Nx);
+    UP(t.perm, perm.data(), d.Nx);
+  }
+
+  // ---- vertical tables ----
+  UP(t.V, g->V, (size_t)P * P);
+  UP(t.Vinv, g->V_inv, (size_t)P * P);
+  UP(t.proj, g->proj_dirichlet, (size_t)P * P);
+  UP(t.D1, g->sbp_D1, (size_t)P * P);
+  UP(t.Lsbp, g->sbp_L, (size_t)P * P);
+  UP(t.GZ, g->G_Z, (size_t)P * P);
+  {
+    std::vector<double> gz2((size_t)P * P, 0.0);
+    // G_Z2 = G_Z @ G_Z (nhqg/grid.py:463)
+    for (int i = 0; i < P; ++i)
+      for (int kk = 0; kk < P; ++kk) {
+        const double a = g->G_Z[(size_t)i * P + kk];
+        if (a == 0.0) continue;
+        for (int j = 0; j < P; ++j) gz2[(size_t)i * P + j] += a * g->G_Z[(size_t)kk * P + j];
+      }
+    UP(t.GZ2, gz2.data(), (size_t)P * P);
+  }
+  if (g->mean_solve) UP(t.mean_solve, g->mean_solve, (size_t)P * P);
+  {
+    CSR a = to_csr(g->cgl_to_sbp, P), b = to_csr(g->sbp_to_cgl, P);
+    UP(t.c2s_ptr, a.ptr.data(), a.ptr.size()); UP(t.c2s_col, a.col.data(), a.col.size());
+    UP(t.c2s_val, a.val.data(), a.val.size());
+    UP(t.s2c_ptr, b.ptr.data(), b.ptr.size()); UP(t.s2c_col, b.col.data(), b.col.size());
+    UP(t.s2c_val, b.val.data(), b.val.size());
+    UP(t.c2s_d, g->cgl_to_sbp, (size_t)P * P);
+    UP(t.s2c_d, g->sbp_to_cgl, (size_t)P * P);
+  }
+  {
+    // F = (proj_dir - I)[N-1:N+1, :] @ V_inv ; bcV = V[:, N-1], V[:, N]
+    std::vector<double> F(2 * (size_t)P, 0.0), bv(2 * (size_t)P);
+    for (int r = 0; r < 2; ++r) {
+      const int row = N - 1 + r;
+      for (int kk = 0; kk < P; ++kk) {
+        const double a = g->proj_dirichlet[(size_t)row * P + kk] - (kk == row ? 1.0 : 0.0);
+        if (a == 0.0) continue;
+        for (int j = 0; j < P; ++j) F[(size_t)r * P + j] += a * g->V_inv[(size_t)kk * P + j];
+      }
+    }
+    for (int l = 0; l < P; ++l) {
+      bv[l] = g->V[(size_t)l * P + (N - 1)];
+      bv[P + l] = g->V[(size_t)l * P + N];
+    }
+    UP(t.bcF, F.data(), F.size());
+    UP(t.bcV, bv.data(), bv.size());
+  }
+
+  // ---- shells present in the band ----
+  {
+    std::map<int, std::vector<int>> by_shell;
+    for (int m = 0; m < M; ++m) by_shell[shell[m]].push_back(m);
+    std::vector<int> start, modes;
+    std::vector<int> used;
+    for (auto& kv : by_shell) {
+      used.push_back(kv.first);
+      start.push_back((int)modes.size());
+      for (int m : kv.second) modes.push_back(m);
+      t.max_shell_modes = std::max(t.max_shell_modes, (int)kv.second.size());
+    }
+    start.push_back((int)modes.size());
+    t.n_shells = (int)used.size();
+    if (dalloc(c, &t.shell_inv, (size_t)t.n_shells * G * G) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+    for (int s = 0; s < t.n_shells; ++s) {
+      if (cudaMemcpy(t.shell_inv + (size_t)s * G * G, g->shell_inv + (size_t)used[s] * G * G,
+                     (size_t)G * G * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(NHQG_ERR_CUDA);
+    }
+    UP(t.shell_start, start.data(), start.size());
+    UP(t.shell_modes, modes.data(), modes.size());
+  }
+
+  // ---- work buffers ----
+  Work& w = c->w;
+  const size_t fe = (size_t)P * M;
+  double2** named[] = {&c->q0, &c->w0, &c->t0, &c->Qn, &c->Wn, &c->Tn, &c->Aq, &c->Aw, &c->At,
+                       &c->E1q, &c->E1w, &c->E1t, &c->Rq, &c->Rt, &c->rhs, &c->Q1, &c->W1,
+                       &c->T1p, &c->T1, &c->Q2, &c->W2, &c->T2p, &c->T2, &c->Wcgl, &c->Wsbp,
+                       &c->Tsbp, &c->Tcgl};
+  for (double2** f : named) {
+    if (dalloc(c, f, fe) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+    if (cudaMemset(*f, 0, fe * sizeof(double2)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  }
+  double** vecs[] = {&c->tb0, &c->tb1p, &c->tb1, &c->tb2p, &c->tb2, &c->E1tb, &c->E2tb, &c->Itb,
+                     &c->flux, &c->dtb};
+  for (double** v : vecs) {
+    if (dalloc(c, v, (size_t)P) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+    cudaMemset(*v, 0, P * sizeof(double));
+  }
+  if (dalloc(c, &w.vec, corrector_vec_doubles(P)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  cudaMemset(w.vec, 0, corrector_vec_doubles(P) * sizeof(double));
+  if (dalloc(c, &w.status, 4) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  cudaMemset(w.status, 0, 4 * sizeof(int));
+  {
+    const int nf1 = (p.advection == NHQG_ADV_JACOBIAN) ? 11 : 5;
+    const int ng = (p.advection == NHQG_ADV_JACOBIAN) ? 3 : 6;
+    w.x1_elems = (size_t)nf1 * P * d.Mc * d.Nx;
+    w.x2_elems = (size_t)ng * P * d.Mc * d.Nx;
+    // the plane API (full Nk columns, up to 11 fields) reuses these in level chunks
+    const size_t plane_min = (size_t)11 * d.Nk * d.Nx;
+    if (w.x1_elems < plane_min) w.x1_elems = plane_min;
+    const size_t plane2_min = (size_t)6 * d.Mc * d.Nx;
+    if (w.x2_elems < plane2_min) w.x2_elems = plane2_min;
+    if (dalloc(c, &w.x1, w.x1_elems) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+    if (dalloc(c, &w.x2, w.x2_elems) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) return fail(NHQG_ERR_CUDA);
+#undef UP
+  (void)rc;
+  *out = c;
+  return NHQG_OK;
+}
+
+int nhqg_ctx_destroy(nhqg_ctx* c) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  cudaDeviceSynchronize();
+  free_all(c);
+  delete c;
+  return NHQG_OK;
+}
+
+int nhqg_get_device_status(nhqg_ctx* c, int reset) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  int s = 0;
+  if (cudaMemcpy(&s, c->w.status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+  if (reset) cudaMemset(c->w.status, 0, sizeof(int));
+  return s;
+}
+
+int nhqg_last_launch_count(const nhqg_ctx* c) { return c ? c->launches : -1; }
+
+}  // extern "C"
+
+// ============================================================== orchestration
+namespace {
+
+cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
+
+int gather_state(nhqg_ctx* c, const nhqg_state* s, cudaStream_t st) {
+  const Params& p = c->p;
+  if (!s || !s->q_hat || !s->w_hat || !s->th_hat || !s->th_bar) return NHQG_ERR_BAD_ARG;
+  CK(launch_gather(p, (const double2*)s->q_hat, c->q0, p.d.P, c->w.status, st));
+  CK(launch_gather(p, (const double2*)s->w_hat, c->w0, p.d.G, c->w.status, st));
+  CK(launch_gather(p, (const double2*)s->th_hat, c->t0, p.d.G, c->w.status, st));
+  CK(cudaMemcpyAsync(c->tb0, s->th_bar, p.d.P * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  c->launches += 3;
+  return NHQG_OK;
+}
+
+int scatter_fields(nhqg_ctx* c, const double2* q, const double2* w, const double2* t,
+                   const double* tb, nhqg_state* o, cudaStream_t st) {
+  const Params& p = c->p;
+  if (!o || !o->q_hat || !o->w_hat || !o->th_hat || !o->th_bar) return NHQG_ERR_BAD_ARG;
+  CK(launch_scatter(p, q, (double2*)o->q_hat, p.d.P, st));
+  CK(launch_scatter(p, w, (double2*)o->w_hat, p.d.G, st));
+  CK(launch_scatter(p, t, (double2*)o->th_hat, p.d.G, st));
+  if (tb) {
+    CK(cudaMemcpyAsync(o->th_bar, tb, p.d.P * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  } else {
+    CK(cudaMemsetAsync(o->th_bar, 0, p.d.P * sizeof(double), st));
+  }
+  c->launches += 3;
+  return NHQG_OK;
+}
+
+int horizontal_step(nhqg_ctx* c, const double2* qn, const double2* wn, const double2* tn,
+                    cudaStream_t st) {
+  const Params& p = c->p;
+  HorizArgs a{};
+  a.form = p.advection == NHQG_ADV_JACOBIAN ? HF_JAC : HF_FLUX;
+  a.sponge = p.has_sponge;
+  a.eta = p.has_eta;
+  a.full_in = false;
+  a.full_out = false;
+  a.psi_derived = true;
+  a.levels = p.d.P;
+  a.psi = nullptr; a.q = qn; a.w = wn; a.th = tn;
+  a.Aq = c->Aq; a.Aw = c->Aw; a.Ath = c->At;
+  CK(launch_horizontal(p, c->t, c->w, a, st, &c->launches));
+  return NHQG_OK;
+}
+
+// explicit RHS at (q, w, t, tb) -> A in c->Aq/Aw/At (nodal) and, for the
+// legacy evolve_mean closure, dtb (nodal dTheta/dZ) and E_tb.
+int explicit_front(nhqg_ctx* c, const double2* q, const double2* w, const double2* t,
+                   const double* tb, bool legacy_mean, double* Etb, double* Itb, bool need_q,
+                   cudaStream_t st) {
+  const Params& p = c->p;
+  CK(launch_vfwd(p, c->t, need_q ? q : nullptr, w, t, c->Qn, c->Wn, c->Tn, st));
+  c->launches += 1;
+  if (legacy_mean) {
+    // <w theta>_xy on the padded grid equals the Parseval sum of the band-limited fields
+    CK(launch_parseval(p, c->Wn, c->Tn, p.d.P, c->flux, st));
+    CK(launch_mean_legacy_rhs(p, c->t, tb, c->flux, c->dtb, Etb, Itb, st));
+    c->launches += 2;
+  }
+  return horizontal_step(c, c->Qn, c->Wn, c->Tn, st);
+}
+
+VArgs base_vargs(nhqg_ctx* c) {
+  VArgs a{};
+  a.Aq = c->Aq; a.Aw = c->Aw; a.At = c->At;
+  a.E1q = c->E1q; a.E1w = c->E1w; a.E1t = c->E1t;
+  a.Wn = c->Wn;
+  a.Rq = c->Rq; a.Rt = c->Rt; a.rhs_w = c->rhs;
+  return a;
+}
+
+int solve_back(nhqg_ctx* c, double2* qo, double2* wo, double2* to, bool zero_mean, cudaStream_t st) {
+  const Params& p = c->p;
+  CK(launch_shell(p, c->t, c->rhs, wo, st));
+  CK(launch_vpost(p, c->t, c->Rq, c->Rt, wo, qo, to, zero_mean, st));
+  c->launches += 2;
+  return NHQG_OK;
+}
+
+// one ARS(2,2,2) step from (q0,w0,t0,tb0); result left in (q0,w0,t0,tb0)
+int one_step(nhqg_ctx* c, cudaStream_t st) {
+  const Params& p = c->p;
+  const double dt = p.dt, g = p.gamma_imex;
+  const double alpha = g * dt;
+  const double delta = -std::sqrt(2.0) / 2.0;
+  const double omega = dt * (1.0 - g);
+  const bool split = p.exchange != NHQG_EXCHANGE_LEGACY;
+  const bool evolve = p.closure == NHQG_CLOSURE_EVOLVE_MEAN;
+  const bool legacy_mean = evolve && !split;
+  const bool pc = p.exchange == NHQG_EXCHANGE_BALANCED_SBP2_PC;
+  const int base_closure = split ? NHQG_CLOSURE_FIXED_CONDUCTION : p.closure;
+  int rc;
+
+  // ---------------- stage 1
+  rc = explicit_front(c, c->q0, c->w0, c->t0, c->tb0, legacy_mean, c->E1tb, nullptr, true, st);
+  if (rc) return rc;
+  VArgs a = base_vargs(c);
+  a.q0 = c->q0; a.w0 = c->w0; a.t0 = c->t0;
+  a.dtb_nodal = legacy_mean ? c->dtb : nullptr;
+  a.alpha = alpha;
+  CK(launch_vback(p, c->t, VB_STAGE1, a, st));
+  MeanArgs m1{};
+  m1.tb0 = c->tb0; m1.E1tb = legacy_mean ? c->E1tb : nullptr; m1.out = c->tb1p;
+  m1.alpha = alpha; m1.stage = 1; m1.closure = base_closure;
+  CK(launch_mean_stage(p, c->t, m1, st));
+  c->launches += 2;
+  if ((rc = solve_back(c, c->Q1, c->W1, c->T1p, false, st))) return rc;
+
+  // stage-1 corrector (pc only)
+  const double2* t1 = c->T1p;
+  const double* tb1 = c->tb1p;
+  bool have_nodal_wt = false;
+  if (pc && evolve) {
+    CorrArgs ca{};
+    ca.wp = c->W1; ca.tp = c->T1p; ca.tbp = c->tb1p;
+    ca.t_out = c->T1; ca.tb_out = c->tb1;
+    ca.wcgl = c->Wcgl; ca.wsbp = c->Wsbp; ca.tsbp = c->Tsbp; ca.tcgl = c->Tcgl;
+    ca.total_dt = alpha;
+    CK(run_corrector(p, c->t, c->w, ca, st, &c->launches));
+    t1 = c->T1;
+    tb1 = c->tb1;
+    have_nodal_wt = true;
+  }
+
+  // ---------------- stage 2
+  if (have_nodal_wt) {
+    // nodal w and theta of state1 come out of the corrector
+    CK(launch_vfwd(p, c->t, c->Q1, nullptr, nullptr, c->Qn, nullptr, nullptr, st));
+    c->launches += 1;
+    if ((rc = horizontal_step(c, c->Qn, c->Wcgl, c->Tcgl, st))) return rc;
+  } else {
+    rc = explicit_front(c, c->Q1, c->W1, t1, tb1, legacy_mean, c->E2tb, c->Itb, true, st);
+    if (rc) return rc;
+  }
+  a = base_vargs(c);
+  a.q0 = c->q0; a.w0 = c->w0; a.t0 = c->t0;
+  a.q1 = c->Q1; a.w1 = c->W1; a.t1 = t1; a.t1p = c->T1p;
+  a.Wn = have_nodal_wt ? c->Wcgl : c->Wn;
+  a.dtb_nodal = legacy_mean ? c->dtb : nullptr;
+  a.c_E1 = dt * delta;
+  a.c_E2 = dt * (1.0 - delta);
+  a.omega = omega;
+  a.inv_alpha_c = (pc && evolve) ? 1.0 / alpha : 0.0;
+  CK(launch_vback(p, c->t, VB_STAGE2, a, st));
+  MeanArgs m2{};
+  m2.tb0 = c->tb0; m2.E1tb = legacy_mean ? c->E1tb : nullptr; m2.E2tb = legacy_mean ? c->E2tb : nullptr;
+  m2.tb1 = tb1; m2.tb1p = c->tb1p; m2.out = c->tb2p;
+  m2.c_E1 = dt * delta; m2.c_E2 = dt * (1.0 - delta); m2.omega = omega;
+  m2.inv_alpha_c = (pc && evolve) ? 1.0 / alpha : 0.0;
+  m2.stage = 2; m2.closure = base_closure; m2.itend = legacy_mean ? 1 : 0;
+  CK(launch_mean_stage(p, c->t, m2, st));
+  c->launches += 2;
+  // balanced_sbp2 (split, not pc) finalizes the base step before its corrector
+  const bool split_plain = split && !pc && evolve;
+  if ((rc = solve_back(c, c->Q2, c->W2, c->T2p, split_plain, st))) return rc;
+
+  const double2* t2 = c->T2p;
+  const double* tb2 = c->tb2p;
+  if (split && evolve) {
+    CorrArgs ca{};
+    ca.wp = c->W2; ca.tp = c->T2p; ca.tbp = c->tb2p;
+    ca.t_out = c->T2; ca.tb_out = c->tb2;
+    ca.wcgl = c->Wcgl; ca.wsbp = c->Wsbp; ca.tsbp = c->Tsbp; ca.tcgl = nullptr;
+    ca.total_dt = pc ? alpha : dt;
+    if (split_plain) {  // the base step's finalize zeroed the k=0 mode of w
+      CK(launch_zero_mode0(p, c->W2, p.d.G, st));
+      c->launches += 1;
+    }
+    CK(run_corrector(p, c->t, c->w, ca, st, &c->launches));
+    t2 = c->T2;
+    tb2 = c->tb2;
+  }
+  CK(launch_finalize(p, c->Q2, c->W2, t2, c->q0, c->w0, c->t0, st));
+  CK(cudaMemcpyAsync(c->tb0, tb2, p.d.P * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  c->launches += 1;
+  return NHQG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nhqg_step(nhqg_ctx* c, nhqg_state* s, int n_steps, void* stream) {
+  if (!c || !s || n_steps < 0) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  int rc = gather_state(c, s, st);
+  if (rc) return rc;
+  for (int i = 0; i < n_steps; ++i)
+    if ((rc = one_step(c, st))) return rc;
+  return scatter_fields(c, c->q0, c->w0, c->t0, c->tb0, s, st);
+}
+
+int nhqg_explicit_rhs(nhqg_ctx* c, const nhqg_state* in, nhqg_state* out, int closure,
+                      int exchange, void* stream) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  int rc = gather_state(c, in, st);
+  if (rc) return rc;
+  const bool legacy_mean = closure == NHQG_CLOSURE_EVOLVE_MEAN && exchange == NHQG_EXCHANGE_LEGACY;
+  if (legacy_mean && !c->t.mean_solve) return NHQG_ERR_UNSUPPORTED;
+  rc = explicit_front(c, c->q0, c->w0, c->t0, c->tb0, legacy_mean, c->E1tb, nullptr, true, st);
+  if (rc) return rc;
+  VArgs a = base_vargs(c);
+  a.q0 = c->q0; a.w0 = c->w0; a.t0 = c->t0;
+  a.dtb_nodal = legacy_mean ? c->dtb : nullptr;
+  a.Eq = c->E1q; a.Ew = c->E1w; a.Et = c->E1t;
+  CK(launch_vback(c->p, c->t, VB_RHS, a, st));
+  c->launches += 1;
+  return scatter_fields(c, c->E1q, c->E1w, c->E1t, legacy_mean ? c->E1tb : nullptr, out, st);
+}
+
+int nhqg_implicit_tendency(nhqg_ctx* c, const nhqg_state* in, nhqg_state* out, int closure,
+                           void* stream) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  int rc = gather_state(c, in, st);
+  if (rc) return rc;
+  CK(launch_itend(c->p, c->t, c->q0, c->w0, c->t0, c->Aq, c->Aw, c->At, st));
+  c->launches += 1;
+  const bool evolve = closure == NHQG_CLOSURE_EVOLVE_MEAN;
+  if (evolve) {
+    CK(launch_mean_legacy_rhs(c->p, c->t, c->tb0, nullptr, nullptr, nullptr, c->Itb, st));
+    c->launches += 1;
+  }
+  return scatter_fields(c, c->Aq, c->Aw, c->At, evolve ? c->Itb : nullptr, out, st);
+}
+
+int nhqg_implicit_solve(nhqg_ctx* c, const nhqg_state* rhs, nhqg_state* out, int closure,
+                        void* stream) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  if (closure == NHQG_CLOSURE_EVOLVE_MEAN && !c->t.mean_solve) return NHQG_ERR_UNSUPPORTED;
+  int rc = gather_state(c, rhs, st);
+  if (rc) return rc;
+  VArgs a = base_vargs(c);
+  a.q0 = c->q0; a.w0 = c->w0; a.t0 = c->t0;
+  CK(launch_vback(c->p, c->t, VB_SOLVE, a, st));
+  MeanArgs m{};
+  m.tb0 = c->tb0; m.out = c->tb1p; m.stage = 1; m.closure = closure;
+  CK(launch_mean_stage(c->p, c->t, m, st));
+  c->launches += 2;
+  if ((rc = solve_back(c, c->Q1, c->W1, c->T1p, false, st))) return rc;
+  return scatter_fields(c, c->Q1, c->W1, c->T1p, c->tb1p, out, st);
+}
+
+int nhqg_sbp2_corrector(nhqg_ctx* c, const nhqg_state* in, nhqg_state* out, double total_dt,
+                        void* stream) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  int rc = gather_state(c, in, st);
+  if (rc) return rc;
+  if (c->p.closure != NHQG_CLOSURE_EVOLVE_MEAN)
+    return scatter_fields(c, c->q0, c->w0, c->t0, c->tb0, out, st);
+  CorrArgs ca{};
+  ca.wp = c->w0; ca.tp = c->t0; ca.tbp = c->tb0;
+  ca.t_out = c->T1; ca.tb_out = c->tb1;
+  ca.wcgl = c->Wcgl; ca.wsbp = c->Wsbp; ca.tsbp = c->Tsbp; ca.tcgl = nullptr;
+  ca.total_dt = total_dt;
+  CK(run_corrector(c->p, c->t, c->w, ca, st, &c->launches));
+  return scatter_fields(c, c->q0, c->w0, c->T1, c->tb1, out, st);
+}
+
+int nhqg_sanitize(nhqg_ctx* c, nhqg_state* s, void* stream) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  int rc = gather_state(c, s, st);
+  if (rc) return rc;
+  CK(launch_hermitian(c->p, c->q0, c->w0, c->t0, st));
+  c->launches += 1;
+  return scatter_fields(c, c->q0, c->w0, c->t0, c->tb0, s, st);
+}
+
+int nhqg_mean_temp_solve(nhqg_ctx* c, const double* R, double* out, int closure, void* stream) {
+  if (!c || !R || !out) return NHQG_ERR_BAD_ARG;
+  if (closure == NHQG_CLOSURE_EVOLVE_MEAN && !c->t.mean_solve) return NHQG_ERR_UNSUPPORTED;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  MeanArgs m{};
+  m.tb0 = R; m.out = out; m.stage = 1; m.closure = closure;
+  CK(launch_mean_stage(c->p, c->t, m, st));
+  c->launches = 1;
+  return NHQG_OK;
+}
+
+int nhqg_triple_advection_23(nhqg_ctx* c, int advection, int levels, const void* psi,
+                             const void* q, const void* w, const void* th, void* Aq, void* Aw,
+                             void* Ath, void* stream) {
+  if (!c || levels <= 0 || !psi || !q || !w || !th || !Aq || !Aw || !Ath) return NHQG_ERR_BAD_ARG;
+  if (advection != NHQG_ADV_FLUX && advection != NHQG_ADV_JACOBIAN) return NHQG_ERR_UNSUPPORTED;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  const Dims& d = c->p.d;
+  const size_t plane = (size_t)d.Nx * d.Nk;
+  const int nf1 = advection == NHQG_ADV_JACOBIAN ? 8 : 5;
+  const int ng = advection == NHQG_ADV_JACOBIAN ? 3 : 6;
+  int chunk = (int)std::min(c->w.x1_elems / ((size_t)nf1 * d.Nk * d.Nx),
+                            c->w.x2_elems / ((size_t)ng * d.Mc * d.Nx));
+  if (chunk < 1) return NHQG_ERR_UNSUPPORTED;
+  CK(cudaMemsetAsync(Aq, 0, (size_t)levels * plane * sizeof(double2), st));
+  CK(cudaMemsetAsync(Aw, 0, (size_t)levels * plane * sizeof(double2), st));
+  CK(cudaMemsetAsync(Ath, 0, (size_t)levels * plane * sizeof(double2), st));
+  for (int l0 = 0; l0 < levels; l0 += chunk) {
+    const int nl = std::min(chunk, levels - l0);
+    HorizArgs a{};
+    a.form = advection == NHQG_ADV_JACOBIAN ? HF_JAC : HF_FLUX;
+    a.sponge = false; a.eta = false; a.full_in = true; a.full_out = true; a.psi_derived = false;
+    a.levels = nl;
+    const size_t off = (size_t)l0 * plane;
+    a.psi = (const double2*)psi + off; a.q = (const double2*)q + off;
+    a.w = (const double2*)w + off; a.th = (const double2*)th + off;
+    a.Aq = (double2*)Aq + off; a.Aw = (double2*)Aw + off; a.Ath = (double2*)Ath + off;
+    CK(launch_horizontal(c->p, c->t, c->w, a, st, &c->launches));
+  }
+  return NHQG_OK;
+}
+
+int nhqg_sponge_product_23(nhqg_ctx* c, int levels, const void* f, void* out, void* stream) {
+  if (!c || levels <= 0 || !f || !out) return NHQG_ERR_BAD_ARG;
+  if (!c->p.has_sponge) return NHQG_ERR_UNSUPPORTED;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  const Dims& d = c->p.d;
+  const size_t plane = (size_t)d.Nx * d.Nk;
+  int chunk = (int)std::min(c->w.x1_elems / ((size_t)d.Nk * d.Nx), c->w.x2_elems / ((size_t)d.Mc * d.Nx));
+  CK(cudaMemsetAsync(out, 0, (size_t)levels * plane * sizeof(double2), st));
+  for (int l0 = 0; l0 < levels; l0 += chunk) {
+    const int nl = std::min(chunk, levels - l0);
+    HorizArgs a{};
+    a.form = HF_SPONGE;
+    a.sponge = true; a.eta = false; a.full_in = true; a.full_out = true; a.psi_derived = false;
+    a.levels = nl;
+    const size_t off = (size_t)l0 * plane;
+    a.q = (const double2*)f + off;
+    a.Aq = (double2*)out + off; a.Aw = nullptr; a.Ath = nullptr;
+    CK(launch_horizontal(c->p, c->t, c->w, a, st, &c->launches));
+  }
+  return NHQG_OK;
+}
+
+}  // extern "C"

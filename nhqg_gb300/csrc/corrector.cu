@@ -1,0 +1,525 @@
+// Balanced SBP2 thermal corrector and the 1-D mean-temperature kernels.
+//
+// Reference: _apply_balanced_sbp2_corrector nhqg/solver.py:909-950 with the
+// per-substep update :873-906 and the SBP exchange fields :346-358.
+//
+// Per substep the reference maps theta back to Galerkin coefficients
+// (pinv(proj(V^-1 s2c theta_sbp))) and forward again (c2s V S theta_hat).
+// S pinv = proj_dir on any coefficient vector, so the round trip is
+//   theta_cgl' = y + V[:,N-1] (F0 . y) + V[:,N] (F1 . y),  y = s2c theta_sbp
+// with F = (proj_dir - I)[N-1:N+1, :] V^-1 -- a rank-2 correction instead of
+// two dense transforms.  Only the last substep returns to coefficients.
+// The 1-D system A = I - half (pentadiagonal: D1 diag(<w^2>) D1 and the SBP
+// Laplacian) is factored once per corrector without pivoting: it is the
+// identity plus a weakly diagonally dominant M-matrix-like term.
+#include "engine.h"
+
+namespace nhqg {
+
+namespace {
+
+constexpr int TM = 8;
+constexpr int NT = 256;
+
+// offsets inside Work::vec (doubles), each block P long unless noted
+struct CV {
+  int P;
+  __host__ __device__ int w2() const { return 0; }
+  __host__ __device__ int flux() const { return P; }
+  __host__ __device__ int tb_sbp() const { return 2 * P; }
+  __host__ __device__ int g_half() const { return 3 * P; }
+  __host__ __device__ int tmp() const { return 4 * P; }
+  __host__ __device__ int tmp2() const { return 5 * P; }
+  __host__ __device__ int Aband() const { return 6 * P; }   // 5P: diag offsets -2..2
+  __host__ __device__ int Bband() const { return 11 * P; }  // 5P
+  __host__ __device__ int dtb() const { return 16 * P; }    // legacy dTheta/dZ nodal
+  __host__ __device__ int Etb1() const { return 17 * P; }
+  __host__ __device__ int Etb2() const { return 18 * P; }
+  __host__ __device__ int Itb() const { return 19 * P; }
+  __host__ __device__ int fluxn() const { return 20 * P; }
+  __host__ __device__ int total() const { return 21 * P; }
+};
+
+struct CK {
+  int P, G, N, M;
+  bool mixed;
+  const double *wa, *wb;
+  const double *V, *Vinv;
+  const int *c2s_ptr, *c2s_col, *s2c_ptr, *s2c_col;
+  const double *c2s_val, *s2c_val;
+  const double *bcF, *bcV, *proj, *D1, *Lsbp;
+  double mu, kappa;
+};
+
+CK make_ck(const Params& p, const Tables& t) {
+  CK k;
+  k.P = p.d.P; k.G = p.d.G; k.N = p.d.Nz; k.M = p.d.M;
+  k.mixed = t.wst_a != nullptr;
+  k.wa = t.wst_a; k.wb = t.wst_b;
+  k.V = t.V; k.Vinv = t.Vinv;
+  k.c2s_ptr = t.c2s_ptr; k.c2s_col = t.c2s_col; k.c2s_val = t.c2s_val;
+  k.s2c_ptr = t.s2c_ptr; k.s2c_col = t.s2c_col; k.s2c_val = t.s2c_val;
+  k.bcF = t.bcF; k.bcV = t.bcV; k.proj = t.proj; k.D1 = t.D1; k.Lsbp = t.Lsbp;
+  k.mu = p.eps_sq;
+  k.kappa = 1.0 / p.sigma;
+  return k;
+}
+
+__device__ __forceinline__ void tload(double2* b, const double2* __restrict__ src, int nlev,
+                                      int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    b[i] = (m < M) ? src[(size_t)l * M + m] : czero();
+  }
+}
+__device__ __forceinline__ void tstore(const double2* b, double2* __restrict__ dst, int nlev,
+                                       int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    if (m < M) dst[(size_t)l * M + m] = b[i];
+  }
+}
+__device__ __forceinline__ void tmat(double2* out, const double2* in, const double* __restrict__ Mat,
+                                     int ld, int nout, int nin) {
+  for (int idx = threadIdx.x; idx < nout * TM; idx += blockDim.x) {
+    const int i = idx / TM, mm = idx - i * TM;
+    const double* row = Mat + (size_t)i * ld;
+    double ax = 0.0, ay = 0.0;
+    for (int j = 0; j < nin; ++j) {
+      const double v = __ldg(row + j);
+      const double2 x = in[j * TM + mm];
+      ax = fma(v, x.x, ax);
+      ay = fma(v, x.y, ay);
+    }
+    out[idx] = make_double2(ax, ay);
+  }
+}
+__device__ __forceinline__ void tcsr(double2* out, const double2* in, const int* __restrict__ ptr,
+                                     const int* __restrict__ col, const double* __restrict__ val,
+                                     int nrow) {
+  for (int idx = threadIdx.x; idx < nrow * TM; idx += blockDim.x) {
+    const int i = idx / TM, mm = idx - i * TM;
+    double ax = 0.0, ay = 0.0;
+    for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+      const double v = val[q];
+      const double2 x = in[col[q] * TM + mm];
+      ax = fma(v, x.x, ax);
+      ay = fma(v, x.y, ay);
+    }
+    out[idx] = make_double2(ax, ay);
+  }
+}
+__device__ __forceinline__ void tstencil(const CK& k, bool wbasis, double2* c, const double2* x) {
+  const bool mixed = wbasis && k.mixed;
+  for (int idx = threadIdx.x; idx < k.P * TM; idx += blockDim.x) {
+    const int n = idx / TM, mm = idx - n * TM;
+    double2 v;
+    if (!mixed) {
+      v = (n < k.G) ? cneg(x[n * TM + mm]) : czero();
+      if (n >= 2 && n - 2 < k.G) v = cadd(v, x[(n - 2) * TM + mm]);
+    } else {
+      v = (n < k.G) ? x[n * TM + mm] : czero();
+      if (n >= 1 && n - 1 < k.G) v = caxpy(__ldg(k.wa + n - 1), x[(n - 1) * TM + mm], v);
+      if (n >= 2 && n - 2 < k.G) v = caxpy(__ldg(k.wb + n - 2), x[(n - 2) * TM + mm], v);
+    }
+    c[idx] = v;
+  }
+}
+__device__ __forceinline__ void tpinv_dir(double2* x, const double2* c, int G) {
+  const int t = threadIdx.x;
+  if (t < 2 * TM) {
+    const int mm = t >> 1;
+    const bool im = t & 1;
+    double xm2 = 0.0, xm1 = 0.0;
+    for (int n = 0; n < G; ++n) {
+      const double cv = im ? c[n * TM + mm].y : c[n * TM + mm].x;
+      const double xn = xm2 - cv;
+      if (im) x[n * TM + mm].y = xn; else x[n * TM + mm].x = xn;
+      xm2 = xm1;
+      xm1 = xn;
+    }
+  }
+}
+
+// ------------------------------------------------------------ per-mode kernels
+__global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const double2* tp,
+                                                 double2* wcgl, double2* wsbp, double2* tsbp) {
+  extern __shared__ double2 sm[];
+  const int PT = k.P * TM;
+  double2 *b0 = sm, *b1 = sm + PT;
+  const int m0 = blockIdx.x * TM;
+  tload(b0, wp, k.G, m0, k.M);
+  __syncthreads();
+  tstencil(k, true, b1, b0);
+  __syncthreads();
+  tmat(b0, b1, k.V, k.P, k.P, k.P);
+  __syncthreads();
+  tstore(b0, wcgl, k.P, m0, k.M);
+  tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
+  __syncthreads();
+  tstore(b1, wsbp, k.P, m0, k.M);
+  __syncthreads();
+  tload(b0, tp, k.G, m0, k.M);
+  __syncthreads();
+  tstencil(k, false, b1, b0);
+  __syncthreads();
+  tmat(b0, b1, k.V, k.P, k.P, k.P);
+  __syncthreads();
+  tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
+  __syncthreads();
+  tstore(b1, tsbp, k.P, m0, k.M);
+}
+
+__global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const double2* wsbp,
+                                                 const double* g_half, double sub_dt, int last,
+                                                 double2* t_out, double2* tcgl) {
+  extern __shared__ double2 sm[];
+  const int PT = k.P * TM;
+  double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT;
+  __shared__ double2 delta[2 * TM];
+  const int m0 = blockIdx.x * TM;
+  const int P = k.P;
+  tload(b0, tsbp, P, m0, k.M);
+  tload(b1, wsbp, P, m0, k.M);
+  __syncthreads();
+  for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+    const int l = i / TM;
+    b0[i] = (l == 0 || l == P - 1) ? czero() : caxpy(-sub_dt * g_half[l], b1[i], b0[i]);
+  }
+  __syncthreads();
+  tcsr(b2, b0, k.s2c_ptr, k.s2c_col, k.s2c_val, P);  // y = s2c theta_sbp_new
+  __syncthreads();
+  if (!last || tcgl != nullptr) {
+    if (threadIdx.x < 4 * TM) {  // delta_j = F_j . y  (j = 0, 1; re/im)
+      const int mm = threadIdx.x % TM, j = (threadIdx.x / TM) & 1, im = threadIdx.x / (2 * TM);
+      const double* F = k.bcF + j * P;
+      double acc = 0.0;
+      for (int l = 0; l < P; ++l) acc = fma(F[l], im ? b2[l * TM + mm].y : b2[l * TM + mm].x, acc);
+      if (im) delta[j * TM + mm].y = acc; else delta[j * TM + mm].x = acc;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+      const int l = i / TM, mm = i - l * TM;
+      double2 v = caxpy(k.bcV[l], delta[mm], b2[i]);
+      b3[i] = caxpy(k.bcV[P + l], delta[TM + mm], v);
+    }
+    __syncthreads();
+    if (!last) {
+      tcsr(b1, b3, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
+      __syncthreads();
+      tstore(b1, tsbp, P, m0, k.M);
+    } else {
+      tstore(b3, tcgl, P, m0, k.M);
+    }
+  }
+  if (last) {
+    __syncthreads();
+    tmat(b0, b2, k.Vinv, P, k.G, P);  // first G Chebyshev coefficients of V^-1 y
+    __syncthreads();
+    tpinv_dir(b1, b0, k.G);
+    __syncthreads();
+    tstore(b1, t_out, k.G, m0, k.M);
+  }
+}
+
+// ------------------------------------------------------------ 1-D kernels (one CTA)
+__device__ void vec_dense(double* out, const double* in, const double* Mat, int n, int ld, int ncol) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double* row = Mat + (size_t)i * ld;
+    double acc = 0.0;
+    for (int j = 0; j < ncol; ++j) acc = fma(row[j], in[j], acc);
+    out[i] = acc;
+  }
+}
+__device__ void vec_csr(double* out, const double* in, const int* ptr, const int* col,
+                        const double* val, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double acc = 0.0;
+    for (int q = ptr[i]; q < ptr[i + 1]; ++q) acc = fma(val[q], in[col[q]], acc);
+    out[i] = acc;
+  }
+}
+// pentadiagonal matrix stored as band[d*P + i] = A[i, i+d-2]
+__device__ void band_matvec(double* out, const double* band, const double* x, int P) {
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    double acc = 0.0;
+    for (int d = 0; d < 5; ++d) {
+      const int j = i + d - 2;
+      if (j >= 0 && j < P) acc = fma(band[d * P + i], x[j], acc);
+    }
+    out[i] = acc;
+  }
+}
+// D1 (tridiagonal) product
+__device__ void d1_matvec(double* out, const double* D1, const double* x, int P) {
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    double acc = 0.0;
+    for (int j = max(0, i - 1); j <= min(P - 1, i + 1); ++j) acc = fma(D1[(size_t)i * P + j], x[j], acc);
+    out[i] = acc;
+  }
+}
+
+__global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt) {
+  const CV cv{k.P};
+  const int P = k.P;
+  double* w2 = vec + cv.w2();
+  double* A = vec + cv.Aband();
+  double* B = vec + cv.Bband();
+  const double c1 = 0.5 * k.mu * k.kappa * sub_dt;
+  const double c2 = 0.25 * k.mu * (sub_dt * sub_dt);
+  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) {
+    const int d = idx / P, i = idx - d * P;
+    const int j = i + d - 2;
+    double h = 0.0, a = 0.0, b = 0.0;
+    if (j >= 0 && j < P) {
+      double dmd = 0.0;  // (D1 diag(w2) D1)[i, j]
+      for (int kk = max(0, i - 1); kk <= min(P - 1, i + 1); ++kk) {
+        if (abs(kk - j) <= 1) dmd = fma(k.D1[(size_t)i * P + kk] * w2[kk], k.D1[(size_t)kk * P + j], dmd);
+      }
+      h = fma(c1, k.Lsbp[(size_t)i * P + j], c2 * dmd);
+      const double id = (i == j) ? 1.0 : 0.0;
+      a = id - h;
+      b = id + h;
+      if (i == 0 || i == P - 1) a = id;
+    }
+    A[idx] = a;
+    B[idx] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // banded LU without pivoting, in place (multipliers below the diagonal)
+    for (int col = 0; col < P; ++col) {
+      const double piv = A[2 * P + col];
+      for (int r = col + 1; r <= min(P - 1, col + 2); ++r) {
+        const int dr = col - r + 2;  // band slot of A[r, col]
+        const double l = A[dr * P + r] / piv;
+        A[dr * P + r] = l;
+        for (int c = col + 1; c <= min(P - 1, col + 2); ++c) {
+          const int drc = c - r + 2;
+          const int dcc = c - col + 2;
+          A[drc * P + r] = fma(-l, A[dcc * P + col], A[drc * P + r]);
+        }
+      }
+    }
+  }
+  // tb_sbp = c2s (V tbp)
+  double* tmp = vec + cv.tmp();
+  vec_dense(tmp, tbp, k.V, P, P, P);
+  __syncthreads();
+  vec_csr(vec + cv.tb_sbp(), tmp, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
+}
+
+__global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, double* tb_out) {
+  const CV cv{k.P};
+  const int P = k.P, N = k.N;
+  __shared__ double red[64];
+  double* flux = vec + cv.flux();
+  double* tbs = vec + cv.tb_sbp();
+  double* gh = vec + cv.g_half();
+  double* rhs = vec + cv.tmp();
+  double* t2 = vec + cv.tmp2();
+  const double* A = vec + cv.Aband();
+  const double* B = vec + cv.Bband();
+  // rhs = B tb_sbp - mu sub_dt D1 flux
+  band_matvec(rhs, B, tbs, P);
+  d1_matvec(t2, k.D1, flux, P);
+  __syncthreads();
+  const double cf = k.mu * sub_dt;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) rhs[i] = (i == 0 || i == P - 1) ? 0.0 : fma(-cf, t2[i], rhs[i]);
+  __syncthreads();
+  if (threadIdx.x == 0) {  // forward / back substitution
+    for (int i = 1; i < P; ++i) {
+      double v = rhs[i];
+      for (int c = max(0, i - 2); c < i; ++c) v = fma(-A[(c - i + 2) * P + i], rhs[c], v);
+      rhs[i] = v;
+    }
+    for (int i = P - 1; i >= 0; --i) {
+      double v = rhs[i];
+      for (int c = i + 1; c <= min(P - 1, i + 2); ++c) v = fma(-A[(c - i + 2) * P + i], rhs[c], v);
+      rhs[i] = v / A[2 * P + i];
+    }
+  }
+  __syncthreads();  // rhs = tb_new
+  for (int i = threadIdx.x; i < P; i += blockDim.x) t2[i] = tbs[i] + rhs[i];
+  __syncthreads();
+  d1_matvec(gh, k.D1, t2, P);
+  __syncthreads();
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    gh[i] *= 0.5;
+    if (i == 0 || i == P - 1) rhs[i] = 0.0;
+  }
+  __syncthreads();
+  vec_csr(t2, rhs, k.s2c_ptr, k.s2c_col, k.s2c_val, P);  // y = s2c tb_new
+  __syncthreads();
+  if (!last) {
+    double a0 = 0.0, a1 = 0.0;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      a0 = fma(k.bcF[i], t2[i], a0);
+      a1 = fma(k.bcF[P + i], t2[i], a1);
+    }
+    const double d0 = block_sum(a0, red);
+    const double d1 = block_sum(a1, red + 32);
+    if (threadIdx.x == 0) { red[0] = d0; red[1] = d1; }
+    __syncthreads();
+    const double e0 = red[0], e1 = red[1];
+    for (int i = threadIdx.x; i < P; i += blockDim.x)
+      rhs[i] = fma(k.bcV[P + i], e1, fma(k.bcV[i], e0, t2[i]));
+    __syncthreads();
+    vec_csr(tbs, rhs, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
+  } else {
+    vec_dense(rhs, t2, k.Vinv, P, P, P);  // Chebyshev coefficients
+    __syncthreads();
+    // tau projection: keep a_0..a_{N-2}, rewrite a_{N-1}, a_N
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      if (i < N - 1) {
+        tb_out[i] = rhs[i];
+      } else {
+        const double* row = k.proj + (size_t)i * P;
+        double acc = 0.0;
+        for (int j = 0; j < N - 1; ++j) acc = fma(row[j], rhs[j], acc);
+        tb_out[i] = acc;
+      }
+    }
+  }
+}
+
+// ---- mean-temperature stage update: R = combos; out = solve(R)
+struct MK {
+  int P, N;
+  const double *proj, *mean_solve, *GZ2;
+  double eps_sq, sigma;
+};
+
+__global__ void k_mean_stage(MK k, MeanArgs a) {
+  __shared__ double R[1024];
+  const int P = k.P, N = k.N;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    double r = a.tb0[i];
+    if (a.stage == 1) {
+      if (a.E1tb) r = fma(a.alpha, a.E1tb[i], r);
+    } else {
+      if (a.E1tb) r = fma(a.c_E1, a.E1tb[i], r);
+      if (a.E2tb) r = fma(a.c_E2, a.E2tb[i], r);
+      if (a.itend) {  // omega * (eps^2/sigma) G_Z2 tb1
+        const double* row = k.GZ2 + (size_t)i * P;
+        double acc = 0.0;
+        for (int j = 0; j < P; ++j) acc = fma(row[j], a.tb1[j], acc);
+        r = fma(a.omega * (k.eps_sq / k.sigma), acc, r);
+      }
+      if (a.inv_alpha_c != 0.0) r = fma(a.omega * a.inv_alpha_c, a.tb1[i] - a.tb1p[i], r);
+    }
+    R[i] = r;
+  }
+  __syncthreads();
+  if (a.closure == NHQG_CLOSURE_EVOLVE_MEAN) {  // legacy implicit 1-D solve with tau rows
+    if (threadIdx.x == 0) { R[N - 1] = 0.0; R[N] = 0.0; }
+    __syncthreads();
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      const double* row = k.mean_solve + (size_t)i * P;
+      double acc = 0.0;
+      for (int j = 0; j < P; ++j) acc = fma(row[j], R[j], acc);
+      a.out[i] = acc;
+    }
+  } else {  // Dirichlet tau projection
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      if (i < N - 1) {
+        a.out[i] = R[i];
+      } else {
+        const double* row = k.proj + (size_t)i * P;
+        double acc = 0.0;
+        for (int j = 0; j < N - 1; ++j) acc = fma(row[j], R[j], acc);
+        a.out[i] = acc;
+      }
+    }
+  }
+}
+
+// legacy evolve_mean explicit pieces: dtb_nodal = V (G_Z tb);
+// E_tb = -eps^2 G_Z (V^-1 flux_nodal); I_tb = (eps^2/sigma) G_Z2 tb
+struct LK {
+  int P;
+  const double *V, *Vinv, *GZ, *GZ2;
+  double eps_sq, sigma;
+};
+__global__ void k_mean_legacy(LK k, const double* tb, const double* flux, double* dtb, double* Etb,
+                              double* Itb) {
+  __shared__ double t1[1024], t2[1024];
+  const int P = k.P;
+  if (dtb) {
+    vec_dense(t1, tb, k.GZ, P, P, P);
+    __syncthreads();
+    vec_dense(dtb, t1, k.V, P, P, P);
+    __syncthreads();
+  }
+  if (Etb) {
+    vec_dense(t2, flux, k.Vinv, P, P, P);
+    __syncthreads();
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      const double* row = k.GZ + (size_t)i * P;
+      double acc = 0.0;
+      for (int j = 0; j < P; ++j) acc = fma(row[j], t2[j], acc);
+      Etb[i] = k.eps_sq * (-acc);
+    }
+  }
+  if (Itb) {
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      const double* row = k.GZ2 + (size_t)i * P;
+      double acc = 0.0;
+      for (int j = 0; j < P; ++j) acc = fma(row[j], tb[j], acc);
+      Itb[i] = (k.eps_sq / k.sigma) * acc;
+    }
+  }
+}
+
+}  // namespace
+
+size_t corrector_vec_doubles(int P) { return (size_t)CV{P}.total(); }
+
+cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrArgs& a,
+                          cudaStream_t st, int* nlaunch) {
+  CK k = make_ck(p, t);
+  const CV cv{p.d.P};
+  const int nsub = p.substeps > 0 ? p.substeps : 1;
+  const double sub_dt = a.total_dt / nsub;
+  const int grid = (p.d.M + TM - 1) / TM;
+  const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2);
+  const size_t sm4 = 4 * (size_t)p.d.P * TM * sizeof(double2);
+  cudaFuncSetAttribute(k_corr_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  cudaFuncSetAttribute(k_corr_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+  k_corr_pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp);
+  launch_parseval(p, a.wsbp, a.wsbp, p.d.P, w.vec + cv.w2(), st);
+  launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), st);
+  k_corr_init<<<1, NT, 0, st>>>(k, w.vec, a.tbp, sub_dt);
+  int n = 4;
+  for (int s = 0; s < nsub; ++s) {
+    const int last = (s == nsub - 1);
+    if (s > 0) { launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), st); ++n; }
+    k_corr_tstep<<<1, NT, 0, st>>>(k, w.vec, sub_dt, last, a.tb_out);
+    k_corr_sub<<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt, last,
+                                      a.t_out, a.tcgl);
+    n += 2;
+  }
+  if (nlaunch) *nlaunch += n;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mean_stage(const Params& p, const Tables& t, const MeanArgs& a, cudaStream_t st) {
+  MK k;
+  k.P = p.d.P; k.N = p.d.Nz;
+  k.proj = t.proj; k.mean_solve = t.mean_solve; k.GZ2 = t.GZ2;
+  k.eps_sq = p.eps_sq; k.sigma = p.sigma;
+  if (a.closure == NHQG_CLOSURE_EVOLVE_MEAN && t.mean_solve == nullptr) return cudaErrorInvalidValue;
+  k_mean_stage<<<1, NT, 0, st>>>(k, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mean_legacy_rhs(const Params& p, const Tables& t, const double* tb,
+                                   const double* flux_nodal, double* dtb_nodal, double* E_tb,
+                                   double* I_tb, cudaStream_t st) {
+  LK k;
+  k.P = p.d.P; k.V = t.V; k.Vinv = t.Vinv; k.GZ = t.GZ; k.GZ2 = t.GZ2;
+  k.eps_sq = p.eps_sq; k.sigma = p.sigma;
+  k_mean_legacy<<<1, NT, 0, st>>>(k, tb, flux_nodal, dtb_nodal, E_tb, I_tb);
+  return cudaGetLastError();
+}
+
+}  // namespace nhqg

@@ -1,0 +1,163 @@
+// Internal engine interface: device tables, work buffers, kernel launchers.
+#pragma once
+#include <cuda_runtime.h>
+#include <vector>
+
+#include "common.cuh"
+#include "fft.cuh"
+#include "nhqg_gpu.h"
+
+namespace nhqg {
+
+// bits of the device status word
+constexpr int NHQG_STATUS_BIT_OOB = 0;      // input content outside the 2/3 band
+constexpr int NHQG_STATUS_BIT_TIMEOUT = 1;  // a bounded device wait ran out
+
+// Device-resident tables, uploaded once by nhqg_ctx_create.
+struct Tables {
+  // per compact mode [M]
+  double *kx = nullptr, *ky = nullptr, *inv_denom = nullptr;
+  double *inv_aq = nullptr, *inv_at = nullptr, *drq = nullptr, *drw = nullptr, *drt = nullptr;
+  double2* eta = nullptr;  // [M] or null
+  // full-layout wavenumbers for the plane API
+  double *kx_full = nullptr, *ky_full = nullptr;  // [Nx], [Nk]
+  double *inv_denom_full = nullptr;               // [Nx*Nk]
+  // physical-space fields [Nx*Nx]
+  double *sponge = nullptr, *eta_phys = nullptr;
+  // FFT over Nx
+  double2* tw = nullptr;  // [Nx]
+  int* perm = nullptr;    // [Nx]
+  // vertical operators
+  double *V = nullptr, *Vinv = nullptr;        // [P*P]
+  double *wst_a = nullptr, *wst_b = nullptr;   // mixed w stencil a_n, b_n [G]; null = Dirichlet
+  int *c2s_ptr = nullptr, *c2s_col = nullptr;
+  double* c2s_val = nullptr;
+  int *s2c_ptr = nullptr, *s2c_col = nullptr;
+  double* s2c_val = nullptr;
+  double* bcF = nullptr;    // [2*P] rows N-1, N of (proj_dir - I) V_inv
+  double* bcV = nullptr;    // [2*P] columns N-1, N of V
+  double* proj = nullptr;   // [P*P] proj_dirichlet
+  double* D1 = nullptr;     // [P*P] SBP first derivative
+  double* Lsbp = nullptr;   // [P*P] SBP Laplacian
+  double* GZ = nullptr;     // [P*P]
+  double* GZ2 = nullptr;    // [P*P]
+  double* mean_solve = nullptr;  // [P*P] or null
+  double* c2s_d = nullptr;  // [P*P] dense (1-D vectors)
+  double* s2c_d = nullptr;  // [P*P]
+  // shells
+  double* shell_inv = nullptr;  // [n_shells*G*G]
+  int* shell_start = nullptr;   // [n_shells+1]
+  int* shell_modes = nullptr;   // [M]
+  int n_shells = 0;
+  int max_shell_modes = 0;
+};
+
+struct Params {
+  Dims d;
+  FftPlan plan;
+  int advection, closure, exchange, wbc, substeps;
+  double dt, gamma_imex, Ra_sigma, sigma, beta, eps_sq;
+  bool has_eta, has_sponge;
+};
+
+// Horizontal product launch description.
+enum HForm { HF_FLUX = 0, HF_JAC = 1, HF_SPONGE = 2 };
+
+struct HorizArgs {
+  int form;            // HForm
+  bool sponge;         // add sigma*f terms (flux/jac forms)
+  bool eta;            // q_adv = q + eta (step engine)
+  bool full_in;        // inputs are full (Nx, Nk) planes, else compact
+  bool full_out;       // outputs are full planes (in-band written), else compact
+  bool psi_derived;    // psi = -inv_denom * q (step engine) else read psi
+  int levels;
+  const double2 *psi, *q, *w, *th;  // planes [level][plane]
+  double2 *Aq, *Aw, *Ath;
+};
+
+struct Work {
+  // H1 / H2 intermediates
+  double2* x1 = nullptr;  size_t x1_elems = 0;
+  double2* x2 = nullptr;  size_t x2_elems = 0;
+  // compact fields [P*M] each
+  std::vector<double2*> f;
+  // small vectors
+  double* vec = nullptr;       // assorted 1-D vectors (see corrector.cu)
+  double* partials = nullptr;  // reductions
+  int* status = nullptr;       // device status word
+};
+
+// ---- launchers (return cudaError_t of the last launch) ----
+cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const HorizArgs& a,
+                              cudaStream_t st, int* nlaunch);
+
+// vertical / column engine
+enum VBackMode { VB_RHS = 0, VB_STAGE1 = 1, VB_STAGE2 = 2, VB_SOLVE = 3 };
+struct VArgs {
+  // state the step started from (y_n) and stage-1 state (s1); predictor theta
+  const double2 *q0, *w0, *t0;
+  const double2 *q1, *w1, *t1, *t1p;
+  // explicit operands (nodal A) and stored E1
+  const double2 *Aq, *Aw, *At;
+  double2 *E1q, *E1w, *E1t;
+  // nodal w (legacy exchange product), dtb nodal vector
+  const double2* Wn;
+  const double* dtb_nodal;  // [P] or null
+  // outputs
+  double2 *Rq, *Rt, *rhs_w;
+  // RHS-only outputs
+  double2 *Eq, *Ew, *Et;
+  double alpha;       // gamma*dt (stage 1)
+  double c_E1, c_E2;  // dt*delta, dt*(1-delta)
+  double omega;       // dt*(1-gamma)
+  double inv_alpha_c; // 1/alpha for the corrector tendency (0 = none)
+};
+cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, const double2* w,
+                        const double2* th, double2* qn, double2* wn, double2* tn, cudaStream_t st);
+cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st);
+cudaError_t launch_shell(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
+                         cudaStream_t st);
+cudaError_t launch_vpost(const Params& p, const Tables& t, const double2* Rq, const double2* Rt,
+                         const double2* w_new, double2* q_out, double2* t_out, bool zero_mean,
+                         cudaStream_t st);
+size_t corrector_vec_doubles(int P);
+cudaError_t launch_itend(const Params& p, const Tables& t, const double2* q, const double2* w,
+                         const double2* th, double2* Iq, double2* Iw, double2* It, cudaStream_t st);
+cudaError_t launch_gather(const Params& p, const double2* full, double2* compact, int levels,
+                          int* status, cudaStream_t st);
+cudaError_t launch_scatter(const Params& p, const double2* compact, double2* full, int levels,
+                           cudaStream_t st);
+cudaError_t launch_finalize(const Params& p, const double2* q, const double2* w, const double2* th,
+                            double2* qo, double2* wo, double2* to, cudaStream_t st);
+cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
+                            double* out, cudaStream_t st);
+cudaError_t launch_hermitian(const Params& p, double2* q, double2* w, double2* th, cudaStream_t st);
+cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStream_t st);
+
+// 1-D mean-temperature kernels (single CTA)
+struct MeanArgs {
+  const double *tb0, *E1tb, *E2tb, *tb1, *tb1p;
+  double* out;
+  double alpha, c_E1, c_E2, omega, inv_alpha_c;
+  int stage;     // 1 or 2
+  int closure;   // solve flavour
+  int itend;     // add omega * I(tb1) (stage 2)
+};
+cudaError_t launch_mean_stage(const Params& p, const Tables& t, const MeanArgs& a, cudaStream_t st);
+cudaError_t launch_mean_legacy_rhs(const Params& p, const Tables& t, const double* tb,
+                                   const double* flux_nodal, double* dtb_nodal, double* E_tb,
+                                   double* I_tb, cudaStream_t st);
+
+// SBP2 corrector
+struct CorrArgs {
+  const double2 *wp, *tp;  // predictor w, theta (Galerkin)
+  const double* tbp;       // predictor th_bar
+  double2* t_out;          // corrected theta
+  double* tb_out;          // corrected th_bar
+  double2 *wcgl, *wsbp, *tsbp, *tcgl;  // work; tcgl may be null
+  double total_dt;
+};
+cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrArgs& a,
+                          cudaStream_t st, int* nlaunch);
+
+}  // namespace nhqg

@@ -1,0 +1,159 @@
+// Batched in-place complex FFTs in shared memory, FP64, lengths 2^a 3^b.
+//
+// Forward transforms run decimation-in-frequency (natural order in,
+// mixed-radix digit-reversed order out); inverse transforms run the exact
+// transpose, decimation-in-time (digit-reversed in, natural out, unscaled).
+// Keeping the digit-reversed order in shared memory lets every butterfly read
+// and write the same R locations, so a pass needs no second buffer; callers
+// address the reversed side through the permutation table perm[k] = position
+// of frequency k.  Radix-4 passes first, then radix-2, then radix-3: the
+// radix-4 butterfly costs 16 DADD + 3 twiddle products (12 FP64 ops) per 4
+// points, the cheapest of the three on the FP64 pipe.
+#pragma once
+#include "common.cuh"
+
+namespace nhqg {
+
+struct FftPlan {
+  int n;
+  int npass;
+  int radix[12];
+};
+
+inline FftPlan make_fft_plan(int n) {
+  FftPlan p{};
+  p.n = n;
+  int m = n;
+  while (m % 4 == 0 && m > 1) { p.radix[p.npass++] = 4; m /= 4; }
+  while (m % 2 == 0 && m > 1) { p.radix[p.npass++] = 2; m /= 2; }
+  while (m % 3 == 0 && m > 1) { p.radix[p.npass++] = 3; m /= 3; }
+  if (m != 1) p.npass = -1;  // unsupported length
+  return p;
+}
+
+// position of frequency k in the digit-reversed output of fft_dif_fwd
+inline void make_fft_perm(const FftPlan& p, int* perm) {
+  for (int k = 0; k < p.n; ++k) {
+    int L = p.n, kk = k, pos = 0;
+    for (int q = 0; q < p.npass; ++q) {
+      const int R = p.radix[q];
+      const int Ls = L / R;
+      pos += (kk % R) * Ls;
+      kk /= R;
+      L = Ls;
+    }
+    perm[k] = pos;
+  }
+}
+
+constexpr double kSqrt3Half = 0.86602540378443864676;
+
+// Forward DFT (sign -1), natural -> reversed.  tw[k] = exp(-2 pi i k / n).
+__device__ __forceinline__ void fft_dif_fwd(double2* __restrict__ data, int nseq, int stride,
+                                            const FftPlan& pl, const double2* __restrict__ tw) {
+  int L = pl.n;
+  for (int q = 0; q < pl.npass; ++q) {
+    const int R = pl.radix[q];
+    const int Ls = L / R;
+    const int nb = pl.n / R;
+    const int tws = pl.n / L;
+    for (int idx = threadIdx.x; idx < nseq * nb; idx += blockDim.x) {
+      const int s = idx / nb, b = idx - s * nb;
+      const int blk = b / Ls, j = b - blk * Ls;
+      double2* a = data + s * stride + blk * L + j;
+      if (R == 4) {
+        const double2 x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
+        const double2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = csub(x1, x3);
+        double2 y1 = make_double2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+        double2 y2 = csub(t0, t2);
+        double2 y3 = make_double2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
+        a[0] = cadd(t0, t2);
+        if (j != 0) {
+          y1 = cmul(y1, tw[j * tws]);
+          y2 = cmul(y2, tw[2 * j * tws]);
+          y3 = cmul(y3, tw[3 * j * tws]);
+        }
+        a[Ls] = y1;
+        a[2 * Ls] = y2;
+        a[3 * Ls] = y3;
+      } else if (R == 2) {
+        const double2 x0 = a[0], x1 = a[Ls];
+        double2 y1 = csub(x0, x1);
+        a[0] = cadd(x0, x1);
+        if (j != 0) y1 = cmul(y1, tw[j * tws]);
+        a[Ls] = y1;
+      } else {  // R == 3
+        const double2 x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls];
+        const double2 sp = cadd(x1, x2);
+        const double2 d = cscale(csub(x1, x2), kSqrt3Half);
+        const double2 m = caxpy(-0.5, sp, x0);
+        double2 y1 = make_double2(m.x + d.y, m.y - d.x);  // m - i d
+        double2 y2 = make_double2(m.x - d.y, m.y + d.x);  // m + i d
+        a[0] = cadd(x0, sp);
+        if (j != 0) {
+          y1 = cmul(y1, tw[j * tws]);
+          y2 = cmul(y2, tw[2 * j * tws]);
+        }
+        a[Ls] = y1;
+        a[2 * Ls] = y2;
+      }
+    }
+    __syncthreads();
+    L = Ls;
+  }
+}
+
+// Inverse DFT (sign +1, unscaled), reversed -> natural.
+__device__ __forceinline__ void fft_dit_inv(double2* __restrict__ data, int nseq, int stride,
+                                            const FftPlan& pl, const double2* __restrict__ tw) {
+  int Ls_of[12];
+  {
+    int L = pl.n;
+    for (int q = 0; q < pl.npass; ++q) { Ls_of[q] = L; L /= pl.radix[q]; }
+  }
+  for (int q = pl.npass - 1; q >= 0; --q) {
+    const int R = pl.radix[q];
+    const int L = Ls_of[q];
+    const int Ls = L / R;
+    const int nb = pl.n / R;
+    const int tws = pl.n / L;
+    for (int idx = threadIdx.x; idx < nseq * nb; idx += blockDim.x) {
+      const int s = idx / nb, b = idx - s * nb;
+      const int blk = b / Ls, j = b - blk * Ls;
+      double2* a = data + s * stride + blk * L + j;
+      if (R == 4) {
+        double2 x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
+        if (j != 0) {
+          x1 = cmulc(x1, tw[j * tws]);
+          x2 = cmulc(x2, tw[2 * j * tws]);
+          x3 = cmulc(x3, tw[3 * j * tws]);
+        }
+        const double2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = csub(x1, x3);
+        a[0] = cadd(t0, t2);
+        a[Ls] = make_double2(t1.x - t3.y, t1.y + t3.x);      // t1 + i t3
+        a[2 * Ls] = csub(t0, t2);
+        a[3 * Ls] = make_double2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+      } else if (R == 2) {
+        double2 x0 = a[0], x1 = a[Ls];
+        if (j != 0) x1 = cmulc(x1, tw[j * tws]);
+        a[0] = cadd(x0, x1);
+        a[Ls] = csub(x0, x1);
+      } else {
+        double2 x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls];
+        if (j != 0) {
+          x1 = cmulc(x1, tw[j * tws]);
+          x2 = cmulc(x2, tw[2 * j * tws]);
+        }
+        const double2 sp = cadd(x1, x2);
+        const double2 d = cscale(csub(x1, x2), kSqrt3Half);
+        const double2 m = caxpy(-0.5, sp, x0);
+        a[0] = cadd(x0, sp);
+        a[Ls] = make_double2(m.x - d.y, m.y + d.x);      // m + i d
+        a[2 * Ls] = make_double2(m.x + d.y, m.y - d.x);  // m - i d
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace nhqg

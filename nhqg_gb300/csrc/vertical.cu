@@ -1,0 +1,759 @@
+// Column engine: everything that acts on one horizontal mode's vertical
+// column (FP64).  Each CTA owns TM consecutive compact modes and stages their
+// columns (all levels) in shared memory as tiles [level][TM].
+//
+// Reference operations (nhqg/solver.py):
+//   Chebyshev <-> CGL nodal transforms V, V^-1           :45-52
+//   Galerkin stencil S and its exact left inverse pinv   :65-72 (grid.py:497-506, 322-342)
+//   d/dZ on Chebyshev coefficients G_Z                    grid.py:148-169
+//   explicit-RHS assembly                                 :541-549
+//   implicit tendency                                     :615-641
+//   implicit solve (block elimination)                    :691-738
+//   stage combinations of ARS(2,2,2) / SBP2-PC            :1023-1048, :1205-1217
+//   finalize + sanitize                                   :993-999, :128-146
+// pinv_w(proj_w(x)) == pinv_w(x) because pinv reads only the first Nz-1
+// Chebyshev coefficients and the tau projection rewrites only the last two,
+// so the tau projections that feed a pinv are not applied.
+#include "engine.h"
+
+namespace nhqg {
+
+namespace {
+
+constexpr int TM = 8;      // modes per CTA
+constexpr int NT = 256;    // threads per CTA
+
+struct VK {
+  int P, G, N, M, Mr, Mc, K, Nx, Nk;
+  bool mixed;                 // open-top (Neumann) w basis
+  const double *wa, *wb;      // mixed stencil coefficients
+  const double *V, *Vinv;
+  const double *kx, *inv_denom, *inv_aq, *inv_at, *drq, *drw, *drt;
+  double beta, Ra, gdt;
+};
+
+VK make_vk(const Params& p, const Tables& t) {
+  VK k;
+  k.P = p.d.P; k.G = p.d.G; k.N = p.d.Nz; k.M = p.d.M; k.Mr = p.d.Mr; k.Mc = p.d.Mc;
+  k.K = p.d.K; k.Nx = p.d.Nx; k.Nk = p.d.Nk;
+  k.mixed = t.wst_a != nullptr;
+  k.wa = t.wst_a; k.wb = t.wst_b;
+  k.V = t.V; k.Vinv = t.Vinv;
+  k.kx = t.kx; k.inv_denom = t.inv_denom; k.inv_aq = t.inv_aq; k.inv_at = t.inv_at;
+  k.drq = t.drq; k.drw = t.drw; k.drt = t.drt;
+  k.beta = p.beta; k.Ra = p.Ra_sigma; k.gdt = p.gamma_imex * p.dt;
+  return k;
+}
+
+// ---- tile helpers: buffers are [level][TM] ----
+__device__ __forceinline__ void tload(double2* b, const double2* __restrict__ src, int nlev,
+                                      int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    b[i] = (m < M) ? src[(size_t)l * M + m] : czero();
+  }
+}
+__device__ __forceinline__ void tstore(const double2* b, double2* __restrict__ dst, int nlev,
+                                       int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    if (m < M) dst[(size_t)l * M + m] = b[i];
+  }
+}
+// out[i] = sum_{j<nin} Mat[i*ld + j] in[j], i < nout
+__device__ __forceinline__ void tmat(double2* out, const double2* in, const double* __restrict__ Mat,
+                                     int ld, int nout, int nin) {
+  for (int idx = threadIdx.x; idx < nout * TM; idx += blockDim.x) {
+    const int i = idx / TM, mm = idx - i * TM;
+    const double* row = Mat + (size_t)i * ld;
+    double ax = 0.0, ay = 0.0;
+    for (int j = 0; j < nin; ++j) {
+      const double v = __ldg(row + j);
+      const double2 x = in[j * TM + mm];
+      ax = fma(v, x.x, ax);
+      ay = fma(v, x.y, ay);
+    }
+    out[idx] = make_double2(ax, ay);
+  }
+}
+// Dirichlet stencil: c_n = -x_n + x_{n-2}   (x has G = N-1 entries, c has P)
+__device__ __forceinline__ void tstencil_dir(double2* c, const double2* x, int P, int G) {
+  for (int idx = threadIdx.x; idx < P * TM; idx += blockDim.x) {
+    const int n = idx / TM, mm = idx - n * TM;
+    double2 v = (n < G) ? cneg(x[n * TM + mm]) : czero();
+    if (n >= 2 && n - 2 < G) v = cadd(v, x[(n - 2) * TM + mm]);
+    c[idx] = v;
+  }
+}
+// w stencil: Dirichlet, or the open-top basis T_n + a_n T_{n+1} + b_n T_{n+2}
+__device__ __forceinline__ void tstencil_w(const VK& k, double2* c, const double2* x) {
+  if (!k.mixed) { tstencil_dir(c, x, k.P, k.G); return; }
+  for (int idx = threadIdx.x; idx < k.P * TM; idx += blockDim.x) {
+    const int n = idx / TM, mm = idx - n * TM;
+    double2 v = (n < k.G) ? x[n * TM + mm] : czero();
+    if (n >= 1 && n - 1 < k.G) v = caxpy(__ldg(k.wa + n - 1), x[(n - 1) * TM + mm], v);
+    if (n >= 2 && n - 2 < k.G) v = caxpy(__ldg(k.wb + n - 2), x[(n - 2) * TM + mm], v);
+    c[idx] = v;
+  }
+}
+// exact left inverse of the Dirichlet stencil: x_n = x_{n-2} - c_n, n < G
+__device__ __forceinline__ void tpinv_dir(double2* x, const double2* c, int G) {
+  const int t = threadIdx.x;
+  if (t < 2 * TM) {
+    const int mm = t >> 1;
+    const bool im = t & 1;
+    double xm2 = 0.0, xm1 = 0.0;
+    for (int n = 0; n < G; ++n) {
+      const double cv = im ? c[n * TM + mm].y : c[n * TM + mm].x;
+      const double xn = xm2 - cv;
+      if (im) x[n * TM + mm].y = xn; else x[n * TM + mm].x = xn;
+      xm2 = xm1;
+      xm1 = xn;
+    }
+  }
+}
+__device__ __forceinline__ void tpinv_w(const VK& k, double2* x, const double2* c) {
+  if (!k.mixed) { tpinv_dir(x, c, k.G); return; }
+  const int t = threadIdx.x;
+  if (t < 2 * TM) {
+    const int mm = t >> 1;
+    const bool im = t & 1;
+    double xm2 = 0.0, xm1 = 0.0;
+    for (int n = 0; n < k.G; ++n) {
+      double v = im ? c[n * TM + mm].y : c[n * TM + mm].x;
+      if (n >= 1) v = fma(-__ldg(k.wa + n - 1), xm1, v);
+      if (n >= 2) v = fma(-__ldg(k.wb + n - 2), xm2, v);
+      if (im) x[n * TM + mm].y = v; else x[n * TM + mm].x = v;
+      xm2 = xm1;
+      xm1 = v;
+    }
+  }
+}
+// d/dZ on Chebyshev coefficients (G_Z = 2 G_xi), backward recurrence
+__device__ __forceinline__ void tgz(double2* b, const double2* a, int N) {
+  const int t = threadIdx.x;
+  if (t < 2 * TM) {
+    const int mm = t >> 1;
+    const bool im = t & 1;
+    auto A = [&](int n) { return im ? a[n * TM + mm].y : a[n * TM + mm].x; };
+    auto S = [&](int n, double v) { if (im) b[n * TM + mm].y = v; else b[n * TM + mm].x = v; };
+    S(N, 0.0);
+    double bk2 = 0.0;                      // b_{k+2}
+    double bk1 = 4.0 * N * A(N);           // b_{N-1}
+    S(N - 1, bk1);
+    for (int kk = N - 2; kk >= 1; --kk) {
+      const double bk = fma(4.0 * (kk + 1), A(kk + 1), bk2);
+      S(kk, bk);
+      bk2 = bk1;
+      bk1 = bk;
+    }
+    // b_0 = b_2 / 2 + 2 a_1
+    S(0, fma(0.5, bk2, 2.0 * A(1)));
+  }
+}
+
+__device__ __forceinline__ int mode_of(int idx, int m0) { return m0 + (idx % TM); }
+
+// =========================================================== forward: to nodal
+__global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const double2* w,
+                                             const double2* th, double2* qn, double2* wn,
+                                             double2* tn) {
+  extern __shared__ double2 sm[];
+  double2* b0 = sm;
+  double2* b1 = sm + k.P * TM;
+  const int m0 = blockIdx.x * TM;
+  if (q) {
+    tload(b0, q, k.P, m0, k.M);
+    __syncthreads();
+    tmat(b1, b0, k.V, k.P, k.P, k.P);
+    __syncthreads();
+    tstore(b1, qn, k.P, m0, k.M);
+    __syncthreads();
+  }
+  if (w) {
+    tload(b0, w, k.G, m0, k.M);
+    __syncthreads();
+    tstencil_w(k, b1, b0);
+    __syncthreads();
+    tmat(b0, b1, k.V, k.P, k.P, k.P);
+    __syncthreads();
+    tstore(b0, wn, k.P, m0, k.M);
+    __syncthreads();
+  }
+  if (th) {
+    tload(b0, th, k.G, m0, k.M);
+    __syncthreads();
+    tstencil_dir(b1, b0, k.P, k.G);
+    __syncthreads();
+    tmat(b0, b1, k.V, k.P, k.P, k.P);
+    __syncthreads();
+    tstore(b0, tn, k.P, m0, k.M);
+  }
+}
+
+// =========================================================== back + stage + solve-pre
+template <int MODE>
+__global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
+  extern __shared__ double2 sm[];
+  const int PT = k.P * TM;
+  double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT, *b4 = sm + 4 * PT;
+  const int m0 = blockIdx.x * TM;
+  const int P = k.P, G = k.G, M = k.M;
+  const size_t Ms = (size_t)M;
+
+  // ------------------------------------------------------------- q
+  if (MODE != VB_SOLVE) {
+    tload(b0, a.Aq, P, m0, M);
+    __syncthreads();
+    tmat(b1, b0, k.Vinv, P, P, P);
+    __syncthreads();
+    // E_q = -Aq - i beta kx psi, psi = -inv_denom * q_state
+    const double2* qs = (MODE == VB_STAGE2) ? a.q1 : a.q0;
+    for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+      const int l = i / TM, m = mode_of(i, m0);
+      if (m >= M) continue;
+      double2 e = cneg(b1[i]);
+      if (k.beta != 0.0) {
+        const double s = k.beta * k.kx[m] * k.inv_denom[m];
+        const double2 qv = qs[(size_t)l * Ms + m];
+        e = make_double2(fma(-s, qv.y, e.x), fma(s, qv.x, e.y));
+      }
+      b1[i] = e;
+    }
+    __syncthreads();
+    if (MODE == VB_RHS) {
+      tstore(b1, a.Eq, P, m0, M);
+    } else if (MODE == VB_STAGE1) {
+      tstore(b1, a.E1q, P, m0, M);
+      for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+        const int l = i / TM, m = mode_of(i, m0);
+        if (m < M) b1[i] = caxpy(a.alpha, b1[i], a.q0[(size_t)l * Ms + m]);
+      }
+    } else {  // STAGE2: I_q = G_Z S_w w1
+      tload(b2, a.w1, G, m0, M);
+      __syncthreads();
+      tstencil_w(k, b3, b2);
+      __syncthreads();
+      tgz(b2, b3, k.N);
+      __syncthreads();
+      for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+        const int l = i / TM, m = mode_of(i, m0);
+        if (m >= M) continue;
+        const size_t g = (size_t)l * Ms + m;
+        double2 r = a.q0[g];
+        r = caxpy(a.c_E1, a.E1q[g], r);
+        r = caxpy(a.c_E2, b1[i], r);
+        r = caxpy(a.omega, b2[i], r);
+        r = caxpy(-a.omega * k.drq[m], a.q1[g], r);
+        b1[i] = r;
+      }
+    }
+    __syncthreads();
+  } else {
+    tload(b1, a.q0, P, m0, M);  // R_q given
+    __syncthreads();
+  }
+  if (MODE != VB_RHS) {
+    tstore(b1, a.Rq, P, m0, M);
+    // temp = R_q / alpha_q ; d_gal = pinv_w(inv_denom * G_Z temp)
+    for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+      const int m = mode_of(i, m0);
+      b2[i] = (m < M) ? cscale(b1[i], k.inv_aq[m]) : czero();
+    }
+    __syncthreads();
+    tgz(b3, b2, k.N);
+    __syncthreads();
+    for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+      const int m = mode_of(i, m0);
+      b3[i] = (m < M) ? cscale(b3[i], k.inv_denom[m]) : czero();
+    }
+    __syncthreads();
+    tpinv_w(k, b4, b3);
+    __syncthreads();
+  }
+
+  // ------------------------------------------------------------- w
+  if (MODE != VB_SOLVE) {
+    tload(b0, a.Aw, P, m0, M);
+    __syncthreads();
+    tmat(b1, b0, k.Vinv, P, P, P);
+    __syncthreads();
+    for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
+    __syncthreads();
+    tpinv_w(k, b2, b1);
+    __syncthreads();
+    if (MODE == VB_RHS) {
+      tstore(b2, a.Ew, G, m0, M);
+    } else if (MODE == VB_STAGE1) {
+      tstore(b2, a.E1w, G, m0, M);
+      for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
+        const int l = i / TM, m = mode_of(i, m0);
+        if (m < M) b2[i] = caxpy(a.alpha, b2[i], a.w0[(size_t)l * Ms + m]);
+      }
+    } else {  // I_w = pinv_w(inv_denom G_Z q1 + Ra S_dir t1)
+      tload(b0, a.q1, P, m0, M);
+      __syncthreads();
+      tgz(b1, b0, k.N);
+      __syncthreads();
+      tload(b0, a.t1, G, m0, M);
+      __syncthreads();
+      tstencil_dir(b3, b0, P, G);
+      __syncthreads();
+      for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+        const int m = mode_of(i, m0);
+        b1[i] = (m < M) ? caxpy(k.Ra, b3[i], cscale(b1[i], k.inv_denom[m])) : czero();
+      }
+      __syncthreads();
+      tpinv_w(k, b0, b1);
+      __syncthreads();
+      for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
+        const int l = i / TM, m = mode_of(i, m0);
+        if (m >= M) continue;
+        const size_t g = (size_t)l * Ms + m;
+        double2 r = a.w0[g];
+        r = caxpy(a.c_E1, a.E1w[g], r);
+        r = caxpy(a.c_E2, b2[i], r);
+        r = caxpy(a.omega, b0[i], r);
+        r = caxpy(-a.omega * k.drw[m], a.w1[g], r);
+        b2[i] = r;
+      }
+    }
+    __syncthreads();
+  } else {
+    tload(b2, a.w0, G, m0, M);  // R_w given
+    __syncthreads();
+  }
+  if (MODE != VB_RHS) {
+    for (int i = threadIdx.x; i < G * TM; i += blockDim.x) b4[i] = caxpy(k.gdt, b4[i], b2[i]);
+    __syncthreads();
+  }
+
+  // ------------------------------------------------------------- theta
+  if (MODE != VB_SOLVE) {
+    tload(b0, a.At, P, m0, M);
+    __syncthreads();
+    if (a.dtb_nodal != nullptr) {  // legacy evolve_mean: + (dTheta/dZ)_nodal * w_nodal
+      for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+        const int l = i / TM, m = mode_of(i, m0);
+        if (m < M) b0[i] = caxpy(a.dtb_nodal[l], a.Wn[(size_t)l * Ms + m], b0[i]);
+      }
+      __syncthreads();
+    }
+    tmat(b1, b0, k.Vinv, P, P, P);
+    __syncthreads();
+    for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
+    __syncthreads();
+    tpinv_dir(b2, b1, G);
+    __syncthreads();
+    if (MODE == VB_RHS) {
+      tstore(b2, a.Et, G, m0, M);
+    } else if (MODE == VB_STAGE1) {
+      tstore(b2, a.E1t, G, m0, M);
+      for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
+        const int l = i / TM, m = mode_of(i, m0);
+        if (m < M) b2[i] = caxpy(a.alpha, b2[i], a.t0[(size_t)l * Ms + m]);
+      }
+    } else {  // I_t = w1 (shared basis) or pinv_dir(S_w w1)
+      tload(b0, a.w1, G, m0, M);
+      __syncthreads();
+      if (k.mixed) {
+        tstencil_w(k, b1, b0);
+        __syncthreads();
+        tpinv_dir(b0, b1, G);
+        __syncthreads();
+      }
+      for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
+        const int l = i / TM, m = mode_of(i, m0);
+        if (m >= M) continue;
+        const size_t g = (size_t)l * Ms + m;
+        double2 r = a.t0[g];
+        r = caxpy(a.c_E1, a.E1t[g], r);
+        r = caxpy(a.c_E2, b2[i], r);
+        r = caxpy(a.omega, b0[i], r);
+        r = caxpy(-a.omega * k.drt[m], a.t1[g], r);
+        if (a.inv_alpha_c != 0.0) {
+          const double2 c = cscale(csub(a.t1[g], a.t1p[g]), a.inv_alpha_c);
+          r = caxpy(a.omega, c, r);
+        }
+        b2[i] = r;
+      }
+    }
+    __syncthreads();
+  } else {
+    tload(b2, a.t0, G, m0, M);  // R_th given
+    __syncthreads();
+  }
+  if (MODE != VB_RHS) {
+    tstore(b2, a.Rt, G, m0, M);
+    for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
+      const int m = mode_of(i, m0);
+      b0[i] = (m < M) ? cscale(b2[i], k.inv_at[m]) : czero();
+    }
+    __syncthreads();
+    if (k.mixed) {  // theta basis -> w basis
+      tstencil_dir(b1, b0, P, G);
+      __syncthreads();
+      tpinv_w(k, b0, b1);
+      __syncthreads();
+    }
+    const double c = k.gdt * k.Ra;
+    for (int i = threadIdx.x; i < G * TM; i += blockDim.x) b4[i] = caxpy(c, b0[i], b4[i]);
+    __syncthreads();
+    tstore(b4, a.rhs_w, G, m0, M);
+  }
+}
+
+// =========================================================== back-substitution
+__global__ void __launch_bounds__(NT) k_vpost(VK k, const double2* Rq, const double2* Rt,
+                                              const double2* wn, double2* qo, double2* to,
+                                              bool zero_mean) {
+  extern __shared__ double2 sm[];
+  const int PT = k.P * TM;
+  double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT;
+  const int m0 = blockIdx.x * TM;
+  const int M = k.M;
+  tload(b0, wn, k.G, m0, M);
+  __syncthreads();
+  tstencil_w(k, b1, b0);  // w Chebyshev coefficients
+  __syncthreads();
+  tgz(b2, b1, k.N);
+  __syncthreads();
+  for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+    const int l = i / TM, m = mode_of(i, m0);
+    if (m >= M) continue;
+    const size_t g = (size_t)l * M + m;
+    qo[g] = (zero_mean && m == 0) ? czero() : cscale(caxpy(k.gdt, b2[i], Rq[g]), k.inv_aq[m]);
+  }
+  if (k.mixed) {  // w basis -> theta basis
+    __syncthreads();
+    tpinv_dir(b0, b1, k.G);
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < k.G * TM; i += blockDim.x) {
+    const int l = i / TM, m = mode_of(i, m0);
+    if (m >= M) continue;
+    const size_t g = (size_t)l * M + m;
+    to[g] = (zero_mean && m == 0) ? czero() : cscale(caxpy(k.gdt, b0[i], Rt[g]), k.inv_at[m]);
+  }
+}
+
+// =========================================================== implicit tendency
+__global__ void __launch_bounds__(NT) k_itend(VK k, const double2* q, const double2* w,
+                                              const double2* th, double2* Iq, double2* Iw,
+                                              double2* It) {
+  extern __shared__ double2 sm[];
+  const int PT = k.P * TM;
+  double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT;
+  const int m0 = blockIdx.x * TM;
+  const int M = k.M;
+  tload(b0, w, k.G, m0, M);
+  __syncthreads();
+  tstencil_w(k, b1, b0);
+  __syncthreads();
+  tgz(b2, b1, k.N);
+  __syncthreads();
+  tstore(b2, Iq, k.P, m0, M);
+  if (k.mixed) {
+    tpinv_dir(b3, b1, k.G);
+    __syncthreads();
+    tstore(b3, It, k.G, m0, M);
+  } else {
+    tstore(b0, It, k.G, m0, M);
+  }
+  __syncthreads();
+  tload(b0, q, k.P, m0, M);
+  __syncthreads();
+  tgz(b1, b0, k.N);
+  tload(b2, th, k.G, m0, M);
+  __syncthreads();
+  tstencil_dir(b3, b2, k.P, k.G);
+  __syncthreads();
+  for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+    const int m = mode_of(i, m0);
+    b1[i] = (m < M) ? caxpy(k.Ra, b3[i], cscale(b1[i], k.inv_denom[m])) : czero();
+  }
+  __syncthreads();
+  tpinv_w(k, b0, b1);
+  __syncthreads();
+  tstore(b0, Iw, k.G, m0, M);
+}
+
+// =========================================================== per-shell dense solve
+// w = imex_inv[shell(k)] @ rhs_w for every mode; one CTA per shell, the
+// shell's matrix streams once through L1 while its modes' columns sit in
+// shared memory.  NC modes per pass (compile-time, so no FMA is wasted).
+template <int NC>
+__device__ __forceinline__ void shell_rows(const double* __restrict__ A, const double2* xs, int G,
+                                           int ld_x, double2* out, const int* modes, int M) {
+  for (int i = threadIdx.x; i < G; i += blockDim.x) {
+    double2 acc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] = czero();
+    const double* row = A + (size_t)i * G;
+    for (int j = 0; j < G; ++j) {
+      const double v = __ldg(row + j);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) acc[c] = caxpy(v, xs[j * ld_x + c], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) out[(size_t)i * M + modes[c]] = acc[c];
+  }
+}
+
+constexpr int SHELL_NC = 8;
+
+__global__ void __launch_bounds__(NT) k_shell(const double* mats, const int* start, const int* list,
+                                              const double2* rhs, double2* out, int G, int M) {
+  extern __shared__ double2 xs[];  // [G][SHELL_NC]
+  __shared__ int modes[SHELL_NC];
+  const int s = blockIdx.x;
+  const int b = start[s], e = start[s + 1];
+  const double* A = mats + (size_t)s * G * G;
+  for (int c0 = b; c0 < e; c0 += SHELL_NC) {
+    const int nc = min(SHELL_NC, e - c0);
+    if (threadIdx.x < nc) modes[threadIdx.x] = list[c0 + threadIdx.x];
+    __syncthreads();
+    for (int i = threadIdx.x; i < G * nc; i += blockDim.x) {
+      const int j = i / nc, c = i - j * nc;
+      xs[j * SHELL_NC + c] = rhs[(size_t)j * M + modes[c]];
+    }
+    __syncthreads();
+    switch (nc) {
+      case 1: shell_rows<1>(A, xs, G, SHELL_NC, out, modes, M); break;
+      case 2: shell_rows<2>(A, xs, G, SHELL_NC, out, modes, M); break;
+      case 3: shell_rows<3>(A, xs, G, SHELL_NC, out, modes, M); break;
+      case 4: shell_rows<4>(A, xs, G, SHELL_NC, out, modes, M); break;
+      case 5: shell_rows<5>(A, xs, G, SHELL_NC, out, modes, M); break;
+      case 6: shell_rows<6>(A, xs, G, SHELL_NC, out, modes, M); break;
+      case 7: shell_rows<7>(A, xs, G, SHELL_NC, out, modes, M); break;
+      default: shell_rows<8>(A, xs, G, SHELL_NC, out, modes, M); break;
+    }
+    __syncthreads();
+  }
+}
+
+// =========================================================== layout kernels
+__global__ void k_gather(Dims d, const double2* full, double2* cmp, int levels, int* status) {
+  const size_t total = (size_t)levels * d.Nx * d.Nk;
+  bool outside_nonzero = false;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % d.Nk);
+    const size_t rest = i / d.Nk;
+    const int row = (int)(rest % d.Nx);
+    const int l = (int)(rest / d.Nx);
+    const int kxi = row <= d.Nx / 2 ? row : row - d.Nx;
+    const double2 v = full[i];
+    if (abs(kxi) <= d.K && c <= d.K) {
+      const int r = kxi >= 0 ? kxi : kxi + 2 * d.K + 1;
+      cmp[(size_t)l * d.M + r * d.Mc + c] = v;
+    } else if (v.x != 0.0 || v.y != 0.0) {
+      outside_nonzero = true;
+    }
+  }
+  if (outside_nonzero && status) atomicOr(status, 1 << NHQG_STATUS_BIT_OOB);
+}
+
+__global__ void k_scatter(Dims d, const double2* cmp, double2* full, int levels) {
+  const size_t total = (size_t)levels * d.Nx * d.Nk;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % d.Nk);
+    const size_t rest = i / d.Nk;
+    const int row = (int)(rest % d.Nx);
+    const int l = (int)(rest / d.Nx);
+    const int kxi = row <= d.Nx / 2 ? row : row - d.Nx;
+    double2 v = czero();
+    if (abs(kxi) <= d.K && c <= d.K) {
+      const int r = kxi >= 0 ? kxi : kxi + 2 * d.K + 1;
+      v = cmp[(size_t)l * d.M + r * d.Mc + c];
+    }
+    full[i] = v;
+  }
+}
+
+// zero the k=0 mode, Hermitian-project the ky=0 column (2/3 band kept)
+__global__ void k_finalize(Dims d, const double2* q, const double2* w, const double2* th,
+                           double2* qo, double2* wo, double2* to) {
+  const int nlev[3] = {d.P, d.G, d.G};
+  const double2* src[3] = {q, w, th};
+  double2* dst[3] = {qo, wo, to};
+  const size_t per = (size_t)d.M;
+  const size_t total = (size_t)(d.P + 2 * d.G) * per;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    int f = 0;
+    size_t j = i;
+    while (j >= (size_t)nlev[f] * per) { j -= (size_t)nlev[f] * per; ++f; }
+    const int m = (int)(j % per);
+    const size_t lbase = j - m;
+    const int r = m / d.Mc, c = m - r * d.Mc;
+    double2 v;
+    if (c != 0) {
+      v = src[f][j];
+    } else {
+      const int rm = mirror_row(r, d.K);
+      double2 a = (r == 0) ? czero() : src[f][lbase + (size_t)r * d.Mc];
+      double2 b = (rm == 0) ? czero() : src[f][lbase + (size_t)rm * d.Mc];
+      v = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+    }
+    dst[f][j] = v;
+  }
+}
+
+// Hermitian projection of the ky=0 column, in place (no k=0 zeroing)
+__global__ void k_hermitian(Dims d, double2* q, double2* w, double2* th) {
+  const int nlev[3] = {d.P, d.G, d.G};
+  double2* f3[3] = {q, w, th};
+  const int half = d.K;  // rows 1..K pair with 2K..K+1
+  const int total = (d.P + 2 * d.G) * (half + 1);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    int f = 0, j = i;
+    while (j >= nlev[f] * (half + 1)) { j -= nlev[f] * (half + 1); ++f; }
+    const int l = j / (half + 1), r = j - l * (half + 1);
+    double2* col = f3[f] + (size_t)l * d.M;  // c = 0 entries at row*Mc
+    if (r == 0) {
+      col[0] = make_double2(col[0].x, 0.0);
+    } else {
+      const int rm = mirror_row(r, d.K);
+      const double2 a = col[(size_t)r * d.Mc], b = col[(size_t)rm * d.Mc];
+      const double2 h = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+      col[(size_t)r * d.Mc] = h;
+      col[(size_t)rm * d.Mc] = cconj(h);
+    }
+  }
+}
+
+// mean over the Nx x Nx grid of irfft2(a) * irfft2(b), per level, by Parseval
+__global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const double2* b,
+                                                 double* out, double scale) {
+  __shared__ double scratch[32];
+  const int l = blockIdx.x;
+  const double2* al = a + (size_t)l * d.M;
+  const double2* bl = b + (size_t)l * d.M;
+  double acc = 0.0;
+  for (int m = threadIdx.x; m < d.M; m += blockDim.x) {
+    const int r = m / d.Mc, c = m - r * d.Mc;
+    if (c != 0) {
+      const double2 x = al[m], y = bl[m];
+      acc += 2.0 * fma(x.x, y.x, x.y * y.y);
+    } else {
+      const int rm = mirror_row(r, d.K);
+      const double2 x = al[m], xm = al[rm * d.Mc];
+      const double2 y = bl[m], ym = bl[rm * d.Mc];
+      const double hx_re = 0.5 * (x.x + xm.x), hx_im = 0.5 * (x.y - xm.y);
+      const double hy_re = 0.5 * (y.x + ym.x), hy_im = 0.5 * (y.y - ym.y);
+      acc += fma(hx_re, hy_re, hx_im * hy_im);
+    }
+  }
+  const double tot = block_sum(acc, scratch);
+  if (threadIdx.x == 0) out[l] = tot * scale;
+}
+
+__global__ void k_zero_mode0(double2* f, int levels, int M) {
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < levels; l += gridDim.x * blockDim.x)
+    f[(size_t)l * M] = czero();
+}
+
+inline size_t vsmem(const Params& p, int nbuf) { return (size_t)nbuf * p.d.P * TM * sizeof(double2); }
+inline int vgrid(const Params& p) { return (p.d.M + TM - 1) / TM; }
+
+}  // namespace
+
+cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, const double2* w,
+                        const double2* th, double2* qn, double2* wn, double2* tn, cudaStream_t st) {
+  VK k = make_vk(p, t);
+  const size_t sm = vsmem(p, 2);
+  cudaFuncSetAttribute(k_vfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_vfwd<<<vgrid(p), NT, sm, st>>>(k, q, w, th, qn, wn, tn);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st) {
+  VK k = make_vk(p, t);
+  const size_t sm = vsmem(p, 5);
+  switch (mode) {
+    case VB_RHS:
+      cudaFuncSetAttribute(k_vback<VB_RHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_vback<VB_RHS><<<vgrid(p), NT, sm, st>>>(k, a);
+      break;
+    case VB_STAGE1:
+      cudaFuncSetAttribute(k_vback<VB_STAGE1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_vback<VB_STAGE1><<<vgrid(p), NT, sm, st>>>(k, a);
+      break;
+    case VB_STAGE2:
+      cudaFuncSetAttribute(k_vback<VB_STAGE2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_vback<VB_STAGE2><<<vgrid(p), NT, sm, st>>>(k, a);
+      break;
+    default:
+      cudaFuncSetAttribute(k_vback<VB_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_vback<VB_SOLVE><<<vgrid(p), NT, sm, st>>>(k, a);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shell(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
+                         cudaStream_t st) {
+  const size_t sm = (size_t)p.d.G * SHELL_NC * sizeof(double2);
+  cudaFuncSetAttribute(k_shell, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_shell<<<t.n_shells, NT, sm, st>>>(t.shell_inv, t.shell_start, t.shell_modes, rhs_w, w_out,
+                                      p.d.G, p.d.M);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vpost(const Params& p, const Tables& t, const double2* Rq, const double2* Rt,
+                         const double2* w_new, double2* q_out, double2* t_out, bool zero_mean,
+                         cudaStream_t st) {
+  VK k = make_vk(p, t);
+  const size_t sm = vsmem(p, 3);
+  cudaFuncSetAttribute(k_vpost, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_vpost<<<vgrid(p), NT, sm, st>>>(k, Rq, Rt, w_new, q_out, t_out, zero_mean);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_itend(const Params& p, const Tables& t, const double2* q, const double2* w,
+                         const double2* th, double2* Iq, double2* Iw, double2* It, cudaStream_t st) {
+  VK k = make_vk(p, t);
+  const size_t sm = vsmem(p, 4);
+  cudaFuncSetAttribute(k_itend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_itend<<<vgrid(p), NT, sm, st>>>(k, q, w, th, Iq, Iw, It);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const Params& p, const double2* full, double2* compact, int levels,
+                          int* status, cudaStream_t st) {
+  k_gather<<<4 * 152, 256, 0, st>>>(p.d, full, compact, levels, status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const Params& p, const double2* compact, double2* full, int levels,
+                           cudaStream_t st) {
+  k_scatter<<<4 * 152, 256, 0, st>>>(p.d, compact, full, levels);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const Params& p, const double2* q, const double2* w, const double2* th,
+                            double2* qo, double2* wo, double2* to, cudaStream_t st) {
+  k_finalize<<<4 * 152, 256, 0, st>>>(p.d, q, w, th, qo, wo, to);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hermitian(const Params& p, double2* q, double2* w, double2* th, cudaStream_t st) {
+  k_hermitian<<<4 * 152, 256, 0, st>>>(p.d, q, w, th);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStream_t st) {
+  k_zero_mode0<<<1, 256, 0, st>>>(f, levels, p.d.M);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
+                            double* out, cudaStream_t st) {
+  const double n2 = (double)p.d.Nx * (double)p.d.Nx;
+  k_parseval<<<levels, NT, 0, st>>>(p.d, a, b, out, 1.0 / (n2 * n2));
+  return cudaGetLastError();
+}
+
+}  // namespace nhqg

@@ -1,0 +1,177 @@
+"""Drop-in time-step API on the GB300 engine.
+
+Same names, argument meaning and return structure as the reference's
+``nhqg.solver`` (nhqg/solver.py): ``State`` (q_hat, w_hat, th_hat, th_bar),
+``imex_step(state, grid) -> State``, ``explicit_rhs``,
+``explicit_rhs_dispatch``, ``implicit_tendency``, ``imex_implicit_solve``,
+``imex_mean_temp_solve``, ``sanitize_state`` and ``run``.  Fields are CUDA
+torch tensors (complex128 / float64) in the reference layout; NumPy arrays
+are accepted and copied to the device.  Functions return new tensors, like
+the reference's functional JAX API; ``step_inplace`` advances a state in
+place for drivers that own their buffers (the analogue of donation).
+
+Every computation runs in the CUDA engine; there is no CPU path.
+"""
+
+from __future__ import annotations
+
+from typing import NamedTuple
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .engine import engine_for, require_cuda
+from .grid import Grid
+
+
+class State(NamedTuple):
+    """q' Chebyshev (Nz+1, Nx, Nk); w, theta Galerkin (Nz-1, Nx, Nk);
+    th_bar Chebyshev (Nz+1,)  (nhqg/solver.py:33-38)."""
+    q_hat: torch.Tensor
+    w_hat: torch.Tensor
+    th_hat: torch.Tensor
+    th_bar: torch.Tensor
+
+
+def _dev(x, dtype) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        return x.to(device="cuda", dtype=dtype).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(x))).to(device="cuda", dtype=dtype)
+
+
+def to_device(state) -> State:
+    """State of CUDA tensors (copies NumPy / host inputs)."""
+    require_cuda()
+    return State(_dev(state[0], torch.complex128), _dev(state[1], torch.complex128),
+                 _dev(state[2], torch.complex128), _dev(state[3], torch.float64))
+
+
+def to_host(state) -> tuple:
+    return tuple(t.detach().cpu().numpy() for t in state)
+
+
+def _fresh(state: State) -> State:
+    return State(*(torch.empty_like(t) for t in state))
+
+
+def _copy(state) -> State:
+    s = to_device(state)
+    return State(*(t.clone() for t in s))
+
+
+def _check_band(eng, what: str) -> None:
+    st = eng.device_status(reset=True)
+    if st & nat.DEVICE_STATUS_OOB:
+        raise ValueError(
+            f"{what}: the state has content outside the 2/3 band; the GPU step "
+            "assumes band-limited input (apply sanitize_state first)")
+
+
+def sanitize_state(state, grid: Grid) -> State:
+    """Hermitian projection of the ky=0 column + 2/3 band limit
+    (nhqg/solver.py:128-146)."""
+    eng = engine_for(grid)
+    s = _copy(state)
+    eng.sanitize(*s)
+    eng.device_status(reset=True)
+    return s
+
+
+def step_inplace(state: State, grid: Grid, n_steps: int = 1, check: bool = False) -> State:
+    """Advance ``state`` (CUDA tensors, reference layout) by ``n_steps``
+    imex_step applications in place; stream-ordered, no host sync unless
+    ``check`` (then the band-limit status is verified)."""
+    eng = engine_for(grid)
+    eng.step(*state, n_steps=n_steps)
+    if check:
+        _check_band(eng, "imex_step")
+    return state
+
+
+def imex_step(state, grid: Grid) -> State:
+    """One IMEX step incl. ``sanitize_state`` (nhqg/solver.py:1228-1242)."""
+    s = _copy(state)
+    return step_inplace(s, grid, 1, check=True)
+
+
+def _split(grid: Grid) -> bool:
+    return grid.mean_exchange_discretization in ("balanced_sbp2", "balanced_sbp2_pc")
+
+
+def explicit_rhs(state, grid: Grid) -> State:
+    """Explicit tendency E (nhqg/solver.py:510-599) for ``grid``'s closure."""
+    eng = engine_for(grid)
+    src = to_device(state)
+    out = _fresh(src)
+    eng.explicit_rhs(src, out, grid.thermal_closure, grid.mean_exchange_discretization)
+    _check_band(eng, "explicit_rhs")
+    return out
+
+
+def explicit_rhs_dispatch(state, grid: Grid) -> State:
+    """nhqg/solver.py:602-608 (vertical_dealiasing='none')."""
+    return explicit_rhs(state, grid)
+
+
+def implicit_tendency(state, grid: Grid) -> State:
+    """Implicit tendency I (nhqg/solver.py:615-641)."""
+    eng = engine_for(grid)
+    src = to_device(state)
+    out = _fresh(src)
+    eng.implicit_tendency(src, out, grid.thermal_closure)
+    _check_band(eng, "implicit_tendency")
+    return out
+
+
+def imex_implicit_solve(R_q, R_w, R_th, grid: Grid):
+    """Block-eliminated implicit stage solve (nhqg/solver.py:691-738)."""
+    eng = engine_for(grid)
+    zero = torch.zeros(grid.Nz + 1, dtype=torch.float64, device="cuda")
+    src = to_device((R_q, R_w, R_th, zero))
+    out = _fresh(src)
+    eng.implicit_solve(src, out, grid.thermal_closure)
+    _check_band(eng, "imex_implicit_solve")
+    return out.q_hat, out.w_hat, out.th_hat
+
+
+def imex_mean_temp_solve(R_th_bar, grid: Grid) -> torch.Tensor:
+    """1-D mean-temperature implicit solve (nhqg/solver.py:741-758)."""
+    eng = engine_for(grid)
+    R = _dev(R_th_bar, torch.float64)
+    out = torch.empty_like(R)
+    eng.mean_temp_solve(R, out, grid.thermal_closure)
+    return out
+
+
+def apply_balanced_sbp2_corrector(state, grid: Grid, total_dt) -> State:
+    """SBP2 thermal corrector (nhqg/solver.py:909-950)."""
+    eng = engine_for(grid)
+    src = to_device(state)
+    out = _fresh(src)
+    eng.corrector(src, out, float(total_dt))
+    _check_band(eng, "apply_balanced_sbp2_corrector")
+    return out
+
+
+def run(grid: Grid, state, n_steps: int, save_interval: int, use_imex: bool = True,
+        callback=None):
+    """Time loop (nhqg/solver.py:1385-1416): sanitize the incoming state, then
+    advance in chunks of ``save_interval`` steps; returns (state, snapshots)
+    with snapshots = [(t, State copy), ...]."""
+    if not use_imex:
+        raise NotImplementedError("the GPU engine implements the IMEX stepper (use_imex=True)")
+    s = sanitize_state(state, grid)
+    snaps = []
+    n_outer = n_steps // save_interval
+    for i in range(n_outer):
+        step_inplace(s, grid, save_interval, check=(i == 0))
+        step = (i + 1) * save_interval
+        t = step * float(grid.dt)
+        if callback is not None:
+            callback(s, step, t)
+        snaps.append((t, State(*(x.clone() for x in s))))
+    rem = n_steps % save_interval
+    if rem:
+        step_inplace(s, grid, rem, check=(n_outer == 0))
+    return s, snaps

@@ -15,14 +15,16 @@ def rel_l2(a, b, floor: float = 0.0) -> float:
     return num / den
 
 
-def assert_state_close(got, ref, tol, names=("q_hat", "w_hat", "th_hat", "th_bar"), floor=1e-30, th_bar_abs=None):
+def assert_state_close(got, ref, tol, names=("q_hat", "w_hat", "th_hat", "th_bar"), th_bar_abs=0.0,
+                       abs_floor=0.0):
+    """Per field: ||got - ref|| <= tol * ||ref||, or <= an absolute floor
+    (``th_bar_abs`` for th_bar, which the reference may keep at exact zero)."""
     for name, g, r in zip(names, got, ref):
         g = np.asarray(g)
         r = np.asarray(r)
         assert g.shape == r.shape, (name, g.shape, r.shape)
-        if name == "th_bar" and th_bar_abs is not None:
-            err = float(np.max(np.abs(g - r)))
-            assert err <= th_bar_abs, f"{name}: abs err {err:.3e} > {th_bar_abs:.1e}"
-            continue
-        e = rel_l2(g, r, floor=floor)
-        assert e <= tol, f"{name}: rel L2 {e:.3e} > {tol:.1e}"
+        err = float(np.linalg.norm(g - r))
+        scale = float(np.linalg.norm(r))
+        floor = th_bar_abs if name == "th_bar" else abs_floor
+        assert err <= max(tol * scale, floor), (
+            f"{name}: |diff| {err:.3e}, rel {err / scale if scale else float('inf'):.3e} > {tol:.1e}")

@@ -1,0 +1,106 @@
+"""Host-side checks (no GPU): the product's make_grid against the oracle's
+restatement of the reference, the C-ABI library surface, and the theta'
+initial state against the reference fixture."""
+
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import fixtures
+import oracle
+from oracle.nhqg_oracle import OracleConfig
+from nhqg_gb300 import NHQGConfig, make_grid, theta_perturbation_state
+from nhqg_gb300 import _native as nat
+
+ROOT = Path(__file__).resolve().parent.parent
+
+CFGS = [
+    dict(Nx=32, Nz=16, L=48.154, Ra_tilde=100.0, nu_q=1.0, nu_w=1.0, nu_theta=1.0, hyper_order=1,
+         dt=5e-5, thermal_closure="evolve_mean", mean_exchange_discretization="balanced_sbp2_pc",
+         sbp_corrector_substeps=4, nonlinear_advection="flux"),
+    dict(Nx=24, Nz=12, L=20.0, Ra_tilde=70.0, nu_q=1e-3, nu_w=2e-3, nu_theta=3e-3, hyper_order=2,
+         dt=1e-4, drag=0.1, Ld=3.0, w_bc_top="neumann", sbp_transfer_mode="mass_adjoint"),
+]
+
+
+def _pair(over):
+    base = dict(float_dtype="float64", horizontal_dealiasing="23_rule")
+    base.update(over)
+    return make_grid(NHQGConfig(**base)), oracle.make_grid(OracleConfig(**base))
+
+
+@pytest.mark.parametrize("over", CFGS)
+def test_grid_matches_oracle(over):
+    g, o = _pair(over)
+    for name in ("G_Z", "G_Z2", "V", "V_inv", "dirichlet_stencil", "dirichlet_pinv", "w_stencil",
+                 "w_pinv", "proj_dirichlet", "proj_neumann", "proj_w", "sbp_D1", "sbp_L",
+                 "cgl_to_sbp", "sbp_to_cgl", "kx", "ky", "ksq", "inv_denom", "mask_23",
+                 "diss_rate_q", "diss_rate_w", "diss_rate_th", "inv_alpha_q", "inv_alpha_th",
+                 "ksq_idx", "Z", "cc_weights"):
+        a, b = np.asarray(getattr(g, name)), np.asarray(getattr(o, name))
+        assert a.shape == b.shape, name
+        assert np.array_equal(a, b), name
+
+
+@pytest.mark.parametrize("over", CFGS)
+def test_shell_tables_bitwise(over):
+    """In-band shell inverses equal the reference-order construction bit for bit."""
+    g, o = _pair(over)
+    rows = g.imex_shell_row
+    band = rows >= 0
+    ref = o.imex_inv[o.ksq_idx[band]]
+    got = g.imex_inv[rows[band]]
+    assert np.array_equal(got, ref)
+    assert np.all(rows[~band] == -1)
+
+
+def test_theta_init_matches_reference_fixture():
+    meta, arrays = fixtures.load_case("prod16")
+    cfg = dict(meta["cfg"])
+    g = make_grid(NHQGConfig(**cfg))
+    s = theta_perturbation_state(g, seed=meta["seed"])
+    for got, ref in zip(s, fixtures.state_from(arrays, "s0")):
+        scale = max(float(np.linalg.norm(ref)), 1e-300)
+        assert float(np.linalg.norm(got - ref)) <= 1e-13 * scale
+
+
+def test_unsupported_configs_raise():
+    with pytest.raises(ValueError):
+        make_grid(NHQGConfig(Nx=32, Nz=8, float_dtype="float64"))  # 3/2 rule
+    with pytest.raises(ValueError):
+        make_grid(NHQGConfig(Nx=32, Nz=8, float_dtype="float32", horizontal_dealiasing="23_rule"))
+    with pytest.raises(ValueError):
+        make_grid(NHQGConfig(Nx=32, Nz=8, float_dtype="float64", horizontal_dealiasing="23_rule",
+                             q_boundary="neumann"))
+    with pytest.raises(ValueError):
+        make_grid(NHQGConfig(Nx=32, Nz=8, float_dtype="float64", horizontal_dealiasing="23_rule",
+                             gamma=1e-3, beta=0.5))
+
+
+def _header_symbols():
+    text = (ROOT / "include" / "nhqg_gpu.h").read_text()
+    return set(re.findall(r"^\s*(?:int|const char \*)\s*(nhqg_\w+)\s*\(", text, flags=re.M))
+
+
+def test_library_exports_header_symbols():
+    lib_path = nat.build()
+    lib = nat.load(lib_path)
+    declared = _header_symbols()
+    assert declared, "no declarations parsed from include/nhqg_gpu.h"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert declared == set(nat.SIGNATURES), declared ^ set(nat.SIGNATURES)
+    assert b"sm_103a" in lib.nhqg_version()
+
+
+def test_ctx_create_rejects_bad_descriptor():
+    lib = nat.load()
+    import ctypes
+    h = ctypes.c_void_p()
+    d = nat.GridDesc()
+    d.Nx, d.Nz = 30, 8  # 30 = 2*3*5: no radix-5 FFT
+    assert lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(h)) == 2  # NHQG_ERR_UNSUPPORTED
+    d.Nx = 32
+    assert lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(h)) == 1  # null tables
