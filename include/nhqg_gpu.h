@@ -148,6 +148,12 @@ int nhqg_get_device_status(nhqg_ctx *ctx, int reset);
 /* Number of kernel launches the last compute call issued (bench accounting). */
 int nhqg_last_launch_count(const nhqg_ctx *ctx);
 
+/* Per-kernel CUDA-event timing of subsequent calls (stream-ordered).
+ * nhqg_profile_report synchronises the device and writes one line per kernel
+ * class, "name launches total_ms", into buf, then clears the record. */
+int nhqg_profile_enable(nhqg_ctx *ctx, int on);
+int nhqg_profile_report(nhqg_ctx *ctx, char *buf, int buflen);
+
 /* Engine build identification string (static storage). */
 const char *nhqg_version(void);
 

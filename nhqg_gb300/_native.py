@@ -138,6 +138,8 @@ SIGNATURES = {
                                             ctypes.c_int, ctypes.c_void_p]),
     "nhqg_get_device_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nhqg_last_launch_count": (ctypes.c_int, [ctypes.c_void_p]),
+    "nhqg_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "nhqg_profile_report": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "nhqg_version": (ctypes.c_char_p, []),
 }
 

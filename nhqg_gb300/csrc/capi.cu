@@ -2,8 +2,10 @@
 // ARS(2,2,2) step orchestration and the per-operator entry points.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
+#include <string>
 #include <new>
 #include <vector>
 
@@ -26,6 +28,14 @@ struct nhqg_ctx {
 };
 
 namespace {
+
+#define PCK(name, call)                      \
+  do {                                        \
+    c->w.prof.begin(name, st);                \
+    cudaError_t e_ = (call);                  \
+    c->w.prof.end(st);                        \
+    if (e_ != cudaSuccess) return NHQG_ERR_CUDA; \
+  } while (0)
 
 #define CK(call)                                  \
   do {                                            \
@@ -75,6 +85,32 @@ CSR to_csr(const double* A, int n) {
 
 int full_index(const Dims& d, int r, int c) { return full_row(r, d.K, d.Nx) * d.Nk + c; }
 
+// exp(-2 pi i k / n) with the angle reduced to [0, pi/4] so that each
+// component comes from one correctly-rounded-in-practice libm call
+double2 twiddle(long k, long n) {
+  k %= n;
+  if (k < 0) k += n;
+  // 8 k / n in [0, 8): octant and reflected fraction
+  const long k8 = 8 * k;
+  const int oct = (int)(k8 / n);
+  long r = k8 - oct * n;                 // remainder in [0, n)
+  if (oct & 1) r = n - r;                // reflect inside the octant
+  const double a = (M_PI / 4.0) * (double)r / (double)n;  // in [0, pi/4]
+  const double c = std::cos(a), s = std::sin(a);
+  double cs, sn;                          // cos, sin of 2 pi k / n
+  switch (oct) {
+    case 0: cs = c;  sn = s;  break;
+    case 1: cs = s;  sn = c;  break;
+    case 2: cs = -s; sn = c;  break;
+    case 3: cs = -c; sn = s;  break;
+    case 4: cs = -c; sn = -s; break;
+    case 5: cs = -s; sn = -c; break;
+    case 6: cs = s;  sn = -c; break;
+    default: cs = c; sn = -s; break;
+  }
+  return make_double2(cs, -sn);
+}
+
 }  // namespace
 
 extern "C" {
@@ -105,6 +141,8 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   Params& p = c->p;
   p.d = make_dims(g->Nx, g->Nz);
   p.plan = plan;
+  p.plan_v = make_fft_plan(2 * g->Nz);
+  p.fast_dct = p.plan_v.npass > 0 && getenv("NHQG_DENSE_VERTICAL") == nullptr;
   p.advection = g->advection;
   p.closure = g->thermal_closure;
   p.exchange = g->exchange;
@@ -179,20 +217,20 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   // ---- FFT tables ----
   {
     std::vector<double2> tw(d.Nx);
-    for (int k = 0; k < d.Nx; ++k) {
-      // exp(-2 pi i k / Nx), argument reduced to the first octant for accuracy
-      const long num = k, den = d.Nx;
-      const double ang = 2.0 * M_PI * (double)num / (double)den;
-      double cs = std::cos(ang), sn = std::sin(ang);
-      if (4 * k == d.Nx) { cs = 0.0; sn = 1.0; }
-      if (2 * k == d.Nx) { cs = -1.0; sn = 0.0; }
-      if (4 * k == 3 * d.Nx) { cs = 0.0; sn = -1.0; }
-      tw[k] = make_double2(cs, -sn);
-    }
+    for (int k = 0; k < d.Nx; ++k) tw[k] = twiddle(k, d.Nx);
     std::vector<int> perm(d.Nx);
     make_fft_perm(plan, perm.data());
     UP(t.tw, tw.data(), d.Nx);
     UP(t.perm, perm.data(), d.Nx);
+  }
+  if (p.fast_dct) {
+    const int L = 2 * d.Nz;
+    std::vector<double2> tw(L);
+    for (int k = 0; k < L; ++k) tw[k] = twiddle(k, L);
+    std::vector<int> perm(L);
+    make_fft_perm(p.plan_v, perm.data());
+    UP(t.tw_v, tw.data(), L);
+    UP(t.perm_v, perm.data(), L);
   }
 
   // ---- vertical tables ----
@@ -325,6 +363,40 @@ int nhqg_get_device_status(nhqg_ctx* c, int reset) {
 
 int nhqg_last_launch_count(const nhqg_ctx* c) { return c ? c->launches : -1; }
 
+int nhqg_profile_enable(nhqg_ctx* c, int on) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  c->w.prof.on = on != 0;
+  c->w.prof.recs.clear();
+  c->w.prof.next = 0;
+  return NHQG_OK;
+}
+
+int nhqg_profile_report(nhqg_ctx* c, char* buf, int buflen) {
+  if (!c || !buf || buflen <= 0) return NHQG_ERR_BAD_ARG;
+  Profiler& pf = c->w.prof;
+  if (cudaDeviceSynchronize() != cudaSuccess) return NHQG_ERR_CUDA;
+  std::vector<std::string> names;
+  std::map<std::string, std::pair<int, double>> acc;
+  for (const auto& r : pf.recs) {
+    if (!r.b) continue;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess) return NHQG_ERR_CUDA;
+    auto it = acc.find(r.name);
+    if (it == acc.end()) { names.push_back(r.name); acc[r.name] = {1, ms}; }
+    else { it->second.first += 1; it->second.second += ms; }
+  }
+  std::string out;
+  char line[160];
+  for (const auto& n : names) {
+    std::snprintf(line, sizeof(line), "%s %d %.6f\n", n.c_str(), acc[n].first, acc[n].second);
+    out += line;
+  }
+  pf.recs.clear();
+  pf.next = 0;
+  std::snprintf(buf, (size_t)buflen, "%s", out.c_str());
+  return (int)out.size() < buflen ? NHQG_OK : NHQG_ERR_BAD_ARG;
+}
+
 }  // extern "C"
 
 // ============================================================== orchestration
@@ -335,9 +407,9 @@ cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
 int gather_state(nhqg_ctx* c, const nhqg_state* s, cudaStream_t st) {
   const Params& p = c->p;
   if (!s || !s->q_hat || !s->w_hat || !s->th_hat || !s->th_bar) return NHQG_ERR_BAD_ARG;
-  CK(launch_gather(p, (const double2*)s->q_hat, c->q0, p.d.P, c->w.status, st));
-  CK(launch_gather(p, (const double2*)s->w_hat, c->w0, p.d.G, c->w.status, st));
-  CK(launch_gather(p, (const double2*)s->th_hat, c->t0, p.d.G, c->w.status, st));
+  PCK("gather", launch_gather(p, (const double2*)s->q_hat, c->q0, p.d.P, c->w.status, st));
+  PCK("gather", launch_gather(p, (const double2*)s->w_hat, c->w0, p.d.G, c->w.status, st));
+  PCK("gather", launch_gather(p, (const double2*)s->th_hat, c->t0, p.d.G, c->w.status, st));
   CK(cudaMemcpyAsync(c->tb0, s->th_bar, p.d.P * sizeof(double), cudaMemcpyDeviceToDevice, st));
   c->launches += 3;
   return NHQG_OK;
@@ -347,9 +419,9 @@ int scatter_fields(nhqg_ctx* c, const double2* q, const double2* w, const double
                    const double* tb, nhqg_state* o, cudaStream_t st) {
   const Params& p = c->p;
   if (!o || !o->q_hat || !o->w_hat || !o->th_hat || !o->th_bar) return NHQG_ERR_BAD_ARG;
-  CK(launch_scatter(p, q, (double2*)o->q_hat, p.d.P, st));
-  CK(launch_scatter(p, w, (double2*)o->w_hat, p.d.G, st));
-  CK(launch_scatter(p, t, (double2*)o->th_hat, p.d.G, st));
+  PCK("scatter", launch_scatter(p, q, (double2*)o->q_hat, p.d.P, st));
+  PCK("scatter", launch_scatter(p, w, (double2*)o->w_hat, p.d.G, st));
+  PCK("scatter", launch_scatter(p, t, (double2*)o->th_hat, p.d.G, st));
   if (tb) {
     CK(cudaMemcpyAsync(o->th_bar, tb, p.d.P * sizeof(double), cudaMemcpyDeviceToDevice, st));
   } else {
@@ -382,12 +454,12 @@ int explicit_front(nhqg_ctx* c, const double2* q, const double2* w, const double
                    const double* tb, bool legacy_mean, double* Etb, double* Itb, bool need_q,
                    cudaStream_t st) {
   const Params& p = c->p;
-  CK(launch_vfwd(p, c->t, need_q ? q : nullptr, w, t, c->Qn, c->Wn, c->Tn, st));
+  PCK("vfwd", launch_vfwd(p, c->t, need_q ? q : nullptr, w, t, c->Qn, c->Wn, c->Tn, st));
   c->launches += 1;
   if (legacy_mean) {
     // <w theta>_xy on the padded grid equals the Parseval sum of the band-limited fields
-    CK(launch_parseval(p, c->Wn, c->Tn, p.d.P, c->flux, st));
-    CK(launch_mean_legacy_rhs(p, c->t, tb, c->flux, c->dtb, Etb, Itb, st));
+    PCK("parseval", launch_parseval(p, c->Wn, c->Tn, p.d.P, c->flux, st));
+    PCK("mean_1d", launch_mean_legacy_rhs(p, c->t, tb, c->flux, c->dtb, Etb, Itb, st));
     c->launches += 2;
   }
   return horizontal_step(c, c->Qn, c->Wn, c->Tn, st);
@@ -404,8 +476,8 @@ VArgs base_vargs(nhqg_ctx* c) {
 
 int solve_back(nhqg_ctx* c, double2* qo, double2* wo, double2* to, bool zero_mean, cudaStream_t st) {
   const Params& p = c->p;
-  CK(launch_shell(p, c->t, c->rhs, wo, st));
-  CK(launch_vpost(p, c->t, c->Rq, c->Rt, wo, qo, to, zero_mean, st));
+  PCK("shell_solve", launch_shell(p, c->t, c->rhs, wo, st));
+  PCK("vpost", launch_vpost(p, c->t, c->Rq, c->Rt, wo, qo, to, zero_mean, st));
   c->launches += 2;
   return NHQG_OK;
 }
@@ -431,11 +503,11 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
   a.q0 = c->q0; a.w0 = c->w0; a.t0 = c->t0;
   a.dtb_nodal = legacy_mean ? c->dtb : nullptr;
   a.alpha = alpha;
-  CK(launch_vback(p, c->t, VB_STAGE1, a, st));
+  PCK("vback_stage1", launch_vback(p, c->t, VB_STAGE1, a, st));
   MeanArgs m1{};
   m1.tb0 = c->tb0; m1.E1tb = legacy_mean ? c->E1tb : nullptr; m1.out = c->tb1p;
   m1.alpha = alpha; m1.stage = 1; m1.closure = base_closure;
-  CK(launch_mean_stage(p, c->t, m1, st));
+  PCK("mean_1d", launch_mean_stage(p, c->t, m1, st));
   c->launches += 2;
   if ((rc = solve_back(c, c->Q1, c->W1, c->T1p, false, st))) return rc;
 
@@ -458,7 +530,7 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
   // ---------------- stage 2
   if (have_nodal_wt) {
     // nodal w and theta of state1 come out of the corrector
-    CK(launch_vfwd(p, c->t, c->Q1, nullptr, nullptr, c->Qn, nullptr, nullptr, st));
+    PCK("vfwd", launch_vfwd(p, c->t, c->Q1, nullptr, nullptr, c->Qn, nullptr, nullptr, st));
     c->launches += 1;
     if ((rc = horizontal_step(c, c->Qn, c->Wcgl, c->Tcgl, st))) return rc;
   } else {
@@ -474,14 +546,14 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
   a.c_E2 = dt * (1.0 - delta);
   a.omega = omega;
   a.inv_alpha_c = (pc && evolve) ? 1.0 / alpha : 0.0;
-  CK(launch_vback(p, c->t, VB_STAGE2, a, st));
+  PCK("vback_stage2", launch_vback(p, c->t, VB_STAGE2, a, st));
   MeanArgs m2{};
   m2.tb0 = c->tb0; m2.E1tb = legacy_mean ? c->E1tb : nullptr; m2.E2tb = legacy_mean ? c->E2tb : nullptr;
   m2.tb1 = tb1; m2.tb1p = c->tb1p; m2.out = c->tb2p;
   m2.c_E1 = dt * delta; m2.c_E2 = dt * (1.0 - delta); m2.omega = omega;
   m2.inv_alpha_c = (pc && evolve) ? 1.0 / alpha : 0.0;
   m2.stage = 2; m2.closure = base_closure; m2.itend = legacy_mean ? 1 : 0;
-  CK(launch_mean_stage(p, c->t, m2, st));
+  PCK("mean_1d", launch_mean_stage(p, c->t, m2, st));
   c->launches += 2;
   // balanced_sbp2 (split, not pc) finalizes the base step before its corrector
   const bool split_plain = split && !pc && evolve;
@@ -496,14 +568,14 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
     ca.wcgl = c->Wcgl; ca.wsbp = c->Wsbp; ca.tsbp = c->Tsbp; ca.tcgl = nullptr;
     ca.total_dt = pc ? alpha : dt;
     if (split_plain) {  // the base step's finalize zeroed the k=0 mode of w
-      CK(launch_zero_mode0(p, c->W2, p.d.G, st));
+      PCK("finalize", launch_zero_mode0(p, c->W2, p.d.G, st));
       c->launches += 1;
     }
     CK(run_corrector(p, c->t, c->w, ca, st, &c->launches));
     t2 = c->T2;
     tb2 = c->tb2;
   }
-  CK(launch_finalize(p, c->Q2, c->W2, t2, c->q0, c->w0, c->t0, st));
+  PCK("finalize", launch_finalize(p, c->Q2, c->W2, t2, c->q0, c->w0, c->t0, st));
   CK(cudaMemcpyAsync(c->tb0, tb2, p.d.P * sizeof(double), cudaMemcpyDeviceToDevice, st));
   c->launches += 1;
   return NHQG_OK;

@@ -12,14 +12,21 @@
 // The 1-D system A = I - half (pentadiagonal: D1 diag(<w^2>) D1 and the SBP
 // Laplacian) is factored once per corrector without pivoting: it is the
 // identity plus a weakly diagonally dominant M-matrix-like term.
+#include "column.cuh"
 #include "engine.h"
 
 namespace nhqg {
 
 namespace {
 
-constexpr int TM = 8;
-constexpr int NT = 256;
+using col::TM;
+using col::NT;
+using col::tload;
+using col::tstore;
+using col::tmat;
+using col::tcsr;
+using col::tpinv_dir;
+using col::tdct;
 
 // offsets inside Work::vec (doubles), each block P long unless noted
 struct CV {
@@ -45,6 +52,7 @@ struct CK {
   bool mixed;
   const double *wa, *wb;
   const double *V, *Vinv;
+  col::Dct dct;
   const int *c2s_ptr, *c2s_col, *s2c_ptr, *s2c_col;
   const double *c2s_val, *s2c_val;
   const double *bcF, *bcV, *proj, *D1, *Lsbp;
@@ -57,6 +65,7 @@ CK make_ck(const Params& p, const Tables& t) {
   k.mixed = t.wst_a != nullptr;
   k.wa = t.wst_a; k.wb = t.wst_b;
   k.V = t.V; k.Vinv = t.Vinv;
+  k.dct = make_dct(p, t);
   k.c2s_ptr = t.c2s_ptr; k.c2s_col = t.c2s_col; k.c2s_val = t.c2s_val;
   k.s2c_ptr = t.s2c_ptr; k.s2c_col = t.s2c_col; k.s2c_val = t.s2c_val;
   k.bcF = t.bcF; k.bcV = t.bcV; k.proj = t.proj; k.D1 = t.D1; k.Lsbp = t.Lsbp;
@@ -65,50 +74,6 @@ CK make_ck(const Params& p, const Tables& t) {
   return k;
 }
 
-__device__ __forceinline__ void tload(double2* b, const double2* __restrict__ src, int nlev,
-                                      int m0, int M) {
-  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
-    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
-    b[i] = (m < M) ? src[(size_t)l * M + m] : czero();
-  }
-}
-__device__ __forceinline__ void tstore(const double2* b, double2* __restrict__ dst, int nlev,
-                                       int m0, int M) {
-  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
-    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
-    if (m < M) dst[(size_t)l * M + m] = b[i];
-  }
-}
-__device__ __forceinline__ void tmat(double2* out, const double2* in, const double* __restrict__ Mat,
-                                     int ld, int nout, int nin) {
-  for (int idx = threadIdx.x; idx < nout * TM; idx += blockDim.x) {
-    const int i = idx / TM, mm = idx - i * TM;
-    const double* row = Mat + (size_t)i * ld;
-    double ax = 0.0, ay = 0.0;
-    for (int j = 0; j < nin; ++j) {
-      const double v = __ldg(row + j);
-      const double2 x = in[j * TM + mm];
-      ax = fma(v, x.x, ax);
-      ay = fma(v, x.y, ay);
-    }
-    out[idx] = make_double2(ax, ay);
-  }
-}
-__device__ __forceinline__ void tcsr(double2* out, const double2* in, const int* __restrict__ ptr,
-                                     const int* __restrict__ col, const double* __restrict__ val,
-                                     int nrow) {
-  for (int idx = threadIdx.x; idx < nrow * TM; idx += blockDim.x) {
-    const int i = idx / TM, mm = idx - i * TM;
-    double ax = 0.0, ay = 0.0;
-    for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
-      const double v = val[q];
-      const double2 x = in[col[q] * TM + mm];
-      ax = fma(v, x.x, ax);
-      ay = fma(v, x.y, ay);
-    }
-    out[idx] = make_double2(ax, ay);
-  }
-}
 __device__ __forceinline__ void tstencil(const CK& k, bool wbasis, double2* c, const double2* x) {
   const bool mixed = wbasis && k.mixed;
   for (int idx = threadIdx.x; idx < k.P * TM; idx += blockDim.x) {
@@ -125,34 +90,19 @@ __device__ __forceinline__ void tstencil(const CK& k, bool wbasis, double2* c, c
     c[idx] = v;
   }
 }
-__device__ __forceinline__ void tpinv_dir(double2* x, const double2* c, int G) {
-  const int t = threadIdx.x;
-  if (t < 2 * TM) {
-    const int mm = t >> 1;
-    const bool im = t & 1;
-    double xm2 = 0.0, xm1 = 0.0;
-    for (int n = 0; n < G; ++n) {
-      const double cv = im ? c[n * TM + mm].y : c[n * TM + mm].x;
-      const double xn = xm2 - cv;
-      if (im) x[n * TM + mm].y = xn; else x[n * TM + mm].x = xn;
-      xm2 = xm1;
-      xm1 = xn;
-    }
-  }
-}
-
 // ------------------------------------------------------------ per-mode kernels
 __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const double2* tp,
                                                  double2* wcgl, double2* wsbp, double2* tsbp) {
   extern __shared__ double2 sm[];
   const int PT = k.P * TM;
   double2 *b0 = sm, *b1 = sm + PT;
+  const col::DctShared ds = col::dct_shared(k.dct, sm + 2 * PT);
   const int m0 = blockIdx.x * TM;
   tload(b0, wp, k.G, m0, k.M);
   __syncthreads();
   tstencil(k, true, b1, b0);
   __syncthreads();
-  tmat(b0, b1, k.V, k.P, k.P, k.P);
+  tdct(b0, b1, k.dct, ds, false, k.P);
   __syncthreads();
   tstore(b0, wcgl, k.P, m0, k.M);
   tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
@@ -163,7 +113,7 @@ __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const 
   __syncthreads();
   tstencil(k, false, b1, b0);
   __syncthreads();
-  tmat(b0, b1, k.V, k.P, k.P, k.P);
+  tdct(b0, b1, k.dct, ds, false, k.P);
   __syncthreads();
   tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
   __syncthreads();
@@ -176,6 +126,7 @@ __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const doub
   extern __shared__ double2 sm[];
   const int PT = k.P * TM;
   double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT;
+  const col::DctShared ds = col::dct_shared(k.dct, sm + 4 * PT);
   __shared__ double2 delta[2 * TM];
   const int m0 = blockIdx.x * TM;
   const int P = k.P;
@@ -214,7 +165,7 @@ __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const doub
   }
   if (last) {
     __syncthreads();
-    tmat(b0, b2, k.Vinv, P, k.G, P);  // first G Chebyshev coefficients of V^-1 y
+    tdct(b0, b2, k.dct, ds, true, k.G);  // first G Chebyshev coefficients of V^-1 y
     __syncthreads();
     tpinv_dir(b1, b0, k.G);
     __syncthreads();
@@ -481,21 +432,40 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   const int nsub = p.substeps > 0 ? p.substeps : 1;
   const double sub_dt = a.total_dt / nsub;
   const int grid = (p.d.M + TM - 1) / TM;
-  const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2);
-  const size_t sm4 = 4 * (size_t)p.d.P * TM * sizeof(double2);
+  const size_t dsm = (size_t)col::dct_smem_elems(k.dct) * sizeof(double2);
+  const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2) + dsm;
+  const size_t sm4 = 4 * (size_t)p.d.P * TM * sizeof(double2) + dsm;
   cudaFuncSetAttribute(k_corr_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
   cudaFuncSetAttribute(k_corr_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+  Profiler& pf = w.prof;
+  pf.begin("corr_pre", st);
   k_corr_pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp);
+  pf.end(st);
+  pf.begin("parseval", st);
   launch_parseval(p, a.wsbp, a.wsbp, p.d.P, w.vec + cv.w2(), st);
+  pf.end(st);
+  pf.begin("parseval", st);
   launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), st);
+  pf.end(st);
+  pf.begin("corr_init_1d", st);
   k_corr_init<<<1, NT, 0, st>>>(k, w.vec, a.tbp, sub_dt);
+  pf.end(st);
   int n = 4;
   for (int s = 0; s < nsub; ++s) {
     const int last = (s == nsub - 1);
-    if (s > 0) { launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), st); ++n; }
+    if (s > 0) {
+      pf.begin("parseval", st);
+      launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), st);
+      pf.end(st);
+      ++n;
+    }
+    pf.begin("corr_step_1d", st);
     k_corr_tstep<<<1, NT, 0, st>>>(k, w.vec, sub_dt, last, a.tb_out);
+    pf.end(st);
+    pf.begin("corr_sub", st);
     k_corr_sub<<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt, last,
                                       a.t_out, a.tcgl);
+    pf.end(st);
     n += 2;
   }
   if (nlaunch) *nlaunch += n;

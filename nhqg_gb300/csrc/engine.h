@@ -27,6 +27,9 @@ struct Tables {
   // FFT over Nx
   double2* tw = nullptr;  // [Nx]
   int* perm = nullptr;    // [Nx]
+  // FFT over 2*Nz (DCT-I of the vertical columns)
+  double2* tw_v = nullptr;  // [2Nz]
+  int* perm_v = nullptr;    // [2Nz]
   // vertical operators
   double *V = nullptr, *Vinv = nullptr;        // [P*P]
   double *wst_a = nullptr, *wst_b = nullptr;   // mixed w stencil a_n, b_n [G]; null = Dirichlet
@@ -55,10 +58,29 @@ struct Tables {
 struct Params {
   Dims d;
   FftPlan plan;
+  FftPlan plan_v;  // length 2*Nz; npass <= 0 -> dense vertical transforms
+  bool fast_dct;
   int advection, closure, exchange, wbc, substeps;
   double dt, gamma_imex, Ra_sigma, sigma, beta, eps_sq;
   bool has_eta, has_sponge;
 };
+
+}  // namespace nhqg
+#include "column.cuh"
+namespace nhqg {
+
+inline col::Dct make_dct(const Params& p, const Tables& t) {
+  col::Dct d;
+  d.N = p.d.Nz;
+  d.P = p.d.P;
+  d.fast = p.fast_dct;
+  d.plan = p.plan_v;
+  d.tw = t.tw_v;
+  d.perm = t.perm_v;
+  d.V = t.V;
+  d.Vinv = t.Vinv;
+  return d;
+}
 
 // Horizontal product launch description.
 enum HForm { HF_FLUX = 0, HF_JAC = 1, HF_SPONGE = 2 };
@@ -75,7 +97,36 @@ struct HorizArgs {
   double2 *Aq, *Aw, *Ath;
 };
 
+// Optional per-kernel CUDA-event timing (stream-ordered, read after a sync).
+struct Profiler {
+  bool on = false;
+  struct Rec { const char* name; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  size_t next = 0;
+  cudaEvent_t get() {
+    if (next == pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pool.push_back(e);
+    }
+    return pool[next++];
+  }
+  void begin(const char* name, cudaStream_t st) {
+    if (!on) return;
+    Rec r{name, get(), nullptr};
+    cudaEventRecord(r.a, st);
+    recs.push_back(r);
+  }
+  void end(cudaStream_t st) {
+    if (!on || recs.empty()) return;
+    recs.back().b = get();
+    cudaEventRecord(recs.back().b, st);
+  }
+};
+
 struct Work {
+  Profiler prof;
   // H1 / H2 intermediates
   double2* x1 = nullptr;  size_t x1_elems = 0;
   double2* x2 = nullptr;  size_t x2_elems = 0;

@@ -347,11 +347,17 @@ cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const H
   cudaFuncSetAttribute(k_h2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
   cudaFuncSetAttribute(k_h3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
   dim3 g1((k.cols_in + CB1 - 1) / CB1, a.levels);
+  w.prof.begin("h1_col_ifft", st);
   k_h1<<<g1, 256, sm1, st>>>(k, CB1);
+  w.prof.end(st);
   dim3 g2(d.Nx / RB, a.levels);
+  w.prof.begin("h2_row_products", st);
   k_h2<<<g2, 256, sm2, st>>>(k, RB);
+  w.prof.end(st);
   dim3 g3((d.Mc + CB3 - 1) / CB3, a.levels);
+  w.prof.begin("h3_col_fft", st);
   k_h3<<<g3, 256, sm3, st>>>(k, CB3);
+  w.prof.end(st);
   if (nlaunch) *nlaunch += 3;
   return cudaGetLastError();
 }

@@ -14,20 +14,28 @@
 // pinv_w(proj_w(x)) == pinv_w(x) because pinv reads only the first Nz-1
 // Chebyshev coefficients and the tau projection rewrites only the last two,
 // so the tau projections that feed a pinv are not applied.
+#include "column.cuh"
 #include "engine.h"
 
 namespace nhqg {
 
 namespace {
 
-constexpr int TM = 8;      // modes per CTA
-constexpr int NT = 256;    // threads per CTA
+using col::TM;
+using col::NT;
+using col::tload;
+using col::tstore;
+using col::tmat;
+using col::tstencil_dir;
+using col::tpinv_dir;
+using col::tgz;
+using col::tdct;
 
 struct VK {
   int P, G, N, M, Mr, Mc, K, Nx, Nk;
   bool mixed;                 // open-top (Neumann) w basis
   const double *wa, *wb;      // mixed stencil coefficients
-  const double *V, *Vinv;
+  col::Dct dct;
   const double *kx, *inv_denom, *inv_aq, *inv_at, *drq, *drw, *drt;
   double beta, Ra, gdt;
 };
@@ -38,118 +46,20 @@ VK make_vk(const Params& p, const Tables& t) {
   k.K = p.d.K; k.Nx = p.d.Nx; k.Nk = p.d.Nk;
   k.mixed = t.wst_a != nullptr;
   k.wa = t.wst_a; k.wb = t.wst_b;
-  k.V = t.V; k.Vinv = t.Vinv;
+  k.dct = make_dct(p, t);
   k.kx = t.kx; k.inv_denom = t.inv_denom; k.inv_aq = t.inv_aq; k.inv_at = t.inv_at;
   k.drq = t.drq; k.drw = t.drw; k.drt = t.drt;
   k.beta = p.beta; k.Ra = p.Ra_sigma; k.gdt = p.gamma_imex * p.dt;
   return k;
 }
 
-// ---- tile helpers: buffers are [level][TM] ----
-__device__ __forceinline__ void tload(double2* b, const double2* __restrict__ src, int nlev,
-                                      int m0, int M) {
-  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
-    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
-    b[i] = (m < M) ? src[(size_t)l * M + m] : czero();
-  }
-}
-__device__ __forceinline__ void tstore(const double2* b, double2* __restrict__ dst, int nlev,
-                                       int m0, int M) {
-  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
-    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
-    if (m < M) dst[(size_t)l * M + m] = b[i];
-  }
-}
-// out[i] = sum_{j<nin} Mat[i*ld + j] in[j], i < nout
-__device__ __forceinline__ void tmat(double2* out, const double2* in, const double* __restrict__ Mat,
-                                     int ld, int nout, int nin) {
-  for (int idx = threadIdx.x; idx < nout * TM; idx += blockDim.x) {
-    const int i = idx / TM, mm = idx - i * TM;
-    const double* row = Mat + (size_t)i * ld;
-    double ax = 0.0, ay = 0.0;
-    for (int j = 0; j < nin; ++j) {
-      const double v = __ldg(row + j);
-      const double2 x = in[j * TM + mm];
-      ax = fma(v, x.x, ax);
-      ay = fma(v, x.y, ay);
-    }
-    out[idx] = make_double2(ax, ay);
-  }
-}
-// Dirichlet stencil: c_n = -x_n + x_{n-2}   (x has G = N-1 entries, c has P)
-__device__ __forceinline__ void tstencil_dir(double2* c, const double2* x, int P, int G) {
-  for (int idx = threadIdx.x; idx < P * TM; idx += blockDim.x) {
-    const int n = idx / TM, mm = idx - n * TM;
-    double2 v = (n < G) ? cneg(x[n * TM + mm]) : czero();
-    if (n >= 2 && n - 2 < G) v = cadd(v, x[(n - 2) * TM + mm]);
-    c[idx] = v;
-  }
-}
-// w stencil: Dirichlet, or the open-top basis T_n + a_n T_{n+1} + b_n T_{n+2}
 __device__ __forceinline__ void tstencil_w(const VK& k, double2* c, const double2* x) {
-  if (!k.mixed) { tstencil_dir(c, x, k.P, k.G); return; }
-  for (int idx = threadIdx.x; idx < k.P * TM; idx += blockDim.x) {
-    const int n = idx / TM, mm = idx - n * TM;
-    double2 v = (n < k.G) ? x[n * TM + mm] : czero();
-    if (n >= 1 && n - 1 < k.G) v = caxpy(__ldg(k.wa + n - 1), x[(n - 1) * TM + mm], v);
-    if (n >= 2 && n - 2 < k.G) v = caxpy(__ldg(k.wb + n - 2), x[(n - 2) * TM + mm], v);
-    c[idx] = v;
-  }
-}
-// exact left inverse of the Dirichlet stencil: x_n = x_{n-2} - c_n, n < G
-__device__ __forceinline__ void tpinv_dir(double2* x, const double2* c, int G) {
-  const int t = threadIdx.x;
-  if (t < 2 * TM) {
-    const int mm = t >> 1;
-    const bool im = t & 1;
-    double xm2 = 0.0, xm1 = 0.0;
-    for (int n = 0; n < G; ++n) {
-      const double cv = im ? c[n * TM + mm].y : c[n * TM + mm].x;
-      const double xn = xm2 - cv;
-      if (im) x[n * TM + mm].y = xn; else x[n * TM + mm].x = xn;
-      xm2 = xm1;
-      xm1 = xn;
-    }
-  }
+  if (!k.mixed) tstencil_dir(c, x, k.P, k.G);
+  else col::tstencil_mixed(c, x, k.P, k.G, k.wa, k.wb);
 }
 __device__ __forceinline__ void tpinv_w(const VK& k, double2* x, const double2* c) {
-  if (!k.mixed) { tpinv_dir(x, c, k.G); return; }
-  const int t = threadIdx.x;
-  if (t < 2 * TM) {
-    const int mm = t >> 1;
-    const bool im = t & 1;
-    double xm2 = 0.0, xm1 = 0.0;
-    for (int n = 0; n < k.G; ++n) {
-      double v = im ? c[n * TM + mm].y : c[n * TM + mm].x;
-      if (n >= 1) v = fma(-__ldg(k.wa + n - 1), xm1, v);
-      if (n >= 2) v = fma(-__ldg(k.wb + n - 2), xm2, v);
-      if (im) x[n * TM + mm].y = v; else x[n * TM + mm].x = v;
-      xm2 = xm1;
-      xm1 = v;
-    }
-  }
-}
-// d/dZ on Chebyshev coefficients (G_Z = 2 G_xi), backward recurrence
-__device__ __forceinline__ void tgz(double2* b, const double2* a, int N) {
-  const int t = threadIdx.x;
-  if (t < 2 * TM) {
-    const int mm = t >> 1;
-    const bool im = t & 1;
-    auto A = [&](int n) { return im ? a[n * TM + mm].y : a[n * TM + mm].x; };
-    auto S = [&](int n, double v) { if (im) b[n * TM + mm].y = v; else b[n * TM + mm].x = v; };
-    S(N, 0.0);
-    double bk2 = 0.0;                      // b_{k+2}
-    double bk1 = 4.0 * N * A(N);           // b_{N-1}
-    S(N - 1, bk1);
-    for (int kk = N - 2; kk >= 1; --kk) {
-      const double bk = fma(4.0 * (kk + 1), A(kk + 1), bk2);
-      S(kk, bk);
-      bk2 = bk1;
-      bk1 = bk;
-    }
-    // b_0 = b_2 / 2 + 2 a_1
-    S(0, fma(0.5, bk2, 2.0 * A(1)));
-  }
+  if (!k.mixed) tpinv_dir(x, c, k.G);
+  else col::tpinv_mixed(x, c, k.G, k.wa, k.wb);
 }
 
 __device__ __forceinline__ int mode_of(int idx, int m0) { return m0 + (idx % TM); }
@@ -161,11 +71,12 @@ __global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const doubl
   extern __shared__ double2 sm[];
   double2* b0 = sm;
   double2* b1 = sm + k.P * TM;
+  const col::DctShared ds = col::dct_shared(k.dct, sm + 2 * k.P * TM);
   const int m0 = blockIdx.x * TM;
   if (q) {
     tload(b0, q, k.P, m0, k.M);
     __syncthreads();
-    tmat(b1, b0, k.V, k.P, k.P, k.P);
+    tdct(b1, b0, k.dct, ds, false, k.P);
     __syncthreads();
     tstore(b1, qn, k.P, m0, k.M);
     __syncthreads();
@@ -175,7 +86,7 @@ __global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const doubl
     __syncthreads();
     tstencil_w(k, b1, b0);
     __syncthreads();
-    tmat(b0, b1, k.V, k.P, k.P, k.P);
+    tdct(b0, b1, k.dct, ds, false, k.P);
     __syncthreads();
     tstore(b0, wn, k.P, m0, k.M);
     __syncthreads();
@@ -185,7 +96,7 @@ __global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const doubl
     __syncthreads();
     tstencil_dir(b1, b0, k.P, k.G);
     __syncthreads();
-    tmat(b0, b1, k.V, k.P, k.P, k.P);
+    tdct(b0, b1, k.dct, ds, false, k.P);
     __syncthreads();
     tstore(b0, tn, k.P, m0, k.M);
   }
@@ -197,6 +108,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   extern __shared__ double2 sm[];
   const int PT = k.P * TM;
   double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT, *b4 = sm + 4 * PT;
+  const col::DctShared ds = col::dct_shared(k.dct, sm + 5 * PT);
   const int m0 = blockIdx.x * TM;
   const int P = k.P, G = k.G, M = k.M;
   const size_t Ms = (size_t)M;
@@ -205,7 +117,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   if (MODE != VB_SOLVE) {
     tload(b0, a.Aq, P, m0, M);
     __syncthreads();
-    tmat(b1, b0, k.Vinv, P, P, P);
+    tdct(b1, b0, k.dct, ds, true, P);
     __syncthreads();
     // E_q = -Aq - i beta kx psi, psi = -inv_denom * q_state
     const double2* qs = (MODE == VB_STAGE2) ? a.q1 : a.q0;
@@ -276,7 +188,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   if (MODE != VB_SOLVE) {
     tload(b0, a.Aw, P, m0, M);
     __syncthreads();
-    tmat(b1, b0, k.Vinv, P, P, P);
+    tdct(b1, b0, k.dct, ds, true, P);
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
     __syncthreads();
@@ -339,7 +251,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
       }
       __syncthreads();
     }
-    tmat(b1, b0, k.Vinv, P, P, P);
+    tdct(b1, b0, k.dct, ds, true, P);
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
     __syncthreads();
@@ -655,7 +567,11 @@ __global__ void k_zero_mode0(double2* f, int levels, int M) {
     f[(size_t)l * M] = czero();
 }
 
-inline size_t vsmem(const Params& p, int nbuf) { return (size_t)nbuf * p.d.P * TM * sizeof(double2); }
+inline size_t vsmem(const Params& p, int nbuf, bool dct = false) {
+  size_t e = (size_t)nbuf * p.d.P * TM;
+  if (dct) e += (size_t)col::dct_smem_elems(make_dct(p, Tables{}));
+  return e * sizeof(double2);
+}
 inline int vgrid(const Params& p) { return (p.d.M + TM - 1) / TM; }
 
 }  // namespace
@@ -663,7 +579,7 @@ inline int vgrid(const Params& p) { return (p.d.M + TM - 1) / TM; }
 cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, const double2* w,
                         const double2* th, double2* qn, double2* wn, double2* tn, cudaStream_t st) {
   VK k = make_vk(p, t);
-  const size_t sm = vsmem(p, 2);
+  const size_t sm = vsmem(p, 2, true);
   cudaFuncSetAttribute(k_vfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_vfwd<<<vgrid(p), NT, sm, st>>>(k, q, w, th, qn, wn, tn);
   return cudaGetLastError();
@@ -671,7 +587,7 @@ cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, cons
 
 cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st) {
   VK k = make_vk(p, t);
-  const size_t sm = vsmem(p, 5);
+  const size_t sm = vsmem(p, 5, true);
   switch (mode) {
     case VB_RHS:
       cudaFuncSetAttribute(k_vback<VB_RHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);

@@ -109,6 +109,19 @@ class Engine:
     def device_status(self, reset: bool = True) -> int:
         return int(self.lib.nhqg_get_device_status(self.handle, 1 if reset else 0))
 
+    def profile(self, on: bool) -> None:
+        nat.check(self.lib.nhqg_profile_enable(self.handle, 1 if on else 0), "nhqg_profile_enable")
+
+    def profile_report(self) -> dict[str, tuple[int, float]]:
+        """{kernel class: (launches, total ms)} since profile(True)."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        nat.check(self.lib.nhqg_profile_report(self.handle, buf, len(buf)), "nhqg_profile_report")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.split()
+            out[name] = (int(n), float(ms))
+        return out
+
     def launches(self) -> int:
         return int(self.lib.nhqg_last_launch_count(self.handle))
 

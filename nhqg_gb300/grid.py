@@ -19,8 +19,6 @@ row, -1 outside the band; ``ksq_idx`` keeps the reference's shell numbering.
 
 from __future__ import annotations
 
-import os
-from concurrent.futures import ThreadPoolExecutor
 from typing import NamedTuple
 
 import numpy as np
@@ -196,7 +194,7 @@ def _shell_inverse(kv, hyper_order, gamma, dt, nu_q, nu_w, nu_theta, drag, sigma
     return np.linalg.inv(couple - (gamma * dt) ** 2 * c_k * B)
 
 
-def make_grid(cfg: NHQGConfig, threads: int | None = None) -> Grid:
+def make_grid(cfg: NHQGConfig) -> Grid:
     """Build the Grid of ``cfg`` (nhqg/grid.py:439-789)."""
     if cfg.float_dtype != "float64":
         raise ValueError("the GPU time step computes in float64; set float_dtype='float64'")
@@ -354,16 +352,10 @@ def make_grid(cfg: NHQGConfig, threads: int | None = None) -> Grid:
             cfg.Ld_inv_sq, WG, G_Z, w_stencil, N - 1, buoyancy_K)
     imex_inv = np.empty((len(used), N - 1, N - 1))
 
-    def build(i):
+    # one shell at a time: the BLAS inside each product is already threaded
+    # (host threads around threaded BLAS calls oversubscribe the cores)
+    for i in range(len(used)):
         imex_inv[i] = _shell_inverse(unique_ksq[used[i]], *args)
-
-    nthreads = threads or int(os.environ.get("NHQG_GRID_THREADS", "0")) or (os.cpu_count() or 1)
-    if len(used) > 64 and nthreads > 1:
-        with ThreadPoolExecutor(max_workers=nthreads) as ex:
-            list(ex.map(build, range(len(used))))
-    else:
-        for i in range(len(used)):
-            build(i)
 
     mean_solve = None
     if cfg.thermal_closure == "evolve_mean" and cfg.mean_exchange_discretization == "legacy":

@@ -654,36 +654,60 @@ def implicit_tendency(state: OracleState, grid: OracleGrid) -> OracleState:
 
 
 def _shell_inverse_lookup(grid: OracleGrid, shells: np.ndarray) -> np.ndarray:
+    """A'^-1 for the given shell ids (built lazily when the grid was made
+    without the table)."""
     if grid.imex_inv is not None:
         return grid.imex_inv[shells]
     cache = grid.__dict__.setdefault("_shell_cache", {})
     missing = [int(s) for s in np.unique(shells) if int(s) not in cache]
     if missing:
         c = grid.cfg
-        ksq_rounded = np.round(grid.ksq.ravel(), decimals=8)
-        uniq = np.unique(ksq_rounded)
-        sub = uniq[missing]
+        uniq = np.unique(np.round(grid.ksq.ravel(), decimals=8))
         bK = None if grid.map_th_to_w is None else grid.map_th_to_w @ grid.map_w_to_th
         inv, _ = build_shell_inverses(
-            grid.G_Z, grid.w_stencil, grid.w_pinv, sub, c.Ld_inv_sq, grid.dt,
+            grid.G_Z, grid.w_stencil, grid.w_pinv, uniq[missing], c.Ld_inv_sq, grid.dt,
             grid.gamma_imex, grid.Nz, c.nu_q, c.nu_w, c.nu_theta, c.sigma,
             grid.Ra_sigma, c.drag, c.hyper_order, bK)
         for s, m in zip(missing, inv):
             cache[s] = m
-    return np.stack([cache[int(s)] for s in shells.ravel()]).reshape(shells.shape + cache[int(shells.ravel()[0])].shape)
+    flat = np.asarray(shells).ravel()
+    out = np.stack([cache[int(s)] for s in flat])
+    return out.reshape(np.shape(shells) + out.shape[1:])
 
 
-def per_shell_matmul(grid: OracleGrid, field: np.ndarray, rows_per_chunk: int = 8) -> np.ndarray:
-    """Apply A'^-1[shell(k)] to each mode's column, in kx-row chunks
-    (nhqg/solver.py:648-675; the chunked path bounds the gather)."""
-    f_t = np.transpose(field, (1, 2, 0))  # (Nx, Nk, m)
-    out = np.empty_like(f_t)
-    Nx = f_t.shape[0]
-    for r0 in range(0, Nx, rows_per_chunk):
-        idx = grid.ksq_idx[r0:r0 + rows_per_chunk]
-        mats = _shell_inverse_lookup(grid, idx)
-        out[r0:r0 + rows_per_chunk] = np.einsum("abij,abj->abi", mats, f_t[r0:r0 + rows_per_chunk])
-    return np.transpose(out, (2, 0, 1))
+def _shell_groups(grid: OracleGrid):
+    """Modes grouped by shell: (shell ids, start offsets, flat mode order)."""
+    g = grid.__dict__.get("_shell_groups")
+    if g is None:
+        idx = grid.ksq_idx.ravel()
+        order = np.argsort(idx, kind="stable")
+        shells, starts = np.unique(idx[order], return_index=True)
+        g = (shells, np.append(starts, idx.size), order)
+        grid.__dict__["_shell_groups"] = g
+    return g
+
+
+def per_shell_matmul(grid: OracleGrid, field: np.ndarray) -> np.ndarray:
+    """Apply A'^-1[shell(k)] to each mode's column (nhqg/solver.py:648-675).
+    Modes of one shell share the matrix, so each shell is one small GEMM
+    instead of the reference's gathered (Nx, Nk, m, m) batch; the products
+    are the same per mode."""
+    m = field.shape[0]
+    cols = np.ascontiguousarray(np.transpose(field, (1, 2, 0))).reshape(-1, m)
+    out = np.empty_like(cols)
+    shells, starts, order = _shell_groups(grid)
+    if grid.imex_inv is None:
+        _shell_inverse_lookup(grid, shells[:1])  # warm the lazy cache ...
+        cache = grid.__dict__["_shell_cache"]
+        if len(cache) < len(shells):             # ... for every shell at once
+            _shell_inverse_lookup(grid, shells)
+        table = [cache[int(s)] for s in shells]
+    else:
+        table = [grid.imex_inv[s] for s in shells]
+    for i, A in enumerate(table):
+        modes = order[starts[i]:starts[i + 1]]
+        out[modes] = cols[modes] @ A.T
+    return np.transpose(out.reshape(field.shape[1], field.shape[2], m), (2, 0, 1))
 
 
 def imex_implicit_solve(R_q, R_w, R_th, grid: OracleGrid):
