@@ -35,7 +35,8 @@ typedef enum nhqg_status {
   NHQG_ERR_UNSUPPORTED = 2,      /* configuration outside the GPU path */
   NHQG_ERR_CUDA = 3,             /* a CUDA runtime call failed */
   NHQG_ERR_DEVICE_TIMEOUT = 4,   /* a bounded device wait ran out */
-  NHQG_ERR_NOT_BAND_LIMITED = 5  /* input had content outside the 2/3 band */
+  NHQG_ERR_NOT_BAND_LIMITED = 5, /* input had content outside the 2/3 band */
+  NHQG_ERR_SCRATCH_TOO_SMALL = 6 /* one level does not fit the static scratch */
 } nhqg_status;
 
 enum { NHQG_ADV_FLUX = 0, NHQG_ADV_JACOBIAN = 1 };
@@ -127,6 +128,27 @@ int nhqg_triple_advection_23(nhqg_ctx *ctx, int advection, int levels,
                              const void *psi, const void *q, const void *w,
                              const void *th, void *Aq, void *Aw, void *Ath,
                              void *stream);
+
+/* Allocation-free variant of nhqg_triple_advection_23.  It has no
+ * counterpart in the reference.  It is for callers that must not allocate
+ * device memory themselves: XLA FFI handlers (all buffers come from XLA's
+ * allocator), code inside CUDA-graph capture, fixed device-memory pools.  No
+ * context is needed and nothing is allocated: the FFT tables and the H1/H2
+ * intermediates live in one static __device__ array of
+ * NHQG_NOALLOC_SCRATCH_BYTES per GPU, held from library load until process
+ * exit.  kx (Nx doubles) and ky (Nx/2+1 doubles) are device pointers with the
+ * reference's wavenumbers; planes as in nhqg_triple_advection_23.  Levels are
+ * processed in chunks that fit the array; Nx above 2048, or an Nx whose single
+ * level does not fit, returns NHQG_ERR_UNSUPPORTED / NHQG_ERR_SCRATCH_TOO_SMALL.
+ * The first call on each device sets up the array's address with that device
+ * current (make it before any stream capture).  All calls share the array, so
+ * calls that overlap on the GPU race on it. */
+#define NHQG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int nhqg_triple_advection_23_noalloc(int advection, int Nx, int levels,
+                                     const double *kx, const double *ky,
+                                     const void *psi, const void *q, const void *w,
+                                     const void *th, void *Aq, void *Aw, void *Ath,
+                                     void *stream);
 
 /* sponge_product_23 (nhqg/spectral.py:53-60) with the context's sponge. */
 int nhqg_sponge_product_23(nhqg_ctx *ctx, int levels, const void *f, void *out,

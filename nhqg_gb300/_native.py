@@ -21,14 +21,15 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libnhqg_gpu.so"
-SOURCES = ("horizontal.cu", "vertical.cu", "corrector.cu", "capi.cu")
+SOURCES = ("horizontal.cu", "vertical.cu", "corrector.cu", "capi.cu", "noalloc.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
 
 # status codes (include/nhqg_gpu.h)
 NHQG_OK = 0
 STATUS_NAMES = {0: "NHQG_OK", 1: "NHQG_ERR_BAD_ARG", 2: "NHQG_ERR_UNSUPPORTED", 3: "NHQG_ERR_CUDA",
-                4: "NHQG_ERR_DEVICE_TIMEOUT", 5: "NHQG_ERR_NOT_BAND_LIMITED"}
+                4: "NHQG_ERR_DEVICE_TIMEOUT", 5: "NHQG_ERR_NOT_BAND_LIMITED",
+                6: "NHQG_ERR_SCRATCH_TOO_SMALL"}
 DEVICE_STATUS_OOB = 1 << 0
 DEVICE_STATUS_TIMEOUT = 1 << 1
 
@@ -131,6 +132,8 @@ SIGNATURES = {
                                            ctypes.POINTER(StateDesc), ctypes.c_double, ctypes.c_void_p]),
     "nhqg_triple_advection_23": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] +
                                  [ctypes.c_void_p] * 7 + [ctypes.c_void_p]),
+    "nhqg_triple_advection_23_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] +
+                                         [ctypes.c_void_p] * 9 + [ctypes.c_void_p]),
     "nhqg_sponge_product_23": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p]),
     "nhqg_sanitize": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(StateDesc), ctypes.c_void_p]),
