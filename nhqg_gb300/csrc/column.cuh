@@ -23,6 +23,7 @@ struct Dct {
   bool fast;
   FftPlan plan;               // length 2N
   const double2* tw;          // [2N] global
+  const float2* tw_f;         // [2N] global, FP32 copy (mixed-precision path)
   const int* perm;            // [2N] global
   const double *V, *Vinv;     // dense fallback [P*P]
 };
@@ -98,22 +99,50 @@ __device__ __forceinline__ void tstencil_mixed(double2* c, const double2* x, int
     c[idx] = v;
   }
 }
-// exact left inverse of the Dirichlet stencil: x_n = x_{n-2} - c_n, n < G
-__device__ __forceinline__ void tpinv_dir(double2* x, const double2* c, int G) {
-  const int t = threadIdx.x;
-  if (t < 2 * TM) {
-    const int mm = t >> 1;
-    const bool im = t & 1;
-    double xm2 = 0.0, xm1 = 0.0;
-    for (int n = 0; n < G; ++n) {
-      const double cv = im ? c[n * TM + mm].y : c[n * TM + mm].x;
-      const double xn = xm2 - cv;
-      if (im) x[n * TM + mm].y = xn; else x[n * TM + mm].x = xn;
-      xm2 = xm1;
-      xm1 = xn;
-    }
+// Inclusive sums along one parity class of a strided column, one warp per
+// (mode, re/im) column; lanes 0-15 take even indices, lanes 16-31 odd ones.
+// get(n) reads element n (0 <= n < len), put(n, v) writes result n.  With
+// reverse = true the sums run from the top index down (suffix sums).
+template <typename Get, typename Put>
+__device__ __forceinline__ void warp_parity_scan(int len, bool reverse, Get get, Put put) {
+  const int lane = threadIdx.x & 31;
+  const int cls = lane >> 4;               // parity class
+  const int sl = lane & 15;                // lane within the class
+  const int m = (len - cls + 1) / 2;       // elements in this class
+  const int chunk = (m + 15) / 16;
+  const int j0 = sl * chunk;
+  const int j1 = min(m, j0 + chunk);
+  const int top = len - 1 - ((len - 1 - cls) & 1);  // highest index of this class
+  auto idx = [&](int j) { return reverse ? top - 2 * j : 2 * j + cls; };
+  double run = 0.0;
+  for (int j = j0; j < j1; ++j) run += get(idx(j));
+  // inclusive scan of the 16 chunk totals within each half-warp
+  double incl = run;
+  for (int o = 1; o < 16; o <<= 1) {
+    const double t = __shfl_up_sync(0xffffffffu, incl, o, 16);
+    if (sl >= o) incl += t;
+  }
+  double acc = incl - run;                 // exclusive offset of this chunk
+  for (int j = j0; j < j1; ++j) {
+    const int n = idx(j);
+    acc += get(n);
+    put(n, acc);
   }
 }
+
+// exact left inverse of the Dirichlet stencil: x_n = x_{n-2} - c_n, i.e.
+// x_n = -(sum of c_i over i <= n, i = n mod 2), n < G.  Needs 2*TM warps.
+__device__ __forceinline__ void tpinv_dir(double2* x, const double2* c, int G) {
+  const int w = threadIdx.x >> 5;
+  if (w < 2 * TM) {
+    const int mm = w >> 1;
+    const bool im = w & 1;
+    warp_parity_scan(G, false,
+        [&](int n) { return im ? -c[n * TM + mm].y : -c[n * TM + mm].x; },
+        [&](int n, double v) { if (im) x[n * TM + mm].y = v; else x[n * TM + mm].x = v; });
+  }
+}
+
 // exact left inverse of the open-top stencil: x_n = c_n - a_{n-1} x_{n-1} - b_{n-2} x_{n-2}
 __device__ __forceinline__ void tpinv_mixed(double2* x, const double2* c, int G,
                                             const double* __restrict__ wa,
@@ -133,79 +162,103 @@ __device__ __forceinline__ void tpinv_mixed(double2* x, const double2* c, int G,
     }
   }
 }
-// d/dZ on Chebyshev coefficients, G_Z = 2 G_xi: b_{N-1} = 4N a_N,
-// b_k = b_{k+2} + 4(k+1) a_{k+1}, b_0 = b_2/2 + 2 a_1 (nhqg/grid.py:148-169)
+// d/dZ on Chebyshev coefficients, G_Z = 2 G_xi (nhqg/grid.py:148-169):
+// b_k = sum_{j > k, j - k odd} 4 j a_j for 1 <= k <= N-1, b_N = 0,
+// b_0 = b_2 / 2 + 2 a_1 -- suffix sums over a parity class.  Needs 2*TM warps.
 __device__ __forceinline__ void tgz(double2* b, const double2* a, int N) {
-  const int t = threadIdx.x;
-  if (t < 2 * TM) {
-    const int mm = t >> 1;
-    const bool im = t & 1;
-    auto A = [&](int n) { return im ? a[n * TM + mm].y : a[n * TM + mm].x; };
-    auto S = [&](int n, double v) { if (im) b[n * TM + mm].y = v; else b[n * TM + mm].x = v; };
-    S(N, 0.0);
-    double bk2 = 0.0;
-    double bk1 = 4.0 * N * A(N);
-    S(N - 1, bk1);
-    for (int kk = N - 2; kk >= 1; --kk) {
-      const double bk = fma(4.0 * (kk + 1), A(kk + 1), bk2);
-      S(kk, bk);
-      bk2 = bk1;
-      bk1 = bk;
+  const int w = threadIdx.x >> 5;
+  if (w < 2 * TM) {
+    const int mm = w >> 1;
+    const bool im = w & 1;
+    // t_j = 4 j a_j for j = 1..N, scanned from the top: U_j = sum_{i>=j, i=j mod 2} t_i
+    // stored as b_{j-1} = U_j (j = 2..N), b_0 fixed up below
+    warp_parity_scan(N, true,
+        [&](int n) {  // n = j - 1 in [0, N-1]
+          const double av = im ? a[(n + 1) * TM + mm].y : a[(n + 1) * TM + mm].x;
+          return (4.0 * (n + 1)) * av;
+        },
+        [&](int n, double v) { if (n >= 1) { if (im) b[n * TM + mm].y = v; else b[n * TM + mm].x = v; } });
+    if ((threadIdx.x & 31) == 0) {
+      if (im) b[N * TM + mm].y = 0.0; else b[N * TM + mm].x = 0.0;
     }
-    S(0, fma(0.5, bk2, 2.0 * A(1)));
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * TM) {
+    const int mm = threadIdx.x >> 1;
+    const bool im = threadIdx.x & 1;
+    const double b2 = N >= 2 ? (im ? b[2 * TM + mm].y : b[2 * TM + mm].x) : 0.0;
+    const double a1 = im ? a[TM + mm].y : a[TM + mm].x;
+    const double b0 = fma(0.5, b2, 2.0 * a1);
+    if (im) b[mm].y = b0; else b[mm].x = b0;
   }
 }
 
 // Load the DCT twiddle / permutation tables into shared memory.
-struct DctShared {
-  double2* work;
-  double2* tw;
+template <typename C>
+struct DctSharedT {
+  C* work;
+  C* tw;
   int* perm;
 };
-__device__ __forceinline__ DctShared dct_shared(const Dct& d, double2* base) {
-  DctShared s;
-  s.work = base;
-  s.tw = base + TM * 2 * d.N;
+using DctShared = DctSharedT<double2>;
+
+template <typename C>
+__device__ __forceinline__ const C* dct_tw(const Dct& d);
+template <> __device__ __forceinline__ const double2* dct_tw<double2>(const Dct& d) { return d.tw; }
+template <> __device__ __forceinline__ const float2* dct_tw<float2>(const Dct& d) { return d.tw_f; }
+
+template <typename C = double2>
+__device__ __forceinline__ DctSharedT<C> dct_shared(const Dct& d, void* base) {
+  DctSharedT<C> s;
+  s.work = reinterpret_cast<C*>(base);
+  s.tw = s.work + TM * 2 * d.N;
   s.perm = reinterpret_cast<int*>(s.tw + 2 * d.N);
   if (d.fast) {
+    const C* tw = dct_tw<C>(d);
     for (int i = threadIdx.x; i < 2 * d.N; i += blockDim.x) {
-      s.tw[i] = d.tw[i];
+      s.tw[i] = tw[i];
       s.perm[i] = d.perm[i];
     }
   }
   return s;
 }
 
-// out[0:nout] = V in (inverse == false) or V^-1 in (inverse == true), per column.
-// Caller syncs before (in ready) and after (out ready).  out != in.
-__device__ __forceinline__ void tdct(double2* out, const double2* in, const Dct& d,
-                                     const DctShared& s, bool inverse, int nout) {
+// out[0:nout] = V in (inverse == false) or V^-1 in (inverse == true), per column,
+// in the precision of C.  Caller syncs before (in ready) and after (out
+// ready).  out != in.  The FP32 instantiation requires d.fast.
+template <typename C>
+__device__ __forceinline__ void tdct(C* out, const C* in, const Dct& d, const DctSharedT<C>& s,
+                                     bool inverse, int nout) {
+  using T = decltype(C().x);
   const int N = d.N;
-  if (!d.fast) {
-    tmat(out, in, inverse ? d.Vinv : d.V, d.P, nout, d.P);
-    return;
+  if constexpr (sizeof(T) == 8) {
+    if (!d.fast) {
+      tmat(out, in, inverse ? d.Vinv : d.V, d.P, nout, d.P);
+      return;
+    }
   }
   const int L = 2 * N;
+  const T half = T(0.5);
   for (int idx = threadIdx.x; idx < TM * L; idx += blockDim.x) {
     const int mm = idx / L, n = idx - mm * L;
     const int src = n <= N ? n : L - n;
-    double2 v = in[src * TM + mm];
-    if (inverse && (src == 0 || src == N)) v = cscale(v, 0.5);
+    C v = in[src * TM + mm];
+    if (inverse && (src == 0 || src == N)) v = gscale(v, half);
     s.work[idx] = v;
   }
   __syncthreads();
   fft_dif_fwd(s.work, TM, L, d.plan, s.tw);
-  const double sc = inverse ? (1.0 / N) : 0.5;  // (2/N)/2 after the 1/2 of the DCT-I identity
+  const T sc = inverse ? T(1.0 / N) : half;  // (2/N)/2 after the 1/2 of the DCT-I identity
   for (int idx = threadIdx.x; idx < nout * TM; idx += blockDim.x) {
     const int j = idx / TM, mm = idx - j * TM;
-    const double2 Y = s.work[mm * L + s.perm[j]];
-    double2 c0 = in[mm], cN = in[N * TM + mm];
-    if (inverse) { c0 = cscale(c0, 0.5); cN = cscale(cN, 0.5); }
-    double2 y = cadd(Y, c0);
-    y = (j & 1) ? csub(y, cN) : cadd(y, cN);
-    double f = sc;
-    if (inverse && (j == 0 || j == N)) f *= 0.5;
-    out[idx] = cscale(y, f);
+    const C Y = s.work[mm * L + s.perm[j]];
+    C c0 = in[mm], cN = in[N * TM + mm];
+    if (inverse) { c0 = gscale(c0, half); cN = gscale(cN, half); }
+    C y = gadd(Y, c0);
+    y = (j & 1) ? gsub(y, cN) : gadd(y, cN);
+    T f = sc;
+    if (inverse && (j == 0 || j == N)) f *= half;
+    out[idx] = gscale(y, f);
   }
 }
 

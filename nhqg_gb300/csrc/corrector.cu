@@ -141,12 +141,16 @@ __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const doub
   tcsr(b2, b0, k.s2c_ptr, k.s2c_col, k.s2c_val, P);  // y = s2c theta_sbp_new
   __syncthreads();
   if (!last || tcgl != nullptr) {
-    if (threadIdx.x < 4 * TM) {  // delta_j = F_j . y  (j = 0, 1; re/im)
-      const int mm = threadIdx.x % TM, j = (threadIdx.x / TM) & 1, im = threadIdx.x / (2 * TM);
-      const double* F = k.bcF + j * P;
-      double acc = 0.0;
-      for (int l = 0; l < P; ++l) acc = fma(F[l], im ? b2[l * TM + mm].y : b2[l * TM + mm].x, acc);
-      if (im) delta[j * TM + mm].y = acc; else delta[j * TM + mm].x = acc;
+    {  // delta_j = F_j . y for j = 0, 1, re/im: 4*TM dot products, one warp each pass
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int d = warp; d < 4 * TM; d += blockDim.x >> 5) {
+        const int mm = d % TM, j = (d / TM) & 1, im = d / (2 * TM);
+        const double* F = k.bcF + j * P;
+        double acc = 0.0;
+        for (int l = lane; l < P; l += 32) acc = fma(F[l], im ? b2[l * TM + mm].y : b2[l * TM + mm].x, acc);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) { if (im) delta[j * TM + mm].y = acc; else delta[j * TM + mm].x = acc; }
+      }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) {
@@ -237,12 +241,14 @@ __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt)
     B[idx] = b;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {  // banded LU without pivoting, in place (multipliers below the diagonal)
+  if (threadIdx.x == 0) {  // banded LU without pivoting, in place (multipliers below the diagonal);
+                           // the diagonal slot keeps 1/pivot for the substitutions
     for (int col = 0; col < P; ++col) {
-      const double piv = A[2 * P + col];
+      const double rp = 1.0 / A[2 * P + col];
+      A[2 * P + col] = rp;
       for (int r = col + 1; r <= min(P - 1, col + 2); ++r) {
         const int dr = col - r + 2;  // band slot of A[r, col]
-        const double l = A[dr * P + r] / piv;
+        const double l = A[dr * P + r] * rp;
         A[dr * P + r] = l;
         for (int c = col + 1; c <= min(P - 1, col + 2); ++c) {
           const int drc = c - r + 2;
@@ -286,7 +292,7 @@ __global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, double*
     for (int i = P - 1; i >= 0; --i) {
       double v = rhs[i];
       for (int c = i + 1; c <= min(P - 1, i + 2); ++c) v = fma(-A[(c - i + 2) * P + i], rhs[c], v);
-      rhs[i] = v / A[2 * P + i];
+      rhs[i] = v * A[2 * P + i];
     }
   }
   __syncthreads();  // rhs = tb_new

@@ -27,6 +27,9 @@ struct Tables {
   // FFT over Nx
   double2* tw = nullptr;  // [Nx]
   int* perm = nullptr;    // [Nx]
+  // FP32 copies for the mixed-precision path
+  float *kx_f = nullptr, *ky_f = nullptr, *sponge_f = nullptr, *eta_phys_f = nullptr;
+  float2 *eta_f = nullptr, *tw_f = nullptr, *tw_v_f = nullptr;
   // FFT over 2*Nz (DCT-I of the vertical columns)
   double2* tw_v = nullptr;  // [2Nz]
   int* perm_v = nullptr;    // [2Nz]
@@ -125,6 +128,27 @@ struct Profiler {
   }
 };
 
+// Horizontal-kernel tables in the compute precision (T = real of C).
+template <typename C>
+struct HTables {
+  using T = decltype(C().x);
+  const T *kx_full, *ky_full;  // [Nx], [Nk]
+  const double* inv_denom;     // compact [M] (psi derivation)
+  const C* eta;                // compact [M] or null
+  const T *sponge, *eta_phys;  // [Nx*Nx] or null
+  const C* tw;                 // [Nx]
+  const int* perm;             // [Nx]
+};
+
+template <typename C, typename CI>
+struct HorizArgsT {
+  int form;
+  bool sponge, eta, full_in, full_out, psi_derived;
+  int levels;
+  const CI *psi, *q, *w, *th;
+  C *Aq, *Aw, *Ath;
+};
+
 struct Work {
   Profiler prof;
   // H1 / H2 intermediates
@@ -141,6 +165,12 @@ struct Work {
 // ---- launchers (return cudaError_t of the last launch) ----
 cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const HorizArgs& a,
                               cudaStream_t st, int* nlaunch);
+
+cudaError_t launch_horizontal_f32(const Params& p, const Tables& t, Work& w,
+                                  const HorizArgsT<float2, float2>& a, cudaStream_t st, int* nlaunch);
+cudaError_t launch_horizontal_f32_from64(const Params& p, const Tables& t, Work& w,
+                                         const HorizArgsT<float2, double2>& a, cudaStream_t st,
+                                         int* nlaunch);
 
 // vertical / column engine
 enum VBackMode { VB_RHS = 0, VB_STAGE1 = 1, VB_STAGE2 = 2, VB_SOLVE = 3 };

@@ -48,9 +48,29 @@ inline void make_fft_perm(const FftPlan& p, int* perm) {
 
 constexpr double kSqrt3Half = 0.86602540378443864676;
 
+// complex type per real type
+template <typename T> struct CT;
+template <> struct CT<double> { using type = double2; };
+template <> struct CT<float> { using type = float2; };
+template <typename T> using cplx_t = typename CT<T>::type;
+
+template <typename C> __device__ __forceinline__ C gadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C gsub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C, typename T> __device__ __forceinline__ C gscale(C a, T s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+template <typename C> __device__ __forceinline__ C gmk(decltype(C().x) x, decltype(C().x) y) { C r; r.x = x; r.y = y; return r; }
+// a * b and a * conj(b)
+template <typename C> __device__ __forceinline__ C gmul(C a, C b) {
+  return gmk<C>(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+template <typename C> __device__ __forceinline__ C gmulc(C a, C b) {
+  return gmk<C>(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -a.x * b.y));
+}
+
 // Forward DFT (sign -1), natural -> reversed.  tw[k] = exp(-2 pi i k / n).
-__device__ __forceinline__ void fft_dif_fwd(double2* __restrict__ data, int nseq, int stride,
-                                            const FftPlan& pl, const double2* __restrict__ tw) {
+template <typename C>
+__device__ __forceinline__ void fft_dif_fwd(C* __restrict__ data, int nseq, int stride,
+                                            const FftPlan& pl, const C* __restrict__ tw) {
+  using T = decltype(C().x);
   int L = pl.n;
   for (int q = 0; q < pl.npass; ++q) {
     const int R = pl.radix[q];
@@ -60,39 +80,39 @@ __device__ __forceinline__ void fft_dif_fwd(double2* __restrict__ data, int nseq
     for (int idx = threadIdx.x; idx < nseq * nb; idx += blockDim.x) {
       const int s = idx / nb, b = idx - s * nb;
       const int blk = b / Ls, j = b - blk * Ls;
-      double2* a = data + s * stride + blk * L + j;
+      C* a = data + s * stride + blk * L + j;
       if (R == 4) {
-        const double2 x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
-        const double2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = csub(x1, x3);
-        double2 y1 = make_double2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
-        double2 y2 = csub(t0, t2);
-        double2 y3 = make_double2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
-        a[0] = cadd(t0, t2);
+        const C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
+        const C t0 = gadd(x0, x2), t1 = gsub(x0, x2), t2 = gadd(x1, x3), t3 = gsub(x1, x3);
+        C y1 = gmk<C>(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+        C y2 = gsub(t0, t2);
+        C y3 = gmk<C>(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
+        a[0] = gadd(t0, t2);
         if (j != 0) {
-          y1 = cmul(y1, tw[j * tws]);
-          y2 = cmul(y2, tw[2 * j * tws]);
-          y3 = cmul(y3, tw[3 * j * tws]);
+          y1 = gmul(y1, tw[j * tws]);
+          y2 = gmul(y2, tw[2 * j * tws]);
+          y3 = gmul(y3, tw[3 * j * tws]);
         }
         a[Ls] = y1;
         a[2 * Ls] = y2;
         a[3 * Ls] = y3;
       } else if (R == 2) {
-        const double2 x0 = a[0], x1 = a[Ls];
-        double2 y1 = csub(x0, x1);
-        a[0] = cadd(x0, x1);
-        if (j != 0) y1 = cmul(y1, tw[j * tws]);
+        const C x0 = a[0], x1 = a[Ls];
+        C y1 = gsub(x0, x1);
+        a[0] = gadd(x0, x1);
+        if (j != 0) y1 = gmul(y1, tw[j * tws]);
         a[Ls] = y1;
       } else {  // R == 3
-        const double2 x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls];
-        const double2 sp = cadd(x1, x2);
-        const double2 d = cscale(csub(x1, x2), kSqrt3Half);
-        const double2 m = caxpy(-0.5, sp, x0);
-        double2 y1 = make_double2(m.x + d.y, m.y - d.x);  // m - i d
-        double2 y2 = make_double2(m.x - d.y, m.y + d.x);  // m + i d
-        a[0] = cadd(x0, sp);
+        const C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls];
+        const C sp = gadd(x1, x2);
+        const C d = gscale(gsub(x1, x2), (T)kSqrt3Half);
+        const C m = gmk<C>(fma((T)-0.5, sp.x, x0.x), fma((T)-0.5, sp.y, x0.y));
+        C y1 = gmk<C>(m.x + d.y, m.y - d.x);  // m - i d
+        C y2 = gmk<C>(m.x - d.y, m.y + d.x);  // m + i d
+        a[0] = gadd(x0, sp);
         if (j != 0) {
-          y1 = cmul(y1, tw[j * tws]);
-          y2 = cmul(y2, tw[2 * j * tws]);
+          y1 = gmul(y1, tw[j * tws]);
+          y2 = gmul(y2, tw[2 * j * tws]);
         }
         a[Ls] = y1;
         a[2 * Ls] = y2;
@@ -104,8 +124,10 @@ __device__ __forceinline__ void fft_dif_fwd(double2* __restrict__ data, int nseq
 }
 
 // Inverse DFT (sign +1, unscaled), reversed -> natural.
-__device__ __forceinline__ void fft_dit_inv(double2* __restrict__ data, int nseq, int stride,
-                                            const FftPlan& pl, const double2* __restrict__ tw) {
+template <typename C>
+__device__ __forceinline__ void fft_dit_inv(C* __restrict__ data, int nseq, int stride,
+                                            const FftPlan& pl, const C* __restrict__ tw) {
+  using T = decltype(C().x);
   int Ls_of[12];
   {
     int L = pl.n;
@@ -120,36 +142,36 @@ __device__ __forceinline__ void fft_dit_inv(double2* __restrict__ data, int nseq
     for (int idx = threadIdx.x; idx < nseq * nb; idx += blockDim.x) {
       const int s = idx / nb, b = idx - s * nb;
       const int blk = b / Ls, j = b - blk * Ls;
-      double2* a = data + s * stride + blk * L + j;
+      C* a = data + s * stride + blk * L + j;
       if (R == 4) {
-        double2 x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
+        C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
         if (j != 0) {
-          x1 = cmulc(x1, tw[j * tws]);
-          x2 = cmulc(x2, tw[2 * j * tws]);
-          x3 = cmulc(x3, tw[3 * j * tws]);
+          x1 = gmulc(x1, tw[j * tws]);
+          x2 = gmulc(x2, tw[2 * j * tws]);
+          x3 = gmulc(x3, tw[3 * j * tws]);
         }
-        const double2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = csub(x1, x3);
-        a[0] = cadd(t0, t2);
-        a[Ls] = make_double2(t1.x - t3.y, t1.y + t3.x);      // t1 + i t3
-        a[2 * Ls] = csub(t0, t2);
-        a[3 * Ls] = make_double2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+        const C t0 = gadd(x0, x2), t1 = gsub(x0, x2), t2 = gadd(x1, x3), t3 = gsub(x1, x3);
+        a[0] = gadd(t0, t2);
+        a[Ls] = gmk<C>(t1.x - t3.y, t1.y + t3.x);      // t1 + i t3
+        a[2 * Ls] = gsub(t0, t2);
+        a[3 * Ls] = gmk<C>(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
       } else if (R == 2) {
-        double2 x0 = a[0], x1 = a[Ls];
-        if (j != 0) x1 = cmulc(x1, tw[j * tws]);
-        a[0] = cadd(x0, x1);
-        a[Ls] = csub(x0, x1);
+        C x0 = a[0], x1 = a[Ls];
+        if (j != 0) x1 = gmulc(x1, tw[j * tws]);
+        a[0] = gadd(x0, x1);
+        a[Ls] = gsub(x0, x1);
       } else {
-        double2 x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls];
+        C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls];
         if (j != 0) {
-          x1 = cmulc(x1, tw[j * tws]);
-          x2 = cmulc(x2, tw[2 * j * tws]);
+          x1 = gmulc(x1, tw[j * tws]);
+          x2 = gmulc(x2, tw[2 * j * tws]);
         }
-        const double2 sp = cadd(x1, x2);
-        const double2 d = cscale(csub(x1, x2), kSqrt3Half);
-        const double2 m = caxpy(-0.5, sp, x0);
-        a[0] = cadd(x0, sp);
-        a[Ls] = make_double2(m.x - d.y, m.y + d.x);      // m + i d
-        a[2 * Ls] = make_double2(m.x + d.y, m.y - d.x);  // m - i d
+        const C sp = gadd(x1, x2);
+        const C d = gscale(gsub(x1, x2), (T)kSqrt3Half);
+        const C m = gmk<C>(fma((T)-0.5, sp.x, x0.x), fma((T)-0.5, sp.y, x0.y));
+        a[0] = gadd(x0, sp);
+        a[Ls] = gmk<C>(m.x - d.y, m.y + d.x);      // m + i d
+        a[2 * Ls] = gmk<C>(m.x + d.y, m.y - d.x);  // m - i d
       }
     }
     __syncthreads();

@@ -23,7 +23,9 @@ namespace nhqg {
 
 namespace {
 
+template <typename C, typename CI>
 struct HK {
+  using T = decltype(C().x);
   // geometry
   int Nx, Nk, K, Mr, Mc, M;
   int levels;
@@ -31,23 +33,29 @@ struct HK {
   bool full_in, full_out;
   int form, nf1, nprod, ng;
   bool sponge, eta, psi_derived;
-  double scale;  // 1/Nx^2
+  T scale;  // 1/Nx^2
   FftPlan plan;
-  const double2 *psi, *q, *w, *th;
-  const double *kx_full, *ky_full, *inv_denom;  // inv_denom compact [M]
-  const double2* eta_c;                          // compact eta [M]
-  const double *sponge_phys, *eta_phys;
-  const double2* tw;
+  const CI *psi, *q, *w, *th;
+  const T *kx_full, *ky_full;
+  const double* inv_denom;  // compact [M]
+  const C* eta_c;           // compact eta [M]
+  const T *sponge_phys, *eta_phys;
+  const C* tw;
   const int* perm;
-  double2 *x1, *x2;
-  double2 *Aq, *Aw, *Ath;
+  C *x1, *x2;
+  C *Aq, *Aw, *Ath;
 };
 
-__device__ __forceinline__ int plane_index(const HK& k, int r, int c) {
+template <typename C, typename CI>
+__device__ __forceinline__ C to_c(CI v) { C r; r.x = v.x; r.y = v.y; return r; }
+
+template <typename K>
+__device__ __forceinline__ int plane_index(const K& k, int r, int c) {
   return r * k.cols_in + c;
 }
 
-__device__ __forceinline__ void load_tables(const HK& k, double2* tw_s, int* perm_s) {
+template <typename K, typename C>
+__device__ __forceinline__ void load_tables(const K& k, C* tw_s, int* perm_s) {
   for (int i = threadIdx.x; i < k.Nx; i += blockDim.x) {
     tw_s[i] = k.tw[i];
     perm_s[i] = k.perm[i];
@@ -55,17 +63,19 @@ __device__ __forceinline__ void load_tables(const HK& k, double2* tw_s, int* per
 }
 
 // ---------------------------------------------------------------- H1
-__global__ void __launch_bounds__(256) k_h1(HK k, int CB) {
-  extern __shared__ double2 smem[];
-  double2* tw_s = smem;
+template <typename C, typename CI>
+__global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
+  using T = decltype(C().x);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw_s = reinterpret_cast<C*>(smem_raw);
   int* perm_s = reinterpret_cast<int*>(tw_s + k.Nx);
-  double2* seq = tw_s + k.Nx + (k.Nx + 1) / 2;  // after perm (ints packed 2 per double2)
+  C* seq = reinterpret_cast<C*>(perm_s + ((k.Nx + 3) / 4) * 4);
   const int lev = blockIdx.y;
   const int c0 = blockIdx.x * CB;
   const int ncb = min(CB, k.cols_in - c0);
   const int nseq = k.nf1 * CB;
   load_tables(k, tw_s, perm_s);
-  for (int i = threadIdx.x; i < nseq * k.Nx; i += blockDim.x) seq[i] = czero();
+  for (int i = threadIdx.x; i < nseq * k.Nx; i += blockDim.x) seq[i] = gmk<C>(T(0), T(0));
   __syncthreads();
 
   const size_t plane = (size_t)k.rows_in * k.cols_in;
@@ -73,45 +83,45 @@ __global__ void __launch_bounds__(256) k_h1(HK k, int CB) {
     const int r = i / ncb, cc = i - r * ncb, c = c0 + cc;
     const int kf = k.full_in ? r : full_row(r, k.K, k.Nx);
     const size_t off = (size_t)lev * plane + plane_index(k, r, c);
-    const double kxs = k.kx_full[kf] * k.scale;
-    const double kys = k.ky_full[c] * k.scale;
+    const T kxs = k.kx_full[kf] * k.scale;
+    const T kys = k.ky_full[c] * k.scale;
     const int pos = perm_s[kf];
-    double2* s0 = seq + (size_t)cc * k.Nx + pos;
+    C* s0 = seq + (size_t)cc * k.Nx + pos;
     const size_t fs = (size_t)CB * k.Nx;  // stride between fields
     if (k.form == HF_SPONGE) {
-      s0[0] = cscale(k.q[off], k.scale);
+      s0[0] = gscale(to_c<C>(k.q[off]), k.scale);
       continue;
     }
-    double2 qv = k.q[off];
-    double2 psi;
+    C qv = to_c<C>(k.q[off]);
+    C psi;
     if (k.psi_derived) {
       const int m = r * k.Mc + c;  // compact only
-      psi = cscale(qv, -k.inv_denom[m]);
+      psi = gscale(qv, (T)(-k.inv_denom[m]));
     } else {
-      psi = k.psi[off];
+      psi = to_c<C>(k.psi[off]);
     }
-    if (k.eta) qv = cadd(qv, k.eta_c[r * k.Mc + c]);
-    const double2 wv = k.w[off], tv = k.th[off];
+    if (k.eta) qv = gadd(qv, k.eta_c[r * k.Mc + c]);
+    const C wv = to_c<C>(k.w[off]), tv = to_c<C>(k.th[off]);
     if (k.form == HF_FLUX) {
       // u = -i ky psi, v = i kx psi
-      s0[0] = make_double2(kys * psi.y, -kys * psi.x);
-      s0[fs] = make_double2(-kxs * psi.y, kxs * psi.x);
-      s0[2 * fs] = cscale(qv, k.scale);
-      s0[3 * fs] = cscale(wv, k.scale);
-      s0[4 * fs] = cscale(tv, k.scale);
+      s0[0] = gmk<C>(kys * psi.y, -kys * psi.x);
+      s0[fs] = gmk<C>(-kxs * psi.y, kxs * psi.x);
+      s0[2 * fs] = gscale(qv, k.scale);
+      s0[3 * fs] = gscale(wv, k.scale);
+      s0[4 * fs] = gscale(tv, k.scale);
     } else {  // Jacobian: psi_x, psi_y, q_x, q_y, w_x, w_y, t_x, t_y [, q, w, t]
-      s0[0] = make_double2(-kxs * psi.y, kxs * psi.x);
-      s0[fs] = make_double2(-kys * psi.y, kys * psi.x);
-      s0[2 * fs] = make_double2(-kxs * qv.y, kxs * qv.x);
-      s0[3 * fs] = make_double2(-kys * qv.y, kys * qv.x);
-      s0[4 * fs] = make_double2(-kxs * wv.y, kxs * wv.x);
-      s0[5 * fs] = make_double2(-kys * wv.y, kys * wv.x);
-      s0[6 * fs] = make_double2(-kxs * tv.y, kxs * tv.x);
-      s0[7 * fs] = make_double2(-kys * tv.y, kys * tv.x);
+      s0[0] = gmk<C>(-kxs * psi.y, kxs * psi.x);
+      s0[fs] = gmk<C>(-kys * psi.y, kys * psi.x);
+      s0[2 * fs] = gmk<C>(-kxs * qv.y, kxs * qv.x);
+      s0[3 * fs] = gmk<C>(-kys * qv.y, kys * qv.x);
+      s0[4 * fs] = gmk<C>(-kxs * wv.y, kxs * wv.x);
+      s0[5 * fs] = gmk<C>(-kys * wv.y, kys * wv.x);
+      s0[6 * fs] = gmk<C>(-kxs * tv.y, kxs * tv.x);
+      s0[7 * fs] = gmk<C>(-kys * tv.y, kys * tv.x);
       if (k.sponge) {
-        s0[8 * fs] = cscale(qv, k.scale);
-        s0[9 * fs] = cscale(wv, k.scale);
-        s0[10 * fs] = cscale(tv, k.scale);
+        s0[8 * fs] = gscale(qv, k.scale);
+        s0[9 * fs] = gscale(wv, k.scale);
+        s0[10 * fs] = gscale(tv, k.scale);
       }
     }
   }
@@ -127,17 +137,19 @@ __global__ void __launch_bounds__(256) k_h1(HK k, int CB) {
 }
 
 // ---------------------------------------------------------------- H2
-__global__ void __launch_bounds__(256) k_h2(HK k, int RB) {
-  extern __shared__ double2 smem[];
-  double2* tw_s = smem;
+template <typename C, typename CI>
+__global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
+  using T = decltype(C().x);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw_s = reinterpret_cast<C*>(smem_raw);
   int* perm_s = reinterpret_cast<int*>(tw_s + k.Nx);
-  double2* in = tw_s + k.Nx + (k.Nx + 1) / 2;
+  C* in = reinterpret_cast<C*>(perm_s + ((k.Nx + 3) / 4) * 4);
   const int NPR = RB / 2;
-  double2* pr = in + (size_t)k.nf1 * NPR * k.Nx;
+  C* pr = in + (size_t)k.nf1 * NPR * k.Nx;
   const int lev = blockIdx.y;
   const int x0 = blockIdx.x * RB;
   load_tables(k, tw_s, perm_s);
-  for (int i = threadIdx.x; i < k.nf1 * NPR * k.Nx; i += blockDim.x) in[i] = czero();
+  for (int i = threadIdx.x; i < k.nf1 * NPR * k.Nx; i += blockDim.x) in[i] = gmk<C>(T(0), T(0));
   __syncthreads();
   const int half = k.Nx / 2;
   // Hermitian-extended spectra of row pairs (a, b): Z = Xa + i Xb
@@ -147,13 +159,13 @@ __global__ void __launch_bounds__(256) k_h2(HK k, int RB) {
     const int p = rest % NPR, f = rest / NPR;
     const int xa = x0 + 2 * p;
     const size_t base = (((size_t)f * k.levels + lev) * k.cols_in + c) * k.Nx;
-    const double2 A = k.x1[base + xa], B = k.x1[base + xa + 1];
-    double2* s = in + ((size_t)f * NPR + p) * k.Nx;
+    const C A = k.x1[base + xa], B = k.x1[base + xa + 1];
+    C* s = in + ((size_t)f * NPR + p) * k.Nx;
     if (c == 0 || c == half) {
-      s[perm_s[c]] = make_double2(A.x, B.x);
+      s[perm_s[c]] = gmk<C>(A.x, B.x);
     } else {
-      s[perm_s[c]] = make_double2(A.x - B.y, A.y + B.x);
-      s[perm_s[k.Nx - c]] = make_double2(A.x + B.y, B.x - A.y);
+      s[perm_s[c]] = gmk<C>(A.x - B.y, A.y + B.x);
+      s[perm_s[k.Nx - c]] = gmk<C>(A.x + B.y, B.x - A.y);
     }
   }
   __syncthreads();
@@ -163,9 +175,9 @@ __global__ void __launch_bounds__(256) k_h2(HK k, int RB) {
   for (int i = threadIdx.x; i < NPR * k.Nx; i += blockDim.x) {
     const int y = i % k.Nx, p = i / k.Nx;
     const int xa = x0 + 2 * p;
-    const double2* s = in + (size_t)p * k.Nx + y;
-    double2* o = pr + (size_t)p * k.Nx + y;
-    double sa = 0.0, sb = 0.0, ea = 0.0, eb = 0.0;
+    const C* s = in + (size_t)p * k.Nx + y;
+    C* o = pr + (size_t)p * k.Nx + y;
+    T sa = 0, sb = 0, ea = 0, eb = 0;
     if (k.sponge) {
       sa = k.sponge_phys[(size_t)xa * k.Nx + y];
       sb = k.sponge_phys[(size_t)(xa + 1) * k.Nx + y];
@@ -175,36 +187,36 @@ __global__ void __launch_bounds__(256) k_h2(HK k, int RB) {
       }
     }
     if (k.form == HF_FLUX) {
-      const double2 u = s[0], v = s[fs], Q = s[2 * fs], W = s[3 * fs], T = s[4 * fs];
-      o[0] = make_double2(u.x * Q.x, u.y * Q.y);
-      o[fs] = make_double2(v.x * Q.x, v.y * Q.y);
-      o[2 * fs] = make_double2(u.x * W.x, u.y * W.y);
-      o[3 * fs] = make_double2(v.x * W.x, v.y * W.y);
-      o[4 * fs] = make_double2(u.x * T.x, u.y * T.y);
-      o[5 * fs] = make_double2(v.x * T.x, v.y * T.y);
+      const C u = s[0], v = s[fs], Q = s[2 * fs], W = s[3 * fs], Th = s[4 * fs];
+      o[0] = gmk<C>(u.x * Q.x, u.y * Q.y);
+      o[fs] = gmk<C>(v.x * Q.x, v.y * Q.y);
+      o[2 * fs] = gmk<C>(u.x * W.x, u.y * W.y);
+      o[3 * fs] = gmk<C>(v.x * W.x, v.y * W.y);
+      o[4 * fs] = gmk<C>(u.x * Th.x, u.y * Th.y);
+      o[5 * fs] = gmk<C>(v.x * Th.x, v.y * Th.y);
       if (k.sponge) {
-        o[6 * fs] = make_double2(sa * (Q.x - ea), sb * (Q.y - eb));
-        o[7 * fs] = make_double2(sa * W.x, sb * W.y);
-        o[8 * fs] = make_double2(sa * T.x, sb * T.y);
+        o[6 * fs] = gmk<C>(sa * (Q.x - ea), sb * (Q.y - eb));
+        o[7 * fs] = gmk<C>(sa * W.x, sb * W.y);
+        o[8 * fs] = gmk<C>(sa * Th.x, sb * Th.y);
       }
     } else if (k.form == HF_JAC) {
-      const double2 px = s[0], py = s[fs];
+      const C px = s[0], py = s[fs];
       for (int f = 0; f < 3; ++f) {
-        const double2 fx = s[(2 + 2 * f) * fs], fy = s[(3 + 2 * f) * fs];
-        double ja = fma(px.x, fy.x, -py.x * fx.x);
-        double jb = fma(px.y, fy.y, -py.y * fx.y);
+        const C fx = s[(2 + 2 * f) * fs], fy = s[(3 + 2 * f) * fs];
+        T ja = fma(px.x, fy.x, -py.x * fx.x);
+        T jb = fma(px.y, fy.y, -py.y * fx.y);
         if (k.sponge) {
-          const double2 F = s[(8 + f) * fs];
-          const double Fa = (f == 0) ? F.x - ea : F.x;
-          const double Fb = (f == 0) ? F.y - eb : F.y;
+          const C F = s[(8 + f) * fs];
+          const T Fa = (f == 0) ? F.x - ea : F.x;
+          const T Fb = (f == 0) ? F.y - eb : F.y;
           ja = fma(sa, Fa, ja);
           jb = fma(sb, Fb, jb);
         }
-        o[f * fs] = make_double2(ja, jb);
+        o[f * fs] = gmk<C>(ja, jb);
       }
     } else {  // sponge-only product
-      const double2 F = s[0];
-      o[0] = make_double2(sa * F.x, sb * F.y);
+      const C F = s[0];
+      o[0] = gmk<C>(sa * F.x, sb * F.y);
     }
   }
   __syncthreads();
@@ -216,28 +228,28 @@ __global__ void __launch_bounds__(256) k_h2(HK k, int RB) {
     const int p = rest % NPR, g = rest / NPR;
     const int xa = x0 + 2 * p;
     const int pa = perm_s[c], pb = perm_s[c == 0 ? 0 : k.Nx - c];
-    auto split = [&](int prod, double2& Xa, double2& Xb) {
-      const double2* s = pr + ((size_t)prod * NPR + p) * k.Nx;
-      const double2 A = s[pa], B = s[pb];
-      Xa = make_double2(0.5 * (A.x + B.x), 0.5 * (A.y - B.y));
-      Xb = make_double2(0.5 * (A.y + B.y), 0.5 * (B.x - A.x));
+    auto split = [&](int prod, C& Xa, C& Xb) {
+      const C* s = pr + ((size_t)prod * NPR + p) * k.Nx;
+      const C A = s[pa], B = s[pb];
+      Xa = gmk<C>(T(0.5) * (A.x + B.x), T(0.5) * (A.y - B.y));
+      Xb = gmk<C>(T(0.5) * (A.y + B.y), T(0.5) * (B.x - A.x));
     };
-    double2 Ra, Rb;
+    C Ra, Rb;
     if (k.form == HF_FLUX) {
       const int f = g >> 1;
       if ((g & 1) == 0) {
         split(2 * f, Ra, Rb);
       } else {
-        double2 Va, Vb;
+        C Va, Vb;
         split(2 * f + 1, Va, Vb);
-        const double ky = k.ky_full[c];
-        Ra = make_double2(-ky * Va.y, ky * Va.x);
-        Rb = make_double2(-ky * Vb.y, ky * Vb.x);
+        const T ky = k.ky_full[c];
+        Ra = gmk<C>(-ky * Va.y, ky * Va.x);
+        Rb = gmk<C>(-ky * Vb.y, ky * Vb.x);
         if (k.sponge) {
-          double2 Sa, Sb;
+          C Sa, Sb;
           split(6 + f, Sa, Sb);
-          Ra = cadd(Ra, Sa);
-          Rb = cadd(Rb, Sb);
+          Ra = gadd(Ra, Sa);
+          Rb = gadd(Rb, Sb);
         }
       }
     } else {
@@ -250,11 +262,13 @@ __global__ void __launch_bounds__(256) k_h2(HK k, int RB) {
 }
 
 // ---------------------------------------------------------------- H3
-__global__ void __launch_bounds__(256) k_h3(HK k, int CB) {
-  extern __shared__ double2 smem[];
-  double2* tw_s = smem;
+template <typename C, typename CI>
+__global__ void __launch_bounds__(256) k_h3(HK<C, CI> k, int CB) {
+  using T = decltype(C().x);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tw_s = reinterpret_cast<C*>(smem_raw);
   int* perm_s = reinterpret_cast<int*>(tw_s + k.Nx);
-  double2* seq = tw_s + k.Nx + (k.Nx + 1) / 2;
+  C* seq = reinterpret_cast<C*>(perm_s + ((k.Nx + 3) / 4) * 4);
   const int lev = blockIdx.y;
   const int c0 = blockIdx.x * CB;
   const int ncb = min(CB, k.Mc - c0);
@@ -276,28 +290,29 @@ __global__ void __launch_bounds__(256) k_h3(HK k, int CB) {
     const size_t oidx = k.full_out ? ((size_t)lev * k.Nx + kf) * k.Nk + c
                                    : (size_t)lev * k.M + (size_t)r * k.Mc + c;
     for (int f = 0; f < nout; ++f) {
-      double2 val;
+      C val;
       if (k.form == HF_FLUX) {
-        const double2 G = seq[((size_t)(2 * f) * CB + cc) * k.Nx + pos];
-        const double2 H = seq[((size_t)(2 * f + 1) * CB + cc) * k.Nx + pos];
-        const double kx = k.kx_full[kf];
-        val = make_double2(fma(-kx, G.y, H.x), fma(kx, G.x, H.y));
+        const C G = seq[((size_t)(2 * f) * CB + cc) * k.Nx + pos];
+        const C H = seq[((size_t)(2 * f + 1) * CB + cc) * k.Nx + pos];
+        const T kx = k.kx_full[kf];
+        val = gmk<C>(fma(-kx, G.y, H.x), fma(kx, G.x, H.y));
       } else {
         val = seq[((size_t)f * CB + cc) * k.Nx + pos];
       }
-      double2* out = (f == 0) ? k.Aq : (f == 1 ? k.Aw : k.Ath);
+      C* out = (f == 0) ? k.Aq : (f == 1 ? k.Aw : k.Ath);
       out[oidx] = val;
     }
   }
 }
 
-size_t table_bytes(int Nx) { return (size_t)Nx * sizeof(double2) + (size_t)((Nx + 1) / 2) * sizeof(double2); }
+template <typename C>
+size_t table_bytes(int Nx) { return (size_t)Nx * sizeof(C) + (size_t)((Nx + 3) / 4) * 4 * sizeof(int); }
 
-}  // namespace
-
-cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const HorizArgs& a,
-                              cudaStream_t st, int* nlaunch) {
-  HK k;
+template <typename C, typename CI>
+cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, const HorizArgsT<C, CI>& a,
+                                cudaStream_t st, int* nlaunch) {
+  using T = decltype(C().x);
+  HK<C, CI> k;
   const Dims& d = p.d;
   k.Nx = d.Nx; k.Nk = d.Nk; k.K = d.K; k.Mr = d.Mr; k.Mc = d.Mc; k.M = d.M;
   k.levels = a.levels;
@@ -312,7 +327,7 @@ cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const H
   if (a.form == HF_FLUX) { k.nf1 = 5; k.nprod = k.sponge ? 9 : 6; k.ng = 6; }
   else if (a.form == HF_JAC) { k.nf1 = k.sponge ? 11 : 8; k.nprod = 3; k.ng = 3; }
   else { k.nf1 = 1; k.nprod = 1; k.ng = 1; }
-  k.scale = 1.0 / ((double)d.Nx * (double)d.Nx);
+  k.scale = (T)(1.0 / ((double)d.Nx * (double)d.Nx));
   k.plan = p.plan;
   k.psi = a.psi; k.q = a.q; k.w = a.w; k.th = a.th;
   k.kx_full = t.kx_full; k.ky_full = t.ky_full; k.inv_denom = t.inv_denom;
@@ -321,45 +336,70 @@ cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const H
   k.Aq = a.Aq; k.Aw = a.Aw; k.Ath = a.Ath;
   const size_t need1 = (size_t)k.nf1 * a.levels * k.cols_in * d.Nx;
   const size_t need2 = (size_t)k.ng * a.levels * d.Mc * d.Nx;
-  if (need1 > w.x1_elems || need2 > w.x2_elems) return cudaErrorInvalidValue;
-  k.x1 = w.x1; k.x2 = w.x2;
+  const size_t cap1 = w.x1_elems * sizeof(double2) / sizeof(C);
+  const size_t cap2 = w.x2_elems * sizeof(double2) / sizeof(C);
+  if (need1 > cap1 || need2 > cap2) return cudaErrorInvalidValue;
+  k.x1 = reinterpret_cast<C*>(w.x1);
+  k.x2 = reinterpret_cast<C*>(w.x2);
 
-  const size_t tb = table_bytes(d.Nx);
+  const size_t tb = table_bytes<C>(d.Nx);
   const size_t budget = 200 * 1024;
-  // H1: CB columns per CTA
-  int CB1 = (int)((96 * 1024) / ((size_t)k.nf1 * d.Nx * sizeof(double2)));
+  int CB1 = (int)((96 * 1024) / ((size_t)k.nf1 * d.Nx * sizeof(C)));
   CB1 = max(1, min(CB1, k.cols_in));
-  size_t sm1 = tb + (size_t)k.nf1 * CB1 * d.Nx * sizeof(double2);
+  size_t sm1 = tb + (size_t)k.nf1 * CB1 * d.Nx * sizeof(C);
   if (sm1 > budget) return cudaErrorInvalidConfiguration;
-  // H2: RB rows per CTA (even, divides Nx)
   int RB = 2;
   while (RB * 2 <= 16 && d.Nx % (RB * 2) == 0 &&
-         tb + (size_t)(k.nf1 + k.nprod) * RB * d.Nx * sizeof(double2) <= budget)
+         tb + (size_t)(k.nf1 + k.nprod) * RB * d.Nx * sizeof(C) <= budget)
     RB *= 2;
-  size_t sm2 = tb + (size_t)(k.nf1 + k.nprod) * (RB / 2) * d.Nx * sizeof(double2);
+  size_t sm2 = tb + (size_t)(k.nf1 + k.nprod) * (RB / 2) * d.Nx * sizeof(C);
   if (sm2 > budget) return cudaErrorInvalidConfiguration;
-  int CB3 = (int)((96 * 1024) / ((size_t)k.ng * d.Nx * sizeof(double2)));
+  int CB3 = (int)((96 * 1024) / ((size_t)k.ng * d.Nx * sizeof(C)));
   CB3 = max(1, min(CB3, d.Mc));
-  size_t sm3 = tb + (size_t)k.ng * CB3 * d.Nx * sizeof(double2);
+  size_t sm3 = tb + (size_t)k.ng * CB3 * d.Nx * sizeof(C);
   if (sm3 > budget) return cudaErrorInvalidConfiguration;
 
-  cudaFuncSetAttribute(k_h1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
-  cudaFuncSetAttribute(k_h2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
-  cudaFuncSetAttribute(k_h3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
+  cudaFuncSetAttribute(k_h1<C, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
+  cudaFuncSetAttribute(k_h2<C, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
+  cudaFuncSetAttribute(k_h3<C, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
   dim3 g1((k.cols_in + CB1 - 1) / CB1, a.levels);
-  w.prof.begin("h1_col_ifft", st);
-  k_h1<<<g1, 256, sm1, st>>>(k, CB1);
+  w.prof.begin(sizeof(T) == 4 ? "h1_col_ifft_f32" : "h1_col_ifft", st);
+  k_h1<C, CI><<<g1, 256, sm1, st>>>(k, CB1);
   w.prof.end(st);
   dim3 g2(d.Nx / RB, a.levels);
-  w.prof.begin("h2_row_products", st);
-  k_h2<<<g2, 256, sm2, st>>>(k, RB);
+  w.prof.begin(sizeof(T) == 4 ? "h2_row_products_f32" : "h2_row_products", st);
+  k_h2<C, CI><<<g2, 256, sm2, st>>>(k, RB);
   w.prof.end(st);
   dim3 g3((d.Mc + CB3 - 1) / CB3, a.levels);
-  w.prof.begin("h3_col_fft", st);
-  k_h3<<<g3, 256, sm3, st>>>(k, CB3);
+  w.prof.begin(sizeof(T) == 4 ? "h3_col_fft_f32" : "h3_col_fft", st);
+  k_h3<C, CI><<<g3, 256, sm3, st>>>(k, CB3);
   w.prof.end(st);
   if (nlaunch) *nlaunch += 3;
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const HorizArgs& a,
+                              cudaStream_t st, int* nlaunch) {
+  HTables<double2> ht{t.kx_full, t.ky_full, t.inv_denom, t.eta, t.sponge, t.eta_phys, t.tw, t.perm};
+  HorizArgsT<double2, double2> at{a.form, a.sponge, a.eta, a.full_in, a.full_out, a.psi_derived,
+                                  a.levels, a.psi, a.q, a.w, a.th, a.Aq, a.Aw, a.Ath};
+  return launch_horizontal_t<double2, double2>(p, ht, w, at, st, nlaunch);
+}
+
+cudaError_t launch_horizontal_f32(const Params& p, const Tables& t, Work& w,
+                                  const HorizArgsT<float2, float2>& a, cudaStream_t st,
+                                  int* nlaunch) {
+  HTables<float2> ht{t.kx_f, t.ky_f, t.inv_denom, t.eta_f, t.sponge_f, t.eta_phys_f, t.tw_f, t.perm};
+  return launch_horizontal_t<float2, float2>(p, ht, w, a, st, nlaunch);
+}
+
+cudaError_t launch_horizontal_f32_from64(const Params& p, const Tables& t, Work& w,
+                                         const HorizArgsT<float2, double2>& a, cudaStream_t st,
+                                         int* nlaunch) {
+  HTables<float2> ht{t.kx_f, t.ky_f, t.inv_denom, t.eta_f, t.sponge_f, t.eta_phys_f, t.tw_f, t.perm};
+  return launch_horizontal_t<float2, double2>(p, ht, w, a, st, nlaunch);
 }
 
 }  // namespace nhqg
