@@ -44,6 +44,7 @@ enum { NHQG_CLOSURE_FIXED_CONDUCTION = 0, NHQG_CLOSURE_EVOLVE_MEAN = 1 };
 enum { NHQG_EXCHANGE_LEGACY = 0, NHQG_EXCHANGE_BALANCED_SBP2 = 1,
        NHQG_EXCHANGE_BALANCED_SBP2_PC = 2 };
 enum { NHQG_WBC_DIRICHLET = 0, NHQG_WBC_NEUMANN = 1 };
+enum { NHQG_PRECISION_FP64 = 0, NHQG_PRECISION_MIXED = 1 };
 
 /*
  * Host-side description of a Grid (nhqg/grid.py:29-141 Grid fields, built by
@@ -78,6 +79,12 @@ typedef struct nhqg_grid_desc {
   const double *mean_solve;                    /* (P,P) inverse of the tau'd
                                                   1-D mean operator (legacy
                                                   evolve_mean), else NULL */
+  const double *shell_coef;                    /* (n_shells,2) per shell_inv row:
+                                                  alpha_w_eff and
+                                                  (gamma dt)^2 c_k / alpha_q at the
+                                                  shell's rounded |k|^2
+                                                  (nhqg/grid.py:398-430); NULL
+                                                  disables NHQG_PRECISION_MIXED */
 } nhqg_grid_desc;
 
 typedef struct nhqg_ctx nhqg_ctx;
@@ -100,6 +107,24 @@ int nhqg_ctx_destroy(nhqg_ctx *ctx);
  * sanitize_state), in place.  The input must be band-limited (every state
  * that sanitize_state, make_initial_state, run or imex_step produced is). */
 int nhqg_step(nhqg_ctx *ctx, nhqg_state *state, int n_steps, void *stream);
+
+/* Arithmetic of the following nhqg_step / nhqg_explicit_rhs /
+ * nhqg_implicit_solve calls.  It has no counterpart in the reference, whose
+ * only precision switch is float_dtype (nhqg/config.py:59), which changes
+ * every array.
+ *   NHQG_PRECISION_FP64 (default): the plain path, all FP64, the reference's
+ *     dense per-shell inverses.
+ *   NHQG_PRECISION_MIXED: the 2/3-rule products and the Chebyshev <-> nodal
+ *     transforms that feed them and read them back run in FP32; the Galerkin
+ *     stencils, stage combinations, the SBP2 mean exchange and the implicit w
+ *     solve stay FP64, the last as an O(Nz) Chebyshev-tau solve per mode
+ *     instead of the dense shell inverse.  Not supported
+ *     (NHQG_ERR_UNSUPPORTED): legacy evolve_mean (its nodal exchange
+ *     product), Nz whose 2*Nz is not 2^a 3^b, Nz > 886, and a descriptor
+ *     without shell_coef.
+ * The first switch to MIXED allocates 6 FP32 fields of (Nz+1) x (2/3-band
+ * modes) each. */
+int nhqg_set_precision(nhqg_ctx *ctx, int precision);
 
 /* explicit_rhs (nhqg/solver.py:510-599) at `in`, written to `out`.
  * closure/exchange select the Grid flavour the reference call would see

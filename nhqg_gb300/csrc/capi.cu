@@ -25,6 +25,10 @@ struct nhqg_ctx {
   double2 *Q1, *W1, *T1p, *T1, *Q2, *W2, *T2p, *T2, *Wcgl, *Wsbp, *Tsbp, *Tcgl;
   // 1-D vectors [P]
   double *tb0, *tb1p, *tb1, *tb2p, *tb2, *E1tb, *E2tb, *Itb, *flux, *dtb;
+  // mixed-precision path: FP32 nodal inputs and outputs of the horizontal
+  // products, allocated by the first nhqg_set_precision(NHQG_PRECISION_MIXED)
+  int precision = NHQG_PRECISION_FP64;
+  float2 *Qf = nullptr, *Wf = nullptr, *Tf = nullptr, *Aqf = nullptr, *Awf = nullptr, *Atf = nullptr;
 };
 
 namespace {
@@ -115,7 +119,7 @@ double2 twiddle(long k, long n) {
 
 extern "C" {
 
-const char* nhqg_version(void) { return "nhqg_gb300 0.1 (sm_103a, FP64 plain path)"; }
+const char* nhqg_version(void) { return "nhqg_gb300 0.2 (sm_103a, FP64 plain and mixed-precision paths)"; }
 
 int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   if (!g || !out) return NHQG_ERR_BAD_ARG;
@@ -233,6 +237,43 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.perm_v, perm.data(), L);
   }
 
+  // ---- FP32 copies of the horizontal and DCT tables (mixed-precision path) ----
+  {
+    auto f32 = [](const double* a, size_t n) {
+      std::vector<float> v(n);
+      for (size_t i = 0; i < n; ++i) v[i] = (float)a[i];
+      return v;
+    };
+    auto c32 = [](const std::vector<double2>& a) {
+      std::vector<float2> v(a.size());
+      for (size_t i = 0; i < a.size(); ++i) v[i] = make_float2((float)a[i].x, (float)a[i].y);
+      return v;
+    };
+    std::vector<float> kxf = f32(g->kx, d.Nx), kyf = f32(g->ky, d.Nk);
+    UP(t.kx_f, kxf.data(), kxf.size());
+    UP(t.ky_f, kyf.data(), kyf.size());
+    std::vector<double2> tw(d.Nx);
+    for (int k = 0; k < d.Nx; ++k) tw[k] = twiddle(k, d.Nx);
+    std::vector<float2> twf = c32(tw);
+    UP(t.tw_f, twf.data(), twf.size());
+    if (p.fast_dct) {
+      std::vector<double2> twv(2 * (size_t)N);
+      for (int k = 0; k < 2 * N; ++k) twv[k] = twiddle(k, 2 * N);
+      std::vector<float2> twvf = c32(twv);
+      UP(t.tw_v_f, twvf.data(), twvf.size());
+    }
+    if (p.has_sponge) {
+      std::vector<float> v = f32(g->sponge_phys, (size_t)d.Nx * d.Nx);
+      UP(t.sponge_f, v.data(), v.size());
+    }
+    if (p.has_eta) {
+      std::vector<float> v = f32(g->eta_phys, (size_t)d.Nx * d.Nx);
+      UP(t.eta_phys_f, v.data(), v.size());
+      std::vector<float2> e = c32(eta);
+      UP(t.eta_f, e.data(), e.size());
+    }
+  }
+
   // ---- vertical tables ----
   UP(t.V, g->V, (size_t)P * P);
   UP(t.Vinv, g->V_inv, (size_t)P * P);
@@ -302,6 +343,22 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     }
     UP(t.shell_start, start.data(), start.size());
     UP(t.shell_modes, modes.data(), modes.size());
+    // per-shell tau factors of the mixed-precision w solve
+    if (g->shell_coef && tau_smem_bytes(N) <= 227 * 1024) {
+      std::vector<int> mshell(M);
+      std::vector<double> coef(2 * (size_t)t.n_shells);
+      for (int sidx = 0; sidx < t.n_shells; ++sidx) {
+        coef[2 * sidx] = g->shell_coef[2 * (size_t)used[sidx]];
+        coef[2 * sidx + 1] = g->shell_coef[2 * (size_t)used[sidx] + 1];
+        for (int q = start[sidx]; q < start[sidx + 1]; ++q) mshell[modes[q]] = sidx;
+      }
+      std::vector<double> tab, par, uni;
+      build_tau_tables(N, p.wbc == NHQG_WBC_NEUMANN, t.n_shells, coef.data(), tab, par, uni);
+      UP(t.mode_shell, mshell.data(), mshell.size());
+      UP(t.tau_tab, tab.data(), tab.size());
+      UP(t.tau_par, par.data(), par.size());
+      UP(t.tau_uni, uni.data(), uni.size());
+    }
   }
 
   // ---- work buffers ----
@@ -397,6 +454,29 @@ int nhqg_profile_report(nhqg_ctx* c, char* buf, int buflen) {
   return (int)out.size() < buflen ? NHQG_OK : NHQG_ERR_BAD_ARG;
 }
 
+int nhqg_set_precision(nhqg_ctx* c, int precision) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  if (precision == NHQG_PRECISION_FP64) {
+    c->precision = precision;
+    return NHQG_OK;
+  }
+  if (precision != NHQG_PRECISION_MIXED) return NHQG_ERR_BAD_ARG;
+  const Params& p = c->p;
+  if (!p.fast_dct || !c->t.tw_v_f || !c->t.tau_tab) return NHQG_ERR_UNSUPPORTED;
+  if (p.closure == NHQG_CLOSURE_EVOLVE_MEAN && p.exchange == NHQG_EXCHANGE_LEGACY)
+    return NHQG_ERR_UNSUPPORTED;
+  if (!c->Qf) {
+    const size_t fe = (size_t)p.d.P * p.d.M;
+    float2** bufs[] = {&c->Qf, &c->Wf, &c->Tf, &c->Aqf, &c->Awf, &c->Atf};
+    for (float2** b : bufs) {
+      if (dalloc(c, b, fe) != cudaSuccess) return NHQG_ERR_CUDA;
+      if (cudaMemset(*b, 0, fe * sizeof(float2)) != cudaSuccess) return NHQG_ERR_CUDA;
+    }
+  }
+  c->precision = precision;
+  return NHQG_OK;
+}
+
 }  // extern "C"
 
 // ============================================================== orchestration
@@ -431,6 +511,26 @@ int scatter_fields(nhqg_ctx* c, const double2* q, const double2* w, const double
   return NHQG_OK;
 }
 
+bool mixed(const nhqg_ctx* c) { return c->precision == NHQG_PRECISION_MIXED; }
+
+// FP32 products of the mixed-precision path on the FP32 nodal fields
+int horizontal_step_f32(nhqg_ctx* c, const float2* qn, const float2* wn, const float2* tn,
+                        cudaStream_t st) {
+  const Params& p = c->p;
+  HorizArgsT<float2, float2> a{};
+  a.form = p.advection == NHQG_ADV_JACOBIAN ? HF_JAC : HF_FLUX;
+  a.sponge = p.has_sponge;
+  a.eta = p.has_eta;
+  a.full_in = false;
+  a.full_out = false;
+  a.psi_derived = true;
+  a.levels = p.d.P;
+  a.psi = nullptr; a.q = qn; a.w = wn; a.th = tn;
+  a.Aq = c->Aqf; a.Aw = c->Awf; a.Ath = c->Atf;
+  CK(launch_horizontal_f32(p, c->t, c->w, a, st, &c->launches));
+  return NHQG_OK;
+}
+
 int horizontal_step(nhqg_ctx* c, const double2* qn, const double2* wn, const double2* tn,
                     cudaStream_t st) {
   const Params& p = c->p;
@@ -454,6 +554,12 @@ int explicit_front(nhqg_ctx* c, const double2* q, const double2* w, const double
                    const double* tb, bool legacy_mean, double* Etb, double* Itb, bool need_q,
                    cudaStream_t st) {
   const Params& p = c->p;
+  if (mixed(c)) {
+    if (legacy_mean) return NHQG_ERR_UNSUPPORTED;
+    PCK("vfwd_f32", launch_vfwd_f32(p, c->t, need_q ? q : nullptr, w, t, c->Qf, c->Wf, c->Tf, st));
+    c->launches += 1;
+    return horizontal_step_f32(c, c->Qf, c->Wf, c->Tf, st);
+  }
   PCK("vfwd", launch_vfwd(p, c->t, need_q ? q : nullptr, w, t, c->Qn, c->Wn, c->Tn, st));
   c->launches += 1;
   if (legacy_mean) {
@@ -468,6 +574,7 @@ int explicit_front(nhqg_ctx* c, const double2* q, const double2* w, const double
 VArgs base_vargs(nhqg_ctx* c) {
   VArgs a{};
   a.Aq = c->Aq; a.Aw = c->Aw; a.At = c->At;
+  if (mixed(c)) { a.Aqf = c->Aqf; a.Awf = c->Awf; a.Atf = c->Atf; }
   a.E1q = c->E1q; a.E1w = c->E1w; a.E1t = c->E1t;
   a.Wn = c->Wn;
   a.Rq = c->Rq; a.Rt = c->Rt; a.rhs_w = c->rhs;
@@ -476,7 +583,11 @@ VArgs base_vargs(nhqg_ctx* c) {
 
 int solve_back(nhqg_ctx* c, double2* qo, double2* wo, double2* to, bool zero_mean, cudaStream_t st) {
   const Params& p = c->p;
-  PCK("shell_solve", launch_shell(p, c->t, c->rhs, wo, st));
+  if (mixed(c)) {
+    PCK("tau_solve", launch_tau_solve(p, c->t, c->rhs, wo, st));
+  } else {
+    PCK("shell_solve", launch_shell(p, c->t, c->rhs, wo, st));
+  }
   PCK("vpost", launch_vpost(p, c->t, c->Rq, c->Rt, wo, qo, to, zero_mean, st));
   c->launches += 2;
   return NHQG_OK;
@@ -530,9 +641,16 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
   // ---------------- stage 2
   if (have_nodal_wt) {
     // nodal w and theta of state1 come out of the corrector
-    PCK("vfwd", launch_vfwd(p, c->t, c->Q1, nullptr, nullptr, c->Qn, nullptr, nullptr, st));
-    c->launches += 1;
-    if ((rc = horizontal_step(c, c->Qn, c->Wcgl, c->Tcgl, st))) return rc;
+    if (mixed(c)) {
+      PCK("vfwd_f32", launch_vfwd_f32(p, c->t, c->Q1, nullptr, nullptr, c->Qf, nullptr, nullptr, st));
+      PCK("to_f32", launch_to_f32(p, c->Wcgl, c->Tcgl, c->Wf, c->Tf, st));
+      c->launches += 2;
+      if ((rc = horizontal_step_f32(c, c->Qf, c->Wf, c->Tf, st))) return rc;
+    } else {
+      PCK("vfwd", launch_vfwd(p, c->t, c->Q1, nullptr, nullptr, c->Qn, nullptr, nullptr, st));
+      c->launches += 1;
+      if ((rc = horizontal_step(c, c->Qn, c->Wcgl, c->Tcgl, st))) return rc;
+    }
   } else {
     rc = explicit_front(c, c->Q1, c->W1, t1, tb1, legacy_mean, c->E2tb, c->Itb, true, st);
     if (rc) return rc;

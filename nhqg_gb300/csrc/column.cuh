@@ -47,6 +47,31 @@ __device__ __forceinline__ void tstore(const double2* b, double2* __restrict__ d
     if (m < M) dst[(size_t)l * M + m] = b[i];
   }
 }
+// FP32 tiles of the mixed-precision path: load / store float2 columns and
+// convert between the FP64 and FP32 tiles
+__device__ __forceinline__ void tload(float2* b, const float2* __restrict__ src, int nlev, int m0,
+                                      int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    b[i] = (m < M) ? src[(size_t)l * M + m] : make_float2(0.f, 0.f);
+  }
+}
+__device__ __forceinline__ void tstore(const float2* b, float2* __restrict__ dst, int nlev, int m0,
+                                       int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    if (m < M) dst[(size_t)l * M + m] = b[i];
+  }
+}
+__device__ __forceinline__ void tcvt(float2* f, const double2* b, int nlev) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x)
+    f[i] = make_float2((float)b[i].x, (float)b[i].y);
+}
+__device__ __forceinline__ void tcvt(double2* b, const float2* f, int nlev) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x)
+    b[i] = make_double2((double)f[i].x, (double)f[i].y);
+}
+
 // out[i] = sum_{j<nin} Mat[i*ld + j] in[j], i < nout
 __device__ __forceinline__ void tmat(double2* out, const double2* in, const double* __restrict__ Mat,
                                      int ld, int nout, int nin) {

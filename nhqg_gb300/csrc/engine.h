@@ -27,7 +27,7 @@ struct Tables {
   // FFT over Nx
   double2* tw = nullptr;  // [Nx]
   int* perm = nullptr;    // [Nx]
-  // FP32 copies for the mixed-precision path
+  // FP32 copies for the mixed-precision path (kx_f [Nx], ky_f [Nk] full layout)
   float *kx_f = nullptr, *ky_f = nullptr, *sponge_f = nullptr, *eta_phys_f = nullptr;
   float2 *eta_f = nullptr, *tw_f = nullptr, *tw_v_f = nullptr;
   // FFT over 2*Nz (DCT-I of the vertical columns)
@@ -56,6 +56,9 @@ struct Tables {
   int* shell_modes = nullptr;   // [M]
   int n_shells = 0;
   int max_shell_modes = 0;
+  // O(N) tau solve of the mixed-precision path (null: not available)
+  int* mode_shell = nullptr;  // [M] shell of each compact mode (order of shell_inv)
+  double *tau_tab = nullptr, *tau_par = nullptr, *tau_uni = nullptr;
 };
 
 struct Params {
@@ -79,6 +82,7 @@ inline col::Dct make_dct(const Params& p, const Tables& t) {
   d.fast = p.fast_dct;
   d.plan = p.plan_v;
   d.tw = t.tw_v;
+  d.tw_f = t.tw_v_f;
   d.perm = t.perm_v;
   d.V = t.V;
   d.Vinv = t.Vinv;
@@ -168,9 +172,6 @@ cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const H
 
 cudaError_t launch_horizontal_f32(const Params& p, const Tables& t, Work& w,
                                   const HorizArgsT<float2, float2>& a, cudaStream_t st, int* nlaunch);
-cudaError_t launch_horizontal_f32_from64(const Params& p, const Tables& t, Work& w,
-                                         const HorizArgsT<float2, double2>& a, cudaStream_t st,
-                                         int* nlaunch);
 
 // vertical / column engine
 enum VBackMode { VB_RHS = 0, VB_STAGE1 = 1, VB_STAGE2 = 2, VB_SOLVE = 3 };
@@ -178,8 +179,10 @@ struct VArgs {
   // state the step started from (y_n) and stage-1 state (s1); predictor theta
   const double2 *q0, *w0, *t0;
   const double2 *q1, *w1, *t1, *t1p;
-  // explicit operands (nodal A) and stored E1
+  // explicit operands (nodal A) and stored E1; the mixed-precision path
+  // passes A in FP32 (Aqf, Awf, Atf non-null) instead
   const double2 *Aq, *Aw, *At;
+  const float2 *Aqf, *Awf, *Atf;
   double2 *E1q, *E1w, *E1t;
   // nodal w (legacy exchange product), dtb nodal vector
   const double2* Wn;
@@ -195,7 +198,20 @@ struct VArgs {
 };
 cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, const double2* w,
                         const double2* th, double2* qn, double2* wn, double2* tn, cudaStream_t st);
+cudaError_t launch_vfwd_f32(const Params& p, const Tables& t, const double2* q, const double2* w,
+                            const double2* th, float2* qn, float2* wn, float2* tn, cudaStream_t st);
 cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st);
+// FP64 nodal fields (the corrector's w and theta) -> FP32, P*M elements each
+cudaError_t launch_to_f32(const Params& p, const double2* a, const double2* b, float2* fa,
+                          float2* fb, cudaStream_t st);
+// O(N) tau solve of the per-shell w system (the mixed-precision path's
+// replacement for the dense shell inverses)
+cudaError_t launch_tau_solve(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
+                             cudaStream_t st);
+// host factorisation of the per-shell tau systems; coef = [n_shells][2] (a, s)
+void build_tau_tables(int Nz, bool open_top, int n_shells, const double* coef,
+                      std::vector<double>& tab, std::vector<double>& par, std::vector<double>& uni);
+size_t tau_smem_bytes(int Nz);
 cudaError_t launch_shell(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
                          cudaStream_t st);
 cudaError_t launch_vpost(const Params& p, const Tables& t, const double2* Rq, const double2* Rt,

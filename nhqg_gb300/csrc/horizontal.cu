@@ -395,11 +395,4 @@ cudaError_t launch_horizontal_f32(const Params& p, const Tables& t, Work& w,
   return launch_horizontal_t<float2, float2>(p, ht, w, a, st, nlaunch);
 }
 
-cudaError_t launch_horizontal_f32_from64(const Params& p, const Tables& t, Work& w,
-                                         const HorizArgsT<float2, double2>& a, cudaStream_t st,
-                                         int* nlaunch) {
-  HTables<float2> ht{t.kx_f, t.ky_f, t.inv_denom, t.eta_f, t.sponge_f, t.eta_phys_f, t.tw_f, t.perm};
-  return launch_horizontal_t<float2, double2>(p, ht, w, a, st, nlaunch);
-}
-
 }  // namespace nhqg

@@ -14,6 +14,9 @@
 // pinv_w(proj_w(x)) == pinv_w(x) because pinv reads only the first Nz-1
 // Chebyshev coefficients and the tau projection rewrites only the last two,
 // so the tau projections that feed a pinv are not applied.
+#include <algorithm>
+#include <type_traits>
+
 #include "column.cuh"
 #include "engine.h"
 
@@ -25,6 +28,7 @@ using col::TM;
 using col::NT;
 using col::tload;
 using col::tstore;
+using col::tcvt;
 using col::tmat;
 using col::tstencil_dir;
 using col::tpinv_dir;
@@ -65,20 +69,40 @@ __device__ __forceinline__ void tpinv_w(const VK& k, double2* x, const double2* 
 __device__ __forceinline__ int mode_of(int idx, int m0) { return m0 + (idx % TM); }
 
 // =========================================================== forward: to nodal
+// DCT of the FP64 tile src (ready) to nodal values in the precision of CO,
+// stored to out; spare is a free FP64 tile used as scratch.
+template <typename CO>
+__device__ __forceinline__ void to_nodal(const VK& k, const col::DctSharedT<CO>& ds,
+                                         const double2* src, double2* spare, CO* out, int m0) {
+  if constexpr (sizeof(CO) == sizeof(double2)) {
+    tdct(spare, src, k.dct, ds, false, k.P);
+    __syncthreads();
+    tstore(spare, out, k.P, m0, k.M);
+  } else {
+    float2* fs = reinterpret_cast<float2*>(spare);
+    float2* fo = fs + k.P * TM;
+    tcvt(fs, src, k.P);
+    __syncthreads();
+    tdct(fo, fs, k.dct, ds, false, k.P);
+    __syncthreads();
+    tstore(fo, out, k.P, m0, k.M);
+  }
+}
+
+// CO = double2: plain FP64 path; CO = float2: the mixed-precision path keeps
+// the Galerkin stencils in FP64 and runs the DCT in FP32.
+template <typename CO>
 __global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const double2* w,
-                                             const double2* th, double2* qn, double2* wn,
-                                             double2* tn) {
+                                             const double2* th, CO* qn, CO* wn, CO* tn) {
   extern __shared__ double2 sm[];
   double2* b0 = sm;
   double2* b1 = sm + k.P * TM;
-  const col::DctShared ds = col::dct_shared(k.dct, sm + 2 * k.P * TM);
+  const col::DctSharedT<CO> ds = col::dct_shared<CO>(k.dct, sm + 2 * k.P * TM);
   const int m0 = blockIdx.x * TM;
   if (q) {
     tload(b0, q, k.P, m0, k.M);
     __syncthreads();
-    tdct(b1, b0, k.dct, ds, false, k.P);
-    __syncthreads();
-    tstore(b1, qn, k.P, m0, k.M);
+    to_nodal(k, ds, b0, b1, qn, m0);
     __syncthreads();
   }
   if (w) {
@@ -86,9 +110,7 @@ __global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const doubl
     __syncthreads();
     tstencil_w(k, b1, b0);
     __syncthreads();
-    tdct(b0, b1, k.dct, ds, false, k.P);
-    __syncthreads();
-    tstore(b0, wn, k.P, m0, k.M);
+    to_nodal(k, ds, b1, b0, wn, m0);
     __syncthreads();
   }
   if (th) {
@@ -96,28 +118,45 @@ __global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const doubl
     __syncthreads();
     tstencil_dir(b1, b0, k.P, k.G);
     __syncthreads();
-    tdct(b0, b1, k.dct, ds, false, k.P);
+    to_nodal(k, ds, b1, b0, tn, m0);
+  }
+}
+
+// Chebyshev coefficients (FP64 tile out) of the nodal explicit operand A,
+// read in FP64 (Ad) or FP32 (Af, inverse DCT in FP32); tmp is a free tile.
+template <bool F32A, typename DS>
+__device__ __forceinline__ void a_to_coef(const VK& k, const DS& ds, const double2* Ad,
+                                          const float2* Af, double2* tmp, double2* out, int m0) {
+  if constexpr (!F32A) {
+    tload(tmp, Ad, k.P, m0, k.M);
     __syncthreads();
-    tstore(b0, tn, k.P, m0, k.M);
+    tdct(out, tmp, k.dct, ds, true, k.P);
+  } else {
+    float2* fi = reinterpret_cast<float2*>(tmp);
+    float2* fo = fi + k.P * TM;
+    tload(fi, Af, k.P, m0, k.M);
+    __syncthreads();
+    tdct(fo, fi, k.dct, ds, true, k.P);
+    __syncthreads();
+    tcvt(out, fo, k.P);
   }
 }
 
 // =========================================================== back + stage + solve-pre
-template <int MODE>
+template <int MODE, bool F32A>
 __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   extern __shared__ double2 sm[];
   const int PT = k.P * TM;
   double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT, *b4 = sm + 4 * PT;
-  const col::DctShared ds = col::dct_shared(k.dct, sm + 5 * PT);
+  using CA = typename std::conditional<F32A, float2, double2>::type;
+  const col::DctSharedT<CA> ds = col::dct_shared<CA>(k.dct, sm + 5 * PT);
   const int m0 = blockIdx.x * TM;
   const int P = k.P, G = k.G, M = k.M;
   const size_t Ms = (size_t)M;
 
   // ------------------------------------------------------------- q
   if (MODE != VB_SOLVE) {
-    tload(b0, a.Aq, P, m0, M);
-    __syncthreads();
-    tdct(b1, b0, k.dct, ds, true, P);
+    a_to_coef<F32A>(k, ds, a.Aq, a.Aqf, b0, b1, m0);
     __syncthreads();
     // E_q = -Aq - i beta kx psi, psi = -inv_denom * q_state
     const double2* qs = (MODE == VB_STAGE2) ? a.q1 : a.q0;
@@ -186,9 +225,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
 
   // ------------------------------------------------------------- w
   if (MODE != VB_SOLVE) {
-    tload(b0, a.Aw, P, m0, M);
-    __syncthreads();
-    tdct(b1, b0, k.dct, ds, true, P);
+    a_to_coef<F32A>(k, ds, a.Aw, a.Awf, b0, b1, m0);
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
     __syncthreads();
@@ -242,16 +279,20 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
 
   // ------------------------------------------------------------- theta
   if (MODE != VB_SOLVE) {
-    tload(b0, a.At, P, m0, M);
-    __syncthreads();
-    if (a.dtb_nodal != nullptr) {  // legacy evolve_mean: + (dTheta/dZ)_nodal * w_nodal
-      for (int i = threadIdx.x; i < PT; i += blockDim.x) {
-        const int l = i / TM, m = mode_of(i, m0);
-        if (m < M) b0[i] = caxpy(a.dtb_nodal[l], a.Wn[(size_t)l * Ms + m], b0[i]);
-      }
+    if constexpr (!F32A) {
+      tload(b0, a.At, P, m0, M);
       __syncthreads();
+      if (a.dtb_nodal != nullptr) {  // legacy evolve_mean: + (dTheta/dZ)_nodal * w_nodal
+        for (int i = threadIdx.x; i < PT; i += blockDim.x) {
+          const int l = i / TM, m = mode_of(i, m0);
+          if (m < M) b0[i] = caxpy(a.dtb_nodal[l], a.Wn[(size_t)l * Ms + m], b0[i]);
+        }
+        __syncthreads();
+      }
+      tdct(b1, b0, k.dct, ds, true, P);
+    } else {  // the mixed path has no legacy evolve_mean term
+      a_to_coef<true>(k, ds, nullptr, a.Atf, b0, b1, m0);
     }
-    tdct(b1, b0, k.dct, ds, true, P);
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
     __syncthreads();
@@ -574,38 +615,82 @@ inline size_t vsmem(const Params& p, int nbuf, bool dct = false) {
 }
 inline int vgrid(const Params& p) { return (p.d.M + TM - 1) / TM; }
 
+template <typename CO>
+cudaError_t vfwd_t(const Params& p, const Tables& t, const double2* q, const double2* w,
+                   const double2* th, CO* qn, CO* wn, CO* tn, cudaStream_t st) {
+  VK k = make_vk(p, t);
+  const size_t sm = vsmem(p, 2, true);
+  cudaFuncSetAttribute(k_vfwd<CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_vfwd<CO><<<vgrid(p), NT, sm, st>>>(k, q, w, th, qn, wn, tn);
+  return cudaGetLastError();
+}
+
+template <int MODE, bool F32A>
+void vback_t(const VK& k, const VArgs& a, size_t sm, int grid, cudaStream_t st) {
+  cudaFuncSetAttribute(k_vback<MODE, F32A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_vback<MODE, F32A><<<grid, NT, sm, st>>>(k, a);
+}
+
 }  // namespace
 
 cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, const double2* w,
                         const double2* th, double2* qn, double2* wn, double2* tn, cudaStream_t st) {
-  VK k = make_vk(p, t);
-  const size_t sm = vsmem(p, 2, true);
-  cudaFuncSetAttribute(k_vfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_vfwd<<<vgrid(p), NT, sm, st>>>(k, q, w, th, qn, wn, tn);
-  return cudaGetLastError();
+  return vfwd_t<double2>(p, t, q, w, th, qn, wn, tn, st);
+}
+
+cudaError_t launch_vfwd_f32(const Params& p, const Tables& t, const double2* q, const double2* w,
+                            const double2* th, float2* qn, float2* wn, float2* tn, cudaStream_t st) {
+  if (!p.fast_dct || !t.tw_v_f) return cudaErrorInvalidValue;
+  return vfwd_t<float2>(p, t, q, w, th, qn, wn, tn, st);
 }
 
 cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st) {
   VK k = make_vk(p, t);
   const size_t sm = vsmem(p, 5, true);
+  const int g = vgrid(p);
+  const bool f32 = a.Aqf != nullptr;
+  if (f32 && (!p.fast_dct || !t.tw_v_f || a.dtb_nodal || !a.Awf || !a.Atf))
+    return cudaErrorInvalidValue;
   switch (mode) {
     case VB_RHS:
-      cudaFuncSetAttribute(k_vback<VB_RHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      k_vback<VB_RHS><<<vgrid(p), NT, sm, st>>>(k, a);
+      if (f32) vback_t<VB_RHS, true>(k, a, sm, g, st); else vback_t<VB_RHS, false>(k, a, sm, g, st);
       break;
     case VB_STAGE1:
-      cudaFuncSetAttribute(k_vback<VB_STAGE1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      k_vback<VB_STAGE1><<<vgrid(p), NT, sm, st>>>(k, a);
+      if (f32) vback_t<VB_STAGE1, true>(k, a, sm, g, st); else vback_t<VB_STAGE1, false>(k, a, sm, g, st);
       break;
     case VB_STAGE2:
-      cudaFuncSetAttribute(k_vback<VB_STAGE2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      k_vback<VB_STAGE2><<<vgrid(p), NT, sm, st>>>(k, a);
+      if (f32) vback_t<VB_STAGE2, true>(k, a, sm, g, st); else vback_t<VB_STAGE2, false>(k, a, sm, g, st);
       break;
     default:
-      cudaFuncSetAttribute(k_vback<VB_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      k_vback<VB_SOLVE><<<vgrid(p), NT, sm, st>>>(k, a);
+      vback_t<VB_SOLVE, false>(k, a, sm, g, st);
       break;
   }
+  return cudaGetLastError();
+}
+
+namespace {
+
+__global__ void k_to_f32(const double2* __restrict__ a, const double2* __restrict__ b,
+                         float2* __restrict__ fa, float2* __restrict__ fb, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double2 x = a[i], y = b[i];
+    fa[i] = make_float2((float)x.x, (float)x.y);
+    fb[i] = make_float2((float)y.x, (float)y.y);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_to_f32(const Params& p, const double2* a, const double2* b, float2* fa,
+                          float2* fb, cudaStream_t st) {
+  const size_t n = (size_t)p.d.P * p.d.M;
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t want = (n + 255) / 256;
+  const int grid = (int)std::min<size_t>(want, (size_t)(sms > 0 ? sms : 1) * 8);
+  k_to_f32<<<grid, 256, 0, st>>>(a, b, fa, fb, n);
   return cudaGetLastError();
 }
 

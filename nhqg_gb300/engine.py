@@ -84,10 +84,13 @@ class Engine:
             d.sponge_phys = arr("sponge", g.sponge_phys)
         if g.mean_solve is not None:
             d.mean_solve = arr("mean_solve", g.mean_solve)
+        if getattr(g, "imex_shell_coef", None) is not None:
+            d.shell_coef = arr("shell_coef", np.ravel(g.imex_shell_coef))
         self._desc = d
         handle = ctypes.c_void_p()
         nat.check(self.lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(handle)), "nhqg_ctx_create")
         self.handle = handle
+        self.precision = "fp64"
         self._finalizer = weakref.finalize(self, Engine._destroy, self.lib, handle.value)
 
     @staticmethod
@@ -125,13 +128,25 @@ class Engine:
     def launches(self) -> int:
         return int(self.lib.nhqg_last_launch_count(self.handle))
 
+    def set_precision(self, precision: str) -> None:
+        """'fp64' (plain path) or 'mixed' (FP32 products and transforms, FP64
+        solves and mean exchange) for the following step / RHS / solve calls."""
+        if precision not in nat.PRECISION:
+            raise ValueError(f"precision must be one of {sorted(nat.PRECISION)}, got {precision!r}")
+        if precision != self.precision:
+            nat.check(self.lib.nhqg_set_precision(self.handle, nat.PRECISION[precision]),
+                      f"nhqg_set_precision({precision!r})")
+            self.precision = precision
+
     # ------------------------------------------------------------- entry points
-    def step(self, q, w, th, tb, n_steps: int = 1) -> None:
+    def step(self, q, w, th, tb, n_steps: int = 1, precision: str = "fp64") -> None:
+        self.set_precision(precision)
         s = self.state_desc(q, w, th, tb)
         nat.check(self.lib.nhqg_step(self.handle, ctypes.byref(s), int(n_steps), _stream_handle()),
                   "nhqg_step")
 
-    def explicit_rhs(self, src, dst, closure: str, exchange: str) -> None:
+    def explicit_rhs(self, src, dst, closure: str, exchange: str, precision: str = "fp64") -> None:
+        self.set_precision(precision)
         a, b = self.state_desc(*src), self.state_desc(*dst)
         nat.check(self.lib.nhqg_explicit_rhs(self.handle, ctypes.byref(a), ctypes.byref(b),
                                              nat.CLOSURE[closure], nat.EXCHANGE[exchange],
@@ -143,7 +158,8 @@ class Engine:
                                                   nat.CLOSURE[closure], _stream_handle()),
                   "nhqg_implicit_tendency")
 
-    def implicit_solve(self, src, dst, closure: str) -> None:
+    def implicit_solve(self, src, dst, closure: str, precision: str = "fp64") -> None:
+        self.set_precision(precision)
         a, b = self.state_desc(*src), self.state_desc(*dst)
         nat.check(self.lib.nhqg_implicit_solve(self.handle, ctypes.byref(a), ctypes.byref(b),
                                                nat.CLOSURE[closure], _stream_handle()),

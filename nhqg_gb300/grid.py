@@ -96,6 +96,7 @@ class Grid(NamedTuple):
     imex_shell_row: np.ndarray       # (Nx, Nk) row of imex_inv, -1 outside the band
     eta_phys: np.ndarray | None      # (Nx, Nx) irfft2(eta_hat)
     mean_solve: np.ndarray | None    # (P, P) inverse of the tau'd legacy mean operator
+    imex_shell_coef: np.ndarray      # (rows of imex_inv, 2) alpha_w_eff, (gamma dt)^2 c_k / alpha_q
     cfg: NHQGConfig
 
 
@@ -174,7 +175,11 @@ def _tau_projection(rows: np.ndarray, N: int) -> np.ndarray:
 def _shell_inverse(kv, hyper_order, gamma, dt, nu_q, nu_w, nu_theta, drag, sigma,
                    Ra_sigma, Ld_inv_sq, WG, G_Z, w_stencil, NG, buoyancy_K):
     """A'^-1 for one shell, evaluated with the reference's operation order
-    (nhqg/grid.py:398-430), q_boundary='none'."""
+    (nhqg/grid.py:398-430), q_boundary='none', and the shell's scalar
+    coefficients (alpha_w_eff, (gamma dt)^2 c_k / alpha_q) of
+    A' = alpha_w_eff I - (gamma dt)^2 c_k / alpha_q pinv_w G_Z^2 S_w, which the
+    O(Nz) tau solve of the mixed-precision path uses (c_k = 0 when
+    |k|^2 + Ld^-2 = 0)."""
     ksq_p = kv ** hyper_order
     alpha_q = 1.0 + gamma * dt * (nu_q * ksq_p + drag)
     alpha_w = 1.0 + gamma * dt * nu_w * ksq_p
@@ -186,12 +191,13 @@ def _shell_inverse(kv, hyper_order, gamma, dt, nu_q, nu_w, nu_theta, drag, sigma
         couple = alpha_w * np.eye(NG) - (gamma * dt) ** 2 * (Ra_sigma / alpha_th) * buoyancy_K
     denom = kv + Ld_inv_sq
     if denom == 0.0:
-        return np.linalg.inv(couple)
+        return np.linalg.inv(couple), (alpha_w_eff, 0.0)
     c_k = 1.0 / denom
     # (WG @ q_solve) with q_solve = (1/alpha_q) I is WG scaled entrywise
     # (each entry is one product plus exact zeros in the GEMM).
     B = ((WG * (1.0 / alpha_q)) @ G_Z) @ w_stencil
-    return np.linalg.inv(couple - (gamma * dt) ** 2 * c_k * B)
+    coef = (alpha_w_eff, (gamma * dt) ** 2 * c_k / alpha_q)
+    return np.linalg.inv(couple - (gamma * dt) ** 2 * c_k * B), coef
 
 
 def make_grid(cfg: NHQGConfig) -> Grid:
@@ -351,11 +357,12 @@ def make_grid(cfg: NHQGConfig) -> Grid:
     args = (p, gamma_imex, dt, cfg.nu_q, cfg.nu_w, cfg.nu_theta, cfg.drag, cfg.sigma, Ra_sigma,
             cfg.Ld_inv_sq, WG, G_Z, w_stencil, N - 1, buoyancy_K)
     imex_inv = np.empty((len(used), N - 1, N - 1))
+    shell_coef = np.empty((len(used), 2))
 
     # one shell at a time: the BLAS inside each product is already threaded
     # (host threads around threaded BLAS calls oversubscribe the cores)
     for i in range(len(used)):
-        imex_inv[i] = _shell_inverse(unique_ksq[used[i]], *args)
+        imex_inv[i], shell_coef[i] = _shell_inverse(unique_ksq[used[i]], *args)
 
     mean_solve = None
     if cfg.thermal_closure == "evolve_mean" and cfg.mean_exchange_discretization == "legacy":
@@ -386,5 +393,6 @@ def make_grid(cfg: NHQGConfig) -> Grid:
         sbp_transfer_mode=cfg.sbp_transfer_mode,
         sbp_corrector_substeps=int(cfg.sbp_corrector_substeps),
         imex_matmul_chunk=int(cfg.imex_matmul_chunk),
-        imex_shell_row=shell_row, eta_phys=eta_phys, mean_solve=mean_solve, cfg=cfg,
+        imex_shell_row=shell_row, eta_phys=eta_phys, mean_solve=mean_solve,
+        imex_shell_coef=shell_coef, cfg=cfg,
     )

@@ -10,6 +10,12 @@ are accepted and copied to the device.  Functions return new tensors, like
 the reference's functional JAX API; ``step_inplace`` advances a state in
 place for drivers that own their buffers (the analogue of donation).
 
+``precision`` (an addition without a reference counterpart) selects the
+plain FP64 path ('fp64', the default) or the mixed-precision path ('mixed':
+FP32 horizontal products and the Chebyshev <-> nodal transforms around them,
+FP64 Galerkin stencils, stage combinations, implicit solves and SBP2 mean
+exchange).
+
 Every computation runs in the CUDA engine; there is no CPU path.
 """
 
@@ -78,40 +84,42 @@ def sanitize_state(state, grid: Grid) -> State:
     return s
 
 
-def step_inplace(state: State, grid: Grid, n_steps: int = 1, check: bool = False) -> State:
+def step_inplace(state: State, grid: Grid, n_steps: int = 1, check: bool = False,
+                 precision: str = "fp64") -> State:
     """Advance ``state`` (CUDA tensors, reference layout) by ``n_steps``
     imex_step applications in place; stream-ordered, no host sync unless
     ``check`` (then the band-limit status is verified)."""
     eng = engine_for(grid)
-    eng.step(*state, n_steps=n_steps)
+    eng.step(*state, n_steps=n_steps, precision=precision)
     if check:
         _check_band(eng, "imex_step")
     return state
 
 
-def imex_step(state, grid: Grid) -> State:
+def imex_step(state, grid: Grid, precision: str = "fp64") -> State:
     """One IMEX step incl. ``sanitize_state`` (nhqg/solver.py:1228-1242)."""
     s = _copy(state)
-    return step_inplace(s, grid, 1, check=True)
+    return step_inplace(s, grid, 1, check=True, precision=precision)
 
 
 def _split(grid: Grid) -> bool:
     return grid.mean_exchange_discretization in ("balanced_sbp2", "balanced_sbp2_pc")
 
 
-def explicit_rhs(state, grid: Grid) -> State:
+def explicit_rhs(state, grid: Grid, precision: str = "fp64") -> State:
     """Explicit tendency E (nhqg/solver.py:510-599) for ``grid``'s closure."""
     eng = engine_for(grid)
     src = to_device(state)
     out = _fresh(src)
-    eng.explicit_rhs(src, out, grid.thermal_closure, grid.mean_exchange_discretization)
+    eng.explicit_rhs(src, out, grid.thermal_closure, grid.mean_exchange_discretization,
+                     precision=precision)
     _check_band(eng, "explicit_rhs")
     return out
 
 
-def explicit_rhs_dispatch(state, grid: Grid) -> State:
+def explicit_rhs_dispatch(state, grid: Grid, precision: str = "fp64") -> State:
     """nhqg/solver.py:602-608 (vertical_dealiasing='none')."""
-    return explicit_rhs(state, grid)
+    return explicit_rhs(state, grid, precision=precision)
 
 
 def implicit_tendency(state, grid: Grid) -> State:
@@ -124,13 +132,15 @@ def implicit_tendency(state, grid: Grid) -> State:
     return out
 
 
-def imex_implicit_solve(R_q, R_w, R_th, grid: Grid):
-    """Block-eliminated implicit stage solve (nhqg/solver.py:691-738)."""
+def imex_implicit_solve(R_q, R_w, R_th, grid: Grid, precision: str = "fp64"):
+    """Block-eliminated implicit stage solve (nhqg/solver.py:691-738); with
+    precision='mixed' the w system is solved by the O(Nz) Chebyshev-tau
+    recurrence instead of the dense shell inverse (both FP64)."""
     eng = engine_for(grid)
     zero = torch.zeros(grid.Nz + 1, dtype=torch.float64, device="cuda")
     src = to_device((R_q, R_w, R_th, zero))
     out = _fresh(src)
-    eng.implicit_solve(src, out, grid.thermal_closure)
+    eng.implicit_solve(src, out, grid.thermal_closure, precision=precision)
     _check_band(eng, "imex_implicit_solve")
     return out.q_hat, out.w_hat, out.th_hat
 
@@ -155,7 +165,7 @@ def apply_balanced_sbp2_corrector(state, grid: Grid, total_dt) -> State:
 
 
 def run(grid: Grid, state, n_steps: int, save_interval: int, use_imex: bool = True,
-        callback=None):
+        callback=None, precision: str = "fp64"):
     """Time loop (nhqg/solver.py:1385-1416): sanitize the incoming state, then
     advance in chunks of ``save_interval`` steps; returns (state, snapshots)
     with snapshots = [(t, State copy), ...]."""
@@ -165,7 +175,7 @@ def run(grid: Grid, state, n_steps: int, save_interval: int, use_imex: bool = Tr
     snaps = []
     n_outer = n_steps // save_interval
     for i in range(n_outer):
-        step_inplace(s, grid, save_interval, check=(i == 0))
+        step_inplace(s, grid, save_interval, check=(i == 0), precision=precision)
         step = (i + 1) * save_interval
         t = step * float(grid.dt)
         if callback is not None:
@@ -173,5 +183,5 @@ def run(grid: Grid, state, n_steps: int, save_interval: int, use_imex: bool = Tr
         snaps.append((t, State(*(x.clone() for x in s))))
     rem = n_steps % save_interval
     if rem:
-        step_inplace(s, grid, rem, check=(n_outer == 0))
+        step_inplace(s, grid, rem, check=(n_outer == 0), precision=precision)
     return s, snaps
