@@ -4,17 +4,21 @@
 Workload (the headline configuration): Nx=Ny=256, Nz=256, L = 10 L_c
 (L_c = 2 pi / 1.3048), Ra~=100, Pr=1, nu=1 (Laplacian), dt=2e-5, flux-form
 advection, 2/3-rule dealiasing, evolve_mean closure with the balanced SBP2
-predictor/corrector (4 substeps), float64, ARS(2,2,2).  Input: the seeded
-theta' start (1e-3 N(0,1) sin(pi Z), PCG64 seed 0) -- synthetic; the
-5000-step spin-up of the precision study is not run (the step's work does
-not depend on the state).  Every step streams several GB, far above the
+predictor/corrector (4 substeps), ARS(2,2,2).  Input: the seeded theta'
+start (1e-3 N(0,1) sin(pi Z), PCG64 seed 0) -- synthetic -- spun up by
+--spinup plain FP64 steps (100 by default; the precision study's 5000-step
+spin-up is available with --spinup 5000, about 4 minutes).  The step's work
+does not depend on the state.  Every step streams several GB, far above the
 129 MB L2, so no explicit L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-The default arm times the plain FP64 GPU step; ``--impl reference`` times the
-CPU port of the reference algorithm (NumPy/SciPy on all host cores) on the
-same workload.  One JSON line on stdout (rank 0).
+The default arm times the mixed-precision step (value, the headline) and the
+plain FP64 step (plain_fp64) on the same state, and reports the per-field
+relative L2 difference of the mixed state from the plain one after 1 and
+--err-steps steps.  ``--impl reference`` times the CPU port of the reference
+algorithm (NumPy/SciPy on all host cores) on the same workload.  One JSON
+line on stdout (rank 0).
 """
 
 from __future__ import annotations
@@ -116,36 +120,62 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ roofline bookkeeping
-def kernel_work(name: str, g, launches: int) -> tuple[float, float]:
-    """(FP64 flops, algorithmic DRAM bytes) per launch for the algorithm the
-    engine runs.  FFT: 5 n log2 n flops per complex length-n transform; dense
-    vertical transforms: 4 P^2 flops per complex column; shell solve 4 G^2."""
-    Nx, P, G = g.Nx, g.Nz + 1, g.Nz - 1
+NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # FFMA lanes x 2 flops x max SM clock
+
+
+def kernel_work(name: str, g, launches_per_step: int) -> tuple[float, float, str]:
+    """(algorithmic flops, algorithmic DRAM bytes, limiting pipe) per launch of
+    one kernel class, for the algorithm the engine runs.
+
+    FFTs: 5 n log2 n flops per complex length-n transform.  Vertical DCT-I:
+    an FFT of length 2 Nz per complex column (5 (2Nz) log2(2Nz)); dense
+    fallback 4 P^2.  Bytes: each field read or written once per launch
+    (complex128 = 16 B, complex64 = 8 B); the FFT intermediates of the
+    horizontal products make one HBM round trip between the three kernels.
+    The pipe is 'fp64' or 'fp32' (arithmetic) -- the GB300 FP64 rate is 1/64
+    of FP32, so every FP64 kernel is arithmetic-bound -- or 'hbm'."""
+    Nx, Nz = g.Nx, g.Nz
+    P, G = Nz + 1, Nz - 1
     K = Nx // 3
     Mc, Mr = K + 1, 2 * K + 1
     M = Mr * Mc
+    f32 = name.endswith("_f32")
+    base = name[:-4] if f32 else name
+    cplx = 8.0 if f32 else 16.0
+    pipe = "fp32" if f32 else "fp64"
     fft = 5.0 * Nx * math.log2(Nx)
-    cplx = 16.0
+    L = 2 * Nz
+    smooth = L
+    for f in (2, 3):
+        while smooth % f == 0:
+            smooth //= f
+    dct = 5.0 * L * math.log2(L) if smooth == 1 else 4.0 * P * P
     field = P * M * cplx
-    if name == "h1_col_ifft":
-        return 5 * Mc * P * fft, 3 * field + 5 * P * Mc * Nx * cplx
-    if name == "h2_row_products":
-        return (5 + 6) * (Nx / 2) * P * fft + 6 * Nx * Nx * P, (5 + 6) * P * Mc * Nx * cplx
-    if name == "h3_col_fft":
-        return 6 * Mc * P * fft, 6 * P * Mc * Nx * cplx + 3 * field
-    if name == "vfwd":
-        nf = 3 if launches <= 1 else 2  # 3 fields at stage 1, 1 at stage 2 (mean)
-        return nf * 4.0 * P * P * M, 2 * nf * field
+    field64 = P * M * 16.0
+    if base == "h1_col_ifft":
+        return 5 * Mc * P * fft, 3 * field + 5 * P * Mc * Nx * cplx, pipe
+    if base == "h2_row_products":
+        return (5 + 6) * (Nx / 2) * P * fft + 6 * Nx * Nx * P, (5 + 6) * P * Mc * Nx * cplx, pipe
+    if base == "h3_col_fft":
+        return 6 * Mc * P * fft, 6 * P * Mc * Nx * cplx + 3 * field, pipe
+    if base == "vfwd":
+        nf = 3 if launches_per_step <= 1 else 2  # 3 fields at stage 1, 1 at stage 2
+        return nf * dct * M, nf * (field64 + field), pipe
     if name in ("vback_stage1", "vback_stage2"):
-        return 3 * 4.0 * P * P * M, 12 * field
+        # 3 inverse DCTs of A (FP32 in the mixed step) + FP64 stage algebra
+        return 3 * dct * M, 12 * field64, "fp64"
     if name == "shell_solve":
         n_in = len(np.unique(g.imex_shell_row[g.imex_shell_row >= 0]))
-        return 4.0 * G * G * M, 2 * field + n_in * G * G * 8.0
+        return 4.0 * G * G * M, 2 * G * M * 16.0 + n_in * G * G * 8.0, "fp64"
+    if name == "tau_solve":
+        return 2 * 12.0 * Nz * M, 2 * G * M * 16.0, "fp64"
     if name == "corr_pre":
-        return 2 * 4.0 * P * P * M, 5 * field
+        return 2 * dct * M, 5 * field64, "fp64"
     if name == "corr_sub":
-        return 4.0 * P * G * M / 4.0, 4 * field
-    return 0.0, 0.0
+        return 2 * 8.0 * P * M, 4 * field64, "fp64"
+    if name == "to_f32":
+        return 0.0, 2 * P * M * (16.0 + 8.0), "hbm"
+    return 0.0, 0.0, "fp64"
 
 
 def dgemm_peak_tflops() -> float:
@@ -168,16 +198,55 @@ def dgemm_peak_tflops() -> float:
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def sgemm_peak_tflops() -> float:
+    """FP32 CUDA-core GEMM rate (TF32 off), the FP32 analogue of the DGEMM peak."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def measured_hbm_gbs() -> float | None:
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 # ------------------------------------------------------------------ CPU (oracle) arm
-def cpu_reference(cfgd: dict) -> dict:
+def workload_name(nx: int, nz: int) -> str:
+    return (f"{nx}^2x{nz} ARS222, evolve_mean balanced_sbp2_pc sub4, flux, 2/3 rule, "
+            "L=10Lc, Ra=100, Pr=1, dt=2e-5")
+
+
+def cpu_reference(cfgd: dict, samples: int = 1, warmup: int = 0) -> dict:
     """Time the NumPy/SciPy port of the reference step on all host cores.
 
-    A full oracle step at 256^2 x 256 is minutes of CPU time, so the sample is
-    one evaluation of each operator of the step and the step time is their
-    sum weighted by how often one ARS(2,2,2) + SBP2-PC step calls them:
+    A full oracle step at 256^2 x 256 is minutes of CPU time, so one sample
+    is one evaluation of each operator of the step, and the step time is
+    their sum weighted by how often one ARS(2,2,2) + SBP2-PC step calls them:
     2 x explicit RHS, 2 x implicit solve, 1 x implicit tendency,
     2 x SBP2 corrector (4 substeps each), 3 x stage combination.  The per-shell
-    table build (reference make_grid work) is excluded, as on the GPU side."""
+    table build (reference make_grid work) is excluded, as on the GPU side.
+    ``samples`` samples after ``warmup`` untimed ones; the value is their mean."""
     import oracle
     from oracle.nhqg_oracle import OracleConfig, OracleState
     cores = os.cpu_count() or 1
@@ -195,22 +264,85 @@ def cpu_reference(cfgd: dict) -> dict:
         out = fn()
         return time.perf_counter() - t, out
 
-    tE, E = timed(lambda: oracle.explicit_rhs(s, base))
-    tI, _ = timed(lambda: oracle.implicit_tendency(s, base))
-    tS, _ = timed(lambda: oracle.imex_implicit_solve(s.q_hat, s.w_hat, s.th_hat, base))
     alpha = g.gamma_imex * g.dt
-    tC, _ = timed(lambda: oracle.apply_balanced_sbp2_corrector(s, g, alpha))
-    tX, _ = timed(lambda: OracleState(*(a + alpha * e for a, e in zip(s, E))))
+
+    def one():
+        tE, E = timed(lambda: oracle.explicit_rhs(s, base))
+        tI, _ = timed(lambda: oracle.implicit_tendency(s, base))
+        tS, _ = timed(lambda: oracle.imex_implicit_solve(s.q_hat, s.w_hat, s.th_hat, base))
+        tC, _ = timed(lambda: oracle.apply_balanced_sbp2_corrector(s, g, alpha))
+        tX, _ = timed(lambda: OracleState(*(a + alpha * e for a, e in zip(s, E))))
+        return (tE, tS, tI, tC, tX)
+
+    for _ in range(warmup):
+        one()
+    parts = np.mean([one() for _ in range(max(1, samples))], axis=0)
+    tE, tS, tI, tC, tX = (float(x) for x in parts)
     t_step = 2 * tE + 2 * tS + tI + 2 * tC + 3 * tX
     return {"value": 1.0 / t_step, "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": (f"one evaluation of each step operator at {cfgd['Nx']}^2x{cfgd['Nz']} "
-                       f"(RHS {tE:.1f}s, implicit solve {tS:.1f}s, implicit tendency {tI:.1f}s, "
-                       f"SBP2 corrector {tC:.1f}s, stage combination {tX:.2f}s) summed as "
-                       "2E+2S+I+2C+3X; shell-table build excluded "
-                       f"({t_table:.0f}s); NumPy/SciPy execution of the reference algorithm (not XLA)")}
+            "sample": (f"{max(1, samples)} sample(s), each one evaluation of every step operator at "
+                       f"{cfgd['Nx']}^2x{cfgd['Nz']} (mean RHS {tE:.2f}s, implicit solve {tS:.2f}s, "
+                       f"implicit tendency {tI:.2f}s, SBP2 corrector {tC:.2f}s, stage combination "
+                       f"{tX:.3f}s) summed as 2E+2S+I+2C+3X; shell-table build excluded "
+                       f"({t_table:.0f}s); NumPy/SciPy execution of the reference algorithm, plain "
+                       "FP64 (not XLA)")}
 
 
 # ------------------------------------------------------------------ GPU arm
+def _rel(a, b) -> float:
+    import torch
+    den = float(torch.linalg.norm(b))
+    num = float(torch.linalg.norm(a - b))
+    return num / den if den > 0 else num
+
+
+def _timed_arm(S, grid, eng, state, precision, args, ws):
+    """Warm up, then CUDA-event time exactly args.steps single-step calls
+    bracketed by barrier + synchronize; per-kernel profile of the same steps."""
+    import torch
+    S.step_inplace(state, grid, max(3, args.warmup), check=True, precision=precision)
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    eng.profile(True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        S.step_inplace(state, grid, 1, precision=precision)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    prof = eng.profile_report()
+    eng.profile(False)
+    if eng.device_status() != 0:
+        raise RuntimeError(f"device status set during the timed {precision} steps")
+    return allmax(ms, ws), prof
+
+
+def _roofline(prof, grid, steps, peaks):
+    """Per kernel class: achieved rate of its limiting pipe against the
+    measured peak of that pipe, plus the HBM rate at algorithmic bytes."""
+    out = {}
+    for name, (n, ms) in prof.items():
+        flops, bytes_, pipe = kernel_work(name, grid, n // max(1, steps))
+        avg = ms / n
+        entry = {"launches": n, "avg_launch_ms": round(avg, 4), "pipe": pipe,
+                 "hbm_gbs_at_algorithmic_bytes": round(bytes_ / (avg * 1e-3) / 1e9, 1)}
+        if pipe in ("fp64", "fp32") and flops > 0:
+            ach = flops / (avg * 1e-3) / 1e12
+            entry.update(achieved=round(ach, 4), unit="TFLOP/s", peak=round(peaks[pipe], 4),
+                         frac=round(ach / peaks[pipe], 4), flops_per_launch=flops)
+        elif pipe == "hbm" and peaks.get("hbm"):
+            ach = bytes_ / (avg * 1e-3) / 1e9
+            entry.update(achieved=round(ach, 1), unit="GB/s", peak=peaks["hbm"],
+                         frac=round(ach / peaks["hbm"], 4))
+        entry["bytes_per_launch"] = bytes_
+        out[name] = entry
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import torch
     from nhqg_gb300 import NHQGConfig, make_grid, theta_perturbation_state
@@ -225,37 +357,37 @@ def run_ours(args, ws, rank, local):
     host0 = theta_perturbation_state(grid, seed=0)
     state = S.to_device(host0)
     eng = engine_for(grid)
-    peak = dgemm_peak_tflops() if rank == 0 else None
-    S.step_inplace(state, grid, max(3, args.warmup), check=True)
+    peaks = {"fp64": dgemm_peak_tflops(), "fp32": sgemm_peak_tflops(), "hbm": measured_hbm_gbs()}
+
+    # spin-up (plain FP64) from the seeded start, then the accuracy of the
+    # mixed step against the plain step from the same state
+    S.step_inplace(state, grid, args.spinup, check=True)
     torch.cuda.synchronize()
+    ref = S.State(*(t.clone() for t in state))
+    mix = S.State(*(t.clone() for t in state))
+    S.step_inplace(ref, grid, 1, check=True)
+    S.step_inplace(mix, grid, 1, check=True, precision="mixed")
+    names = ("q_hat", "w_hat", "th_hat", "th_bar")
+    err1 = {n: _rel(a, b) for n, a, b in zip(names, mix, ref)}
+    inc1 = {n: _rel(a - s0, b - s0) for n, a, b, s0 in zip(names, mix, ref, state)}
+    S.step_inplace(ref, grid, args.err_steps - 1, check=True)
+    S.step_inplace(mix, grid, args.err_steps - 1, check=True, precision="mixed")
+    errN = {n: _rel(a, b) for n, a, b in zip(names, mix, ref)}
+    del ref, mix
 
     clocks = ClockSampler(local)
     clocks.start()
-    barrier(ws)
-    torch.cuda.synchronize()
-    eng.profile(True)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        S.step_inplace(state, grid, 1)
-    e1.record()
-    torch.cuda.synchronize()
-    barrier(ws)
-    ms = e0.elapsed_time(e1)
-    prof = eng.profile_report()
-    eng.profile(False)
+    ms_plain, prof_plain = _timed_arm(S, grid, eng, S.State(*(t.clone() for t in state)), "fp64", args, ws)
+    ms_mixed, prof_mixed = _timed_arm(S, grid, eng, state, "mixed", args, ws)
     clk = clocks.stop()
-    if eng.device_status() != 0:
-        raise RuntimeError("device status set during the timed region")
     finite = all(bool(torch.isfinite(torch.view_as_real(t) if t.is_complex() else t).all()) for t in state)
-    ms_max = allmax(ms, ws)
-    value = ws * args.steps / (ms_max * 1e-3)
+    value = ws * args.steps / (ms_mixed * 1e-3)
+    value_plain = ws * args.steps / (ms_plain * 1e-3)
 
-    # end to end through the public API with pinned host buffers
-    pinned = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in host0]
+    # end to end through the public API with pinned host buffers (mixed path)
+    pinned = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in S.to_host(state)]
     outs = [torch.empty_like(p).pin_memory() for p in pinned]
-    S.imex_step(pinned, grid)
+    S.imex_step(pinned, grid, precision="mixed")
     torch.cuda.synchronize()
     e2e_steps = max(1, min(args.steps, 10))
     barrier(ws)
@@ -263,7 +395,7 @@ def run_ours(args, ws, rank, local):
     ee1 = torch.cuda.Event(enable_timing=True)
     ee0.record()
     for _ in range(e2e_steps):
-        res = S.imex_step(pinned, grid)
+        res = S.imex_step(pinned, grid, precision="mixed")
         for o, r in zip(outs, res):
             o.copy_(r, non_blocking=True)
     ee1.record()
@@ -273,14 +405,22 @@ def run_ours(args, ws, rank, local):
 
     if rank != 0:
         return None
-    launches = sum(n for n, _ in prof.values())
-    dom = max(prof.items(), key=lambda kv: kv[1][1])
-    dname, (dn, dms) = dom
-    flops, bytes_ = kernel_work(dname, grid, dn // max(1, args.steps))
-    avg_ms = dms / dn
-    achieved = flops / (avg_ms * 1e-3) / 1e12
-    kernels = {k: {"launches": n, "ms_per_step": round(t / args.steps, 4),
-                   "share": round(t / sum(v[1] for v in prof.values()), 4)} for k, (n, t) in prof.items()}
+    roof_mixed = _roofline(prof_mixed, grid, args.steps, peaks)
+    roof_plain = _roofline(prof_plain, grid, args.steps, peaks)
+    dname = max(prof_mixed.items(), key=lambda kv: kv[1][1])[0]
+    dom = dict(roof_mixed[dname])
+    dom["kernel"] = dname
+    dom["bound"] = dom.pop("pipe")
+    dom["traffic"] = None
+    dom["peak_source"] = {"fp64": "cuBLAS DGEMM 8192^3 measured in this run",
+                          "fp32": "cuBLAS SGEMM 8192^3 (TF32 off) measured in this run",
+                          "hbm": "MEASURED_PEAKS.json hbm_gbs"}[dom["bound"]]
+
+    def shares(prof):
+        tot = sum(v[1] for v in prof.values())
+        return {k: {"launches": n, "ms_per_step": round(t / args.steps, 4), "share": round(t / tot, 4)}
+                for k, (n, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+
     line = {
         "metric": METRIC,
         "value": round(value, 4),
@@ -288,31 +428,34 @@ def run_ours(args, ws, rank, local):
         "n_gpus": ws,
         "steps": args.steps,
         "warmup": max(3, args.warmup),
-        "ms_per_step": round(ms_max / args.steps, 4),
+        "ms_per_step": round(ms_mixed / args.steps, 4),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
-        "data": "synthetic (seeded theta' 1e-3 N(0,1) sin(pi Z), PCG64 seed 0; no spin-up)",
-        "config": {"workload": f"{args.nx}^2x{args.nz} plain FP64 ARS222, balanced_sbp2_pc sub4, "
-                               "flux, 2/3 rule, L=10Lc, Ra=100, dt=2e-5",
-                   "path": "plain_fp64", "Nx": args.nx, "Nz": args.nz,
+        "dtype": "f32 products/transforms + f64 solves/exchange",
+        "data": (f"synthetic: seeded theta' 1e-3 N(0,1) sin(pi Z) (PCG64 seed 0), spun up by "
+                 f"{args.spinup} plain FP64 steps"),
+        "config": {"workload": workload_name(args.nx, args.nz), "path": "mixed", "Nx": args.nx, "Nz": args.nz,
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "state and per-step traffic >> 129 MB L2; no flush needed"},
+        "plain_fp64": {"value": round(value_plain, 4), "unit": "steps/s",
+                       "ms_per_step": round(ms_plain / args.steps, 4),
+                       "kernels": shares(prof_plain), "roofline": roof_plain},
+        "mixed_over_plain": round(value / value_plain, 3),
+        "rel_err_vs_plain": {"after_1_step": err1, "increment_1_step": inc1,
+                             f"after_{args.err_steps}_steps": errN},
         "simulated_time_per_wall_hour": round(3600.0 * cfgd["dt"] * value / ws, 6),
-        "gpu_launches": launches,
-        "roofline": {"kernel": dname, "bound": "fp64", "achieved": round(achieved, 4),
-                     "peak": round(peak, 4), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                     "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 pipe; "
-                                    "MEASURED_PEAKS.json has no FP64 figure)",
-                     "flops_per_launch": flops, "avg_launch_ms": round(avg_ms, 4),
-                     "hbm_gbs_at_algorithmic_bytes": round(bytes_ / (avg_ms * 1e-3) / 1e9, 1),
-                     "traffic": None},
-        "kernels": kernels,
+        "gpu_launches": sum(n for n, _ in prof_mixed.values()),
+        "roofline": dom,
+        "kernels": shares(prof_mixed),
+        "roofline_by_kernel": roof_mixed,
+        "peaks": {"fp64_tflops": round(peaks["fp64"], 4), "fp32_tflops": round(peaks["fp32"], 3),
+                  "hbm_gbs": peaks["hbm"], "fp32_nominal_tflops": round(NOMINAL_FP32_TFLOPS, 1)},
         "clocks": clk,
         "e2e": {"value": round(ws * e2e_steps / (e2e_ms * 1e-3), 4), "unit": "steps/s",
                 "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
-                "api": "nhqg_gb300.solver.imex_step(pinned host State) + D2H of the result"},
+                "api": "nhqg_gb300.solver.imex_step(pinned host State, precision='mixed') "
+                       "+ D2H of the result"},
         "finite": finite,
         "grid_build_s": round(t_grid, 2),
     }
@@ -322,17 +465,19 @@ def run_ours(args, ws, rank, local):
 
 
 def run_reference(args, ws, rank):
+    """CPU arm: the oracle port of the reference step on the host cores, on
+    this arm's workload, metric and units; rank 0 only."""
     if rank != 0:
         return None
     cfgd = workload(args.nx, args.nz)
-    cb = cpu_reference(cfgd)
+    cb = cpu_reference(cfgd, samples=args.steps, warmup=max(0, min(args.warmup, 1)))
     return {
         "metric": METRIC, "value": round(cb["value"], 6), "unit": "steps/s", "n_gpus": ws,
-        "steps": 1, "warmup": 1, "ms_per_step": round(1e3 / cb["value"], 2),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / cb["value"], 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded theta' start)", "impl": "reference",
-        "config": {"workload": f"{args.nx}^2x{args.nz} plain FP64 ARS222, balanced_sbp2_pc sub4, "
-                               "flux, 2/3 rule, L=10Lc, Ra=100, dt=2e-5", "path": "cpu_port"},
+        "config": {"workload": workload_name(args.nx, args.nz), "path": "cpu_port",
+                   "Nx": args.nx, "Nz": args.nz, "parallelism": "host cores"},
         "cpu_baseline": cb,
         "e2e": {"value": round(cb["value"], 6), "unit": "steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -347,6 +492,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--nz", type=int, default=256)
+    ap.add_argument("--spinup", type=int, default=100,
+                    help="plain FP64 steps from the seeded start before measuring")
+    ap.add_argument("--err-steps", type=int, default=100,
+                    help="steps of the mixed-vs-plain accuracy comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     ws, rank, local = dist_init()
