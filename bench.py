@@ -173,6 +173,10 @@ def kernel_work(name: str, g, launches_per_step: int) -> tuple[float, float, str
         return 2 * dct * M, 5 * field64, "fp64"
     if name == "corr_sub":
         return 2 * 8.0 * P * M, 4 * field64, "fp64"
+    if name == "corr_sub_mid":  # x = t - dt g w, two dots, R x + rank 2: memory-bound
+        return 2 * 16.0 * P * M, 3 * field64, "hbm"
+    if name == "corr_sub_last":  # + inverse DCT of y and the Dirichlet pseudo-inverse
+        return dct * M + 2 * 16.0 * P * M, 4 * field64, "fp64"
     if name == "to_f32":
         return 0.0, 2 * P * M * (16.0 + 8.0), "hbm"
     return 0.0, 0.0, "fp64"

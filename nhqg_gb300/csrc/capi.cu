@@ -1,5 +1,6 @@
 // C ABI of the NHQG GB300 engine: context creation (table upload), the
 // ARS(2,2,2) step orchestration and the per-operator entry points.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -319,6 +320,51 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     }
     UP(t.bcF, F.data(), F.size());
     UP(t.bcV, bv.data(), bv.size());
+    // fused substep tables: R = c2s s2c, Fs_j = s2c^T F_j, u_j = c2s bcV_j
+    const double* c2s = g->cgl_to_sbp;
+    const double* s2c = g->sbp_to_cgl;
+    std::vector<std::vector<std::pair<int, double>>> rows(P);
+    int rw = 1;
+    for (int l = 0; l < P; ++l) {
+      std::vector<double> acc(P, 0.0);
+      std::vector<char> hit(P, 0);
+      for (int i = 0; i < P; ++i) {
+        const double a = c2s[(size_t)l * P + i];
+        if (a == 0.0) continue;
+        for (int q = 0; q < P; ++q) {
+          const double b = s2c[(size_t)i * P + q];
+          if (b == 0.0) continue;
+          acc[q] = std::fma(a, b, acc[q]);
+          hit[q] = 1;
+        }
+      }
+      for (int q = 0; q < P; ++q)
+        if (hit[q]) rows[l].push_back({q, acc[q]});
+      rw = std::max(rw, (int)rows[l].size());
+    }
+    std::vector<int> rcol((size_t)P * rw, 0);
+    std::vector<double> rval((size_t)P * rw, 0.0);
+    for (int l = 0; l < P; ++l)
+      for (size_t q = 0; q < rows[l].size(); ++q) {
+        rcol[(size_t)l * rw + q] = rows[l][q].first;
+        rval[(size_t)l * rw + q] = rows[l][q].second;
+      }
+    std::vector<double> Fs(2 * (size_t)P, 0.0), Us(2 * (size_t)P, 0.0);
+    for (int j = 0; j < 2; ++j)
+      for (int l = 0; l < P; ++l) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < P; ++i) {
+          a = std::fma(s2c[(size_t)i * P + l], F[(size_t)j * P + i], a);
+          b = std::fma(c2s[(size_t)l * P + i], bv[(size_t)j * P + i], b);
+        }
+        Fs[(size_t)j * P + l] = a;
+        Us[(size_t)j * P + l] = b;
+      }
+    t.R_w = rw;
+    UP(t.R_col, rcol.data(), rcol.size());
+    UP(t.R_val, rval.data(), rval.size());
+    UP(t.Fs, Fs.data(), Fs.size());
+    UP(t.Us, Us.data(), Us.size());
   }
 
   // ---- shells present in the band ----

@@ -177,6 +177,63 @@ __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const doub
   }
 }
 
+// Non-final substep, fused: with x = theta_sbp - sub_dt g_half w_sbp (zero
+// at the two end levels), the round trip above is
+//   theta_sbp' = R x + u_0 (Fs_0 . x) + u_1 (Fs_1 . x)
+// with R = c2s s2c (a few nonzeros per row), Fs_j = s2c^T F_j, u_j = c2s V[:,N-1+j].
+// One CTA holds kSM consecutive modes (coalesced 256-byte level rows);
+// thread (level group lg, mode mm) visits levels lg, lg + 16, ...
+constexpr int kSM = 16;
+constexpr int kSubThreads = 256;
+constexpr int kLG = kSubThreads / kSM;  // level groups
+
+struct SubK {
+  int P, M, rw;
+  const int* Rcol;
+  const double *Rval, *Fs, *Us, *g_half;
+  double sub_dt;
+};
+
+__global__ void __launch_bounds__(kSubThreads) k_corr_sub_mid(SubK k, double2* __restrict__ tsbp,
+                                                              const double2* __restrict__ wsbp) {
+  extern __shared__ double2 xs[];          // [P][kSM]
+  __shared__ double2 part[2][kLG][kSM];    // partial dot products
+  const int P = k.P, M = k.M;
+  const int mm = threadIdx.x % kSM, lg = threadIdx.x / kSM;
+  const int m = blockIdx.x * kSM + mm;
+  const bool ok = m < M;
+  double2 d0 = czero(), d1 = czero();
+  for (int l = lg; l < P; l += kLG) {
+    double2 x = czero();
+    if (ok && l > 0 && l < P - 1) {
+      const size_t g = (size_t)l * M + m;
+      x = caxpy(-k.sub_dt * k.g_half[l], wsbp[g], tsbp[g]);
+    }
+    xs[l * kSM + mm] = x;
+    d0 = caxpy(k.Fs[l], x, d0);
+    d1 = caxpy(k.Fs[P + l], x, d1);
+  }
+  part[0][lg][mm] = d0;
+  part[1][lg][mm] = d1;
+  __syncthreads();
+  if (lg < 2) {  // 32 threads: (j, mm) totals, summed in a fixed order
+    double2 acc = czero();
+    for (int q = 0; q < kLG; ++q) acc = cadd(acc, part[lg][q][mm]);
+    part[lg][0][mm] = acc;
+  }
+  __syncthreads();
+  d0 = part[0][0][mm];
+  d1 = part[1][0][mm];
+  if (!ok) return;
+  for (int l = lg; l < P; l += kLG) {
+    double2 v = caxpy(k.Us[P + l], d1, cscale(d0, k.Us[l]));
+    const int* rc = k.Rcol + (size_t)l * k.rw;
+    const double* rv = k.Rval + (size_t)l * k.rw;
+    for (int q = 0; q < k.rw; ++q) v = caxpy(rv[q], xs[rc[q] * kSM + mm], v);
+    tsbp[(size_t)l * M + m] = v;
+  }
+}
+
 // ------------------------------------------------------------ 1-D kernels (one CTA)
 __device__ void vec_dense(double* out, const double* in, const double* Mat, int n, int ld, int ncol) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -241,21 +298,42 @@ __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt)
     B[idx] = b;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {  // banded LU without pivoting, in place (multipliers below the diagonal);
-                           // the diagonal slot keeps 1/pivot for the substitutions
+  if (threadIdx.x == 0) {
+    // banded LU without pivoting (multipliers below the diagonal; the
+    // diagonal slot keeps 1/pivot for the substitutions).  Row i of the band
+    // is (a0, a1, a2, a3, a4) = A[i, i-2 .. i+2]; the running values of the
+    // two rows below the current pivot stay in registers.
+    double r1_0 = P > 1 ? A[1 * P + 1] : 0.0, r1_1 = P > 1 ? A[2 * P + 1] : 0.0;  // row col+1: cols col, col+1
+    double r1_2 = P > 1 ? A[3 * P + 1] : 0.0;                                     //            col+2
+    double piv = A[2 * P + 0], u1 = A[3 * P + 0], u2 = A[4 * P + 0];               // row col: diag, +1, +2
     for (int col = 0; col < P; ++col) {
-      const double rp = 1.0 / A[2 * P + col];
+      const double rp = 1.0 / piv;
       A[2 * P + col] = rp;
-      for (int r = col + 1; r <= min(P - 1, col + 2); ++r) {
-        const int dr = col - r + 2;  // band slot of A[r, col]
-        const double l = A[dr * P + r] * rp;
-        A[dr * P + r] = l;
-        for (int c = col + 1; c <= min(P - 1, col + 2); ++c) {
-          const int drc = c - r + 2;
-          const int dcc = c - col + 2;
-          A[drc * P + r] = fma(-l, A[dcc * P + col], A[drc * P + r]);
-        }
+      // row col+2 (enters now): cols col, col+1, col+2
+      double r2_0 = 0.0, r2_1 = 0.0, r2_2 = 0.0, r2_3 = 0.0;
+      if (col + 2 < P) {
+        r2_0 = A[0 * P + col + 2];
+        r2_1 = A[1 * P + col + 2];
+        r2_2 = A[2 * P + col + 2];
+        r2_3 = A[3 * P + col + 2];
       }
+      double n_piv = 0.0, n_u1 = 0.0, n_u2 = 0.0;
+      if (col + 1 < P) {
+        const double l = r1_0 * rp;
+        A[1 * P + col + 1] = l;
+        n_piv = fma(-l, u1, r1_1);       // A[col+1, col+1]
+        n_u1 = fma(-l, u2, r1_2);        // A[col+1, col+2]
+        n_u2 = (col + 3 < P) ? A[4 * P + col + 1] : 0.0;  // A[col+1, col+3]
+        A[3 * P + col + 1] = n_u1;
+      }
+      if (col + 2 < P) {
+        const double l = r2_0 * rp;
+        A[0 * P + col + 2] = l;
+        r1_0 = fma(-l, u1, r2_1);        // A[col+2, col+1]
+        r1_1 = fma(-l, u2, r2_2);        // A[col+2, col+2]
+        r1_2 = r2_3;                     // A[col+2, col+3]
+      }
+      piv = n_piv; u1 = n_u1; u2 = n_u2;
     }
   }
   // tb_sbp = c2s (V tbp)
@@ -283,16 +361,24 @@ __global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, double*
   const double cf = k.mu * sub_dt;
   for (int i = threadIdx.x; i < P; i += blockDim.x) rhs[i] = (i == 0 || i == P - 1) ? 0.0 : fma(-cf, t2[i], rhs[i]);
   __syncthreads();
-  if (threadIdx.x == 0) {  // forward / back substitution
+  if (threadIdx.x == 0) {  // forward / back substitution, the last two values in registers
+    double v1 = rhs[0], v2 = 0.0;  // v_{i-1}, v_{i-2}
     for (int i = 1; i < P; ++i) {
-      double v = rhs[i];
-      for (int c = max(0, i - 2); c < i; ++c) v = fma(-A[(c - i + 2) * P + i], rhs[c], v);
+      double v = fma(-A[1 * P + i], v1, rhs[i]);
+      if (i >= 2) v = fma(-A[0 * P + i], v2, v);
       rhs[i] = v;
+      v2 = v1;
+      v1 = v;
     }
+    double x1 = 0.0, x2 = 0.0;  // x_{i+1}, x_{i+2}
     for (int i = P - 1; i >= 0; --i) {
       double v = rhs[i];
-      for (int c = i + 1; c <= min(P - 1, i + 2); ++c) v = fma(-A[(c - i + 2) * P + i], rhs[c], v);
-      rhs[i] = v * A[2 * P + i];
+      if (i + 1 < P) v = fma(-A[3 * P + i], x1, v);
+      if (i + 2 < P) v = fma(-A[4 * P + i], x2, v);
+      v *= A[2 * P + i];
+      rhs[i] = v;
+      x2 = x1;
+      x1 = v;
     }
   }
   __syncthreads();  // rhs = tb_new
@@ -443,6 +529,10 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   const size_t sm4 = 4 * (size_t)p.d.P * TM * sizeof(double2) + dsm;
   cudaFuncSetAttribute(k_corr_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
   cudaFuncSetAttribute(k_corr_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+  const size_t smid = (size_t)p.d.P * kSM * sizeof(double2);
+  const bool fused_mid = smid <= 200 * 1024 && t.R_col != nullptr;
+  if (fused_mid)
+    cudaFuncSetAttribute(k_corr_sub_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
   Profiler& pf = w.prof;
   pf.begin("corr_pre", st);
   k_corr_pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp);
@@ -468,10 +558,17 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
     pf.begin("corr_step_1d", st);
     k_corr_tstep<<<1, NT, 0, st>>>(k, w.vec, sub_dt, last, a.tb_out);
     pf.end(st);
-    pf.begin("corr_sub", st);
-    k_corr_sub<<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt, last,
-                                      a.t_out, a.tcgl);
-    pf.end(st);
+    if (!last && fused_mid) {
+      SubK sk{p.d.P, p.d.M, t.R_w, t.R_col, t.R_val, t.Fs, t.Us, w.vec + cv.g_half(), sub_dt};
+      pf.begin("corr_sub_mid", st);
+      k_corr_sub_mid<<<(p.d.M + kSM - 1) / kSM, kSubThreads, smid, st>>>(sk, a.tsbp, a.wsbp);
+      pf.end(st);
+    } else {
+      pf.begin(last ? "corr_sub_last" : "corr_sub", st);
+      k_corr_sub<<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt, last,
+                                        a.t_out, a.tcgl);
+      pf.end(st);
+    }
     n += 2;
   }
   if (nlaunch) *nlaunch += n;

@@ -42,6 +42,13 @@ struct Tables {
   double* s2c_val = nullptr;
   double* bcF = nullptr;    // [2*P] rows N-1, N of (proj_dir - I) V_inv
   double* bcV = nullptr;    // [2*P] columns N-1, N of V
+  // fused SBP2 substep: R = c2s s2c (rw nonzeros per row, padded), Fs =
+  // s2c^T bcF (2 rows), u = c2s bcV (2 columns)
+  int* R_col = nullptr;     // [P*rw]
+  double* R_val = nullptr;  // [P*rw]
+  int R_w = 0;
+  double* Fs = nullptr;     // [2*P]
+  double* Us = nullptr;     // [2*P]
   double* proj = nullptr;   // [P*P] proj_dirichlet
   double* D1 = nullptr;     // [P*P] SBP first derivative
   double* Lsbp = nullptr;   // [P*P] SBP Laplacian
