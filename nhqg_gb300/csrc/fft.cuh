@@ -66,6 +66,32 @@ template <typename C> __device__ __forceinline__ C gmulc(C a, C b) {
   return gmk<C>(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -a.x * b.y));
 }
 
+// Butterfly index split idx -> (sequence s, block blk, offset j) for nb
+// butterflies per sequence and span Ls: shifts and masks when both are powers
+// of two (every pass of a 2^a length), integer division otherwise.
+struct FftIndex {
+  int nb, Ls, lnb, lls;
+  bool p2;
+  __device__ __forceinline__ FftIndex(int nb_, int Ls_) : nb(nb_), Ls(Ls_) {
+    p2 = ((nb & (nb - 1)) == 0) && ((Ls & (Ls - 1)) == 0);
+    lnb = __ffs(nb) - 1;
+    lls = __ffs(Ls) - 1;
+  }
+  __device__ __forceinline__ void split(int idx, int& s, int& blk, int& j) const {
+    if (p2) {
+      s = idx >> lnb;
+      const int b = idx & (nb - 1);
+      blk = b >> lls;
+      j = b & (Ls - 1);
+    } else {
+      s = idx / nb;
+      const int b = idx - s * nb;
+      blk = b / Ls;
+      j = b - blk * Ls;
+    }
+  }
+};
+
 // Forward DFT (sign -1), natural -> reversed.  tw[k] = exp(-2 pi i k / n).
 template <typename C>
 __device__ __forceinline__ void fft_dif_fwd(C* __restrict__ data, int nseq, int stride,
@@ -77,9 +103,10 @@ __device__ __forceinline__ void fft_dif_fwd(C* __restrict__ data, int nseq, int 
     const int Ls = L / R;
     const int nb = pl.n / R;
     const int tws = pl.n / L;
+    const FftIndex ix(nb, Ls);
     for (int idx = threadIdx.x; idx < nseq * nb; idx += blockDim.x) {
-      const int s = idx / nb, b = idx - s * nb;
-      const int blk = b / Ls, j = b - blk * Ls;
+      int s, blk, j;
+      ix.split(idx, s, blk, j);
       C* a = data + s * stride + blk * L + j;
       if (R == 4) {
         const C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
@@ -139,9 +166,10 @@ __device__ __forceinline__ void fft_dit_inv(C* __restrict__ data, int nseq, int 
     const int Ls = L / R;
     const int nb = pl.n / R;
     const int tws = pl.n / L;
+    const FftIndex ix(nb, Ls);
     for (int idx = threadIdx.x; idx < nseq * nb; idx += blockDim.x) {
-      const int s = idx / nb, b = idx - s * nb;
-      const int blk = b / Ls, j = b - blk * Ls;
+      int s, blk, j;
+      ix.split(idx, s, blk, j);
       C* a = data + s * stride + blk * L + j;
       if (R == 4) {
         C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];

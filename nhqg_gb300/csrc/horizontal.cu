@@ -49,6 +49,12 @@ struct HK {
 template <typename C, typename CI>
 __device__ __forceinline__ C to_c(CI v) { C r; r.x = v.x; r.y = v.y; return r; }
 
+// H1 -> H2 -> H3 intermediates, pair-major: [field][level][x/2][column][x%2]
+template <typename K>
+__device__ __forceinline__ size_t xidx(const K& k, int f, int lev, int pair, int c, int cols) {
+  return ((((size_t)f * k.levels + lev) * (k.Nx / 2) + pair) * cols + c) * 2;
+}
+
 template <typename K>
 __device__ __forceinline__ int plane_index(const K& k, int r, int c) {
   return r * k.cols_in + c;
@@ -127,12 +133,15 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
   }
   __syncthreads();
   fft_dit_inv(seq, nseq, k.Nx, k.plan, tw_s);
+  // pair-major output: consecutive threads take (x parity, column), so the
+  // row pairs H2 reads are contiguous
+  const int half = k.Nx / 2;
   for (int i = threadIdx.x; i < k.nf1 * ncb * k.Nx; i += blockDim.x) {
-    const int x = i % k.Nx;
-    const int rest = i / k.Nx;
-    const int cc = rest % ncb, f = rest / ncb;
-    k.x1[(((size_t)f * k.levels + lev) * k.cols_in + (c0 + cc)) * k.Nx + x] =
-        seq[((size_t)f * CB + cc) * k.Nx + x];
+    const int par = i & 1, r2 = i >> 1;
+    const int cc = r2 % ncb, r3 = r2 / ncb;
+    const int pp = r3 % half, f = r3 / half;
+    const int x = 2 * pp + par;
+    k.x1[xidx(k, f, lev, pp, c0 + cc, k.cols_in) + par] = seq[((size_t)f * CB + cc) * k.Nx + x];
   }
 }
 
@@ -158,8 +167,8 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
     const int rest = i / k.cols_in;
     const int p = rest % NPR, f = rest / NPR;
     const int xa = x0 + 2 * p;
-    const size_t base = (((size_t)f * k.levels + lev) * k.cols_in + c) * k.Nx;
-    const C A = k.x1[base + xa], B = k.x1[base + xa + 1];
+    const size_t base = xidx(k, f, lev, xa >> 1, c, k.cols_in);
+    const C A = k.x1[base], B = k.x1[base + 1];
     C* s = in + ((size_t)f * NPR + p) * k.Nx;
     if (c == 0 || c == half) {
       s[perm_s[c]] = gmk<C>(A.x, B.x);
@@ -255,9 +264,9 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
     } else {
       split(g, Ra, Rb);
     }
-    const size_t base = (((size_t)g * k.levels + lev) * k.Mc + c) * k.Nx;
-    k.x2[base + xa] = Ra;
-    k.x2[base + xa + 1] = Rb;
+    const size_t base = xidx(k, g, lev, xa >> 1, c, k.Mc);
+    k.x2[base] = Ra;
+    k.x2[base + 1] = Rb;
   }
 }
 
@@ -273,12 +282,12 @@ __global__ void __launch_bounds__(256) k_h3(HK<C, CI> k, int CB) {
   const int c0 = blockIdx.x * CB;
   const int ncb = min(CB, k.Mc - c0);
   load_tables(k, tw_s, perm_s);
+  const int half = k.Nx / 2;
   for (int i = threadIdx.x; i < k.ng * ncb * k.Nx; i += blockDim.x) {
-    const int x = i % k.Nx;
-    const int rest = i / k.Nx;
-    const int cc = rest % ncb, g = rest / ncb;
-    seq[((size_t)g * CB + cc) * k.Nx + x] =
-        k.x2[(((size_t)g * k.levels + lev) * k.Mc + (c0 + cc)) * k.Nx + x];
+    const int par = i & 1, r2 = i >> 1;
+    const int cc = r2 % ncb, r3 = r2 / ncb;
+    const int pp = r3 % half, g = r3 / half;
+    seq[((size_t)g * CB + cc) * k.Nx + 2 * pp + par] = k.x2[xidx(k, g, lev, pp, c0 + cc, k.Mc) + par];
   }
   __syncthreads();
   fft_dif_fwd(seq, k.ng * CB, k.Nx, k.plan, tw_s);
@@ -344,17 +353,21 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
 
   const size_t tb = table_bytes<C>(d.Nx);
   const size_t budget = 200 * 1024;
-  int CB1 = (int)((96 * 1024) / ((size_t)k.nf1 * d.Nx * sizeof(C)));
+  // FP64: the FP64 pipe is the limit, large tiles amortise the tables; FP32:
+  // shared-memory latency is the limit, small tiles keep 4 CTAs per SM
+  const size_t tile = sizeof(T) == 8 ? 96 * 1024 : 44 * 1024;
+  const size_t budget2 = sizeof(T) == 8 ? budget : 52 * 1024;
+  int CB1 = (int)(tile / ((size_t)k.nf1 * d.Nx * sizeof(C)));
   CB1 = max(1, min(CB1, k.cols_in));
   size_t sm1 = tb + (size_t)k.nf1 * CB1 * d.Nx * sizeof(C);
   if (sm1 > budget) return cudaErrorInvalidConfiguration;
   int RB = 2;
   while (RB * 2 <= 16 && d.Nx % (RB * 2) == 0 &&
-         tb + (size_t)(k.nf1 + k.nprod) * RB * d.Nx * sizeof(C) <= budget)
+         tb + (size_t)(k.nf1 + k.nprod) * RB * d.Nx * sizeof(C) <= budget2)
     RB *= 2;
   size_t sm2 = tb + (size_t)(k.nf1 + k.nprod) * (RB / 2) * d.Nx * sizeof(C);
   if (sm2 > budget) return cudaErrorInvalidConfiguration;
-  int CB3 = (int)((96 * 1024) / ((size_t)k.ng * d.Nx * sizeof(C)));
+  int CB3 = (int)(tile / ((size_t)k.ng * d.Nx * sizeof(C)));
   CB3 = max(1, min(CB3, d.Mc));
   size_t sm3 = tb + (size_t)k.ng * CB3 * d.Nx * sizeof(C);
   if (sm3 > budget) return cudaErrorInvalidConfiguration;

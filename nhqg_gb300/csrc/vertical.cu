@@ -608,10 +608,18 @@ __global__ void k_zero_mode0(double2* f, int levels, int M) {
     f[(size_t)l * M] = czero();
 }
 
-inline size_t vsmem(const Params& p, int nbuf, bool dct = false) {
-  size_t e = (size_t)nbuf * p.d.P * TM;
-  if (dct) e += (size_t)col::dct_smem_elems(make_dct(p, Tables{}));
-  return e * sizeof(double2);
+// dynamic shared memory of a column kernel: nbuf FP64 tiles plus the DCT
+// work area in FP64 or (f32_dct) FP32
+inline size_t vsmem(const Params& p, int nbuf, bool dct = false, bool f32_dct = false) {
+  size_t b = (size_t)nbuf * p.d.P * TM * sizeof(double2);
+  if (dct) {
+    const col::Dct d = make_dct(p, Tables{});
+    if (f32_dct && d.fast)
+      b += (size_t)(TM + 1) * 2 * d.N * sizeof(float2) + (size_t)2 * d.N * sizeof(int);
+    else
+      b += (size_t)col::dct_smem_elems(d) * sizeof(double2);
+  }
+  return b;
 }
 inline int vgrid(const Params& p) { return (p.d.M + TM - 1) / TM; }
 
@@ -619,7 +627,7 @@ template <typename CO>
 cudaError_t vfwd_t(const Params& p, const Tables& t, const double2* q, const double2* w,
                    const double2* th, CO* qn, CO* wn, CO* tn, cudaStream_t st) {
   VK k = make_vk(p, t);
-  const size_t sm = vsmem(p, 2, true);
+  const size_t sm = vsmem(p, 2, true, sizeof(CO) == sizeof(float2));
   cudaFuncSetAttribute(k_vfwd<CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k_vfwd<CO><<<vgrid(p), NT, sm, st>>>(k, q, w, th, qn, wn, tn);
   return cudaGetLastError();
@@ -646,9 +654,9 @@ cudaError_t launch_vfwd_f32(const Params& p, const Tables& t, const double2* q, 
 
 cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st) {
   VK k = make_vk(p, t);
-  const size_t sm = vsmem(p, 5, true);
-  const int g = vgrid(p);
   const bool f32 = a.Aqf != nullptr;
+  const size_t sm = vsmem(p, 5, true, f32 && mode != VB_SOLVE);
+  const int g = vgrid(p);
   if (f32 && (!p.fast_dct || !t.tw_v_f || a.dtb_nodal || !a.Awf || !a.Atf))
     return cudaErrorInvalidValue;
   switch (mode) {
