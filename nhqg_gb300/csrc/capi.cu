@@ -426,6 +426,9 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   }
   if (dalloc(c, &w.vec, corrector_vec_doubles(P)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
   cudaMemset(w.vec, 0, corrector_vec_doubles(P) * sizeof(double));
+  if (dalloc(c, &w.partials, parseval_partials(P)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  if (dalloc(c, &w.counters, (size_t)P) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  if (cudaMemset(w.counters, 0, (size_t)P * sizeof(unsigned)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
   if (dalloc(c, &w.status, 4) != cudaSuccess) return fail(NHQG_ERR_CUDA);
   cudaMemset(w.status, 0, 4 * sizeof(int));
   {
@@ -610,7 +613,7 @@ int explicit_front(nhqg_ctx* c, const double2* q, const double2* w, const double
   c->launches += 1;
   if (legacy_mean) {
     // <w theta>_xy on the padded grid equals the Parseval sum of the band-limited fields
-    PCK("parseval", launch_parseval(p, c->Wn, c->Tn, p.d.P, c->flux, st));
+    PCK("parseval", launch_parseval(p, c->Wn, c->Tn, p.d.P, c->flux, c->w, st));
     PCK("mean_1d", launch_mean_legacy_rhs(p, c->t, tb, c->flux, c->dtb, Etb, Itb, st));
     c->launches += 2;
   }

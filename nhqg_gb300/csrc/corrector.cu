@@ -271,12 +271,16 @@ __device__ void d1_matvec(double* out, const double* D1, const double* x, int P)
   }
 }
 
+// The band is built and factored in shared memory: the factorisation is a
+// serial recurrence, and shared-memory operands keep each step at on-chip
+// latency.  Dynamic shared memory: 10 P doubles.
 __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt) {
   const CV cv{k.P};
   const int P = k.P;
+  extern __shared__ double band_sm[];
   double* w2 = vec + cv.w2();
-  double* A = vec + cv.Aband();
-  double* B = vec + cv.Bband();
+  double* A = band_sm;
+  double* B = band_sm + 5 * P;
   const double c1 = 0.5 * k.mu * k.kappa * sub_dt;
   const double c2 = 0.25 * k.mu * (sub_dt * sub_dt);
   for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) {
@@ -336,6 +340,11 @@ __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt)
       piv = n_piv; u1 = n_u1; u2 = n_u2;
     }
   }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) {
+    vec[cv.Aband() + idx] = A[idx];
+    vec[cv.Bband() + idx] = B[idx];
+  }
   // tb_sbp = c2s (V tbp)
   double* tmp = vec + cv.tmp();
   vec_dense(tmp, tbp, k.V, P, P, P);
@@ -343,17 +352,21 @@ __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt)
   vec_csr(vec + cv.tb_sbp(), tmp, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
 }
 
+// The LU band and the solution vector are staged in shared memory (6 P
+// doubles of dynamic shared memory) for the serial substitutions.
 __global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, double* tb_out) {
   const CV cv{k.P};
   const int P = k.P, N = k.N;
   __shared__ double red[64];
+  extern __shared__ double band_sm[];
   double* flux = vec + cv.flux();
   double* tbs = vec + cv.tb_sbp();
   double* gh = vec + cv.g_half();
-  double* rhs = vec + cv.tmp();
+  double* rhs = band_sm + 5 * P;
   double* t2 = vec + cv.tmp2();
-  const double* A = vec + cv.Aband();
+  double* A = band_sm;
   const double* B = vec + cv.Bband();
+  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) A[idx] = vec[cv.Aband() + idx];
   // rhs = B tb_sbp - mu sub_dt D1 flux
   band_matvec(rhs, B, tbs, P);
   d1_matvec(t2, k.D1, flux, P);
@@ -538,25 +551,25 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   k_corr_pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp);
   pf.end(st);
   pf.begin("parseval", st);
-  launch_parseval(p, a.wsbp, a.wsbp, p.d.P, w.vec + cv.w2(), st);
+  launch_parseval(p, a.wsbp, a.wsbp, p.d.P, w.vec + cv.w2(), w, st);
   pf.end(st);
   pf.begin("parseval", st);
-  launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), st);
+  launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st);
   pf.end(st);
   pf.begin("corr_init_1d", st);
-  k_corr_init<<<1, NT, 0, st>>>(k, w.vec, a.tbp, sub_dt);
+  k_corr_init<<<1, NT, 10 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, a.tbp, sub_dt);
   pf.end(st);
   int n = 4;
   for (int s = 0; s < nsub; ++s) {
     const int last = (s == nsub - 1);
     if (s > 0) {
       pf.begin("parseval", st);
-      launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), st);
+      launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st);
       pf.end(st);
       ++n;
     }
     pf.begin("corr_step_1d", st);
-    k_corr_tstep<<<1, NT, 0, st>>>(k, w.vec, sub_dt, last, a.tb_out);
+    k_corr_tstep<<<1, NT, 6 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, sub_dt, last, a.tb_out);
     pf.end(st);
     if (!last && fused_mid) {
       SubK sk{p.d.P, p.d.M, t.R_w, t.R_col, t.R_val, t.Fs, t.Us, w.vec + cv.g_half(), sub_dt};

@@ -169,7 +169,8 @@ struct Work {
   std::vector<double2*> f;
   // small vectors
   double* vec = nullptr;       // assorted 1-D vectors (see corrector.cu)
-  double* partials = nullptr;  // reductions
+  double* partials = nullptr;    // per-segment reduction sums [P * parseval segments]
+  unsigned* counters = nullptr;  // per-level arrival counters of the reductions [P], kept at 0
   int* status = nullptr;       // device status word
 };
 
@@ -234,7 +235,8 @@ cudaError_t launch_scatter(const Params& p, const double2* compact, double2* ful
 cudaError_t launch_finalize(const Params& p, const double2* q, const double2* w, const double2* th,
                             double2* qo, double2* wo, double2* to, cudaStream_t st);
 cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
-                            double* out, cudaStream_t st);
+                            double* out, Work& w, cudaStream_t st);
+size_t parseval_partials(int levels);
 cudaError_t launch_hermitian(const Params& p, double2* q, double2* w, double2* th, cudaStream_t st);
 cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStream_t st);
 

@@ -578,29 +578,53 @@ __global__ void k_hermitian(Dims d, double2* q, double2* w, double2* th) {
 }
 
 // mean over the Nx x Nx grid of irfft2(a) * irfft2(b), per level, by Parseval
+// Horizontal mean of a b* per level by Parseval: every mode of the half
+// plane counts twice except the ky = 0 column, which enters through its
+// Hermitian projection.  Each level is split into kParSeg segments, one CTA
+// each; the last CTA of a level to finish adds the segment sums in segment
+// order (deterministic) and resets the level's counter for the next launch.
+constexpr int kParSeg = 8;
 __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const double2* b,
-                                                 double* out, double scale) {
+                                                 double* out, double scale, double* partials,
+                                                 unsigned* counters) {
   __shared__ double scratch[32];
-  const int l = blockIdx.x;
+  __shared__ bool is_last;
+  const int l = blockIdx.y, seg = blockIdx.x;
   const double2* al = a + (size_t)l * d.M;
   const double2* bl = b + (size_t)l * d.M;
+  const int chunk = (d.M + kParSeg - 1) / kParSeg;
+  const int m0 = seg * chunk, m1 = min(d.M, m0 + chunk);
   double acc = 0.0;
-  for (int m = threadIdx.x; m < d.M; m += blockDim.x) {
-    const int r = m / d.Mc, c = m - r * d.Mc;
-    if (c != 0) {
-      const double2 x = al[m], y = bl[m];
-      acc += 2.0 * fma(x.x, y.x, x.y * y.y);
-    } else {
-      const int rm = mirror_row(r, d.K);
-      const double2 x = al[m], xm = al[rm * d.Mc];
-      const double2 y = bl[m], ym = bl[rm * d.Mc];
-      const double hx_re = 0.5 * (x.x + xm.x), hx_im = 0.5 * (x.y - xm.y);
-      const double hy_re = 0.5 * (y.x + ym.x), hy_im = 0.5 * (y.y - ym.y);
-      acc += fma(hx_re, hy_re, hx_im * hy_im);
-    }
+#pragma unroll 4
+  for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+    const double2 x = al[m], y = bl[m];
+    acc += 2.0 * fma(x.x, y.x, x.y * y.y);
+  }
+  // the ky = 0 column: replace the doubled term by the Hermitian projection
+  for (int r = threadIdx.x; r < d.Mr; r += blockDim.x) {
+    const int m = r * d.Mc;
+    if (m < m0 || m >= m1) continue;
+    const int rm = mirror_row(r, d.K);
+    const double2 x = al[m], xm = al[rm * d.Mc];
+    const double2 y = bl[m], ym = bl[rm * d.Mc];
+    const double hx_re = 0.5 * (x.x + xm.x), hx_im = 0.5 * (x.y - xm.y);
+    const double hy_re = 0.5 * (y.x + ym.x), hy_im = 0.5 * (y.y - ym.y);
+    acc += fma(hx_re, hy_re, hx_im * hy_im) - 2.0 * fma(x.x, y.x, x.y * y.y);
   }
   const double tot = block_sum(acc, scratch);
-  if (threadIdx.x == 0) out[l] = tot * scale;
+  if (threadIdx.x == 0) {
+    partials[(size_t)l * kParSeg + seg] = tot;
+    __threadfence();
+    is_last = atomicAdd(&counters[l], 1u) == kParSeg - 1;
+  }
+  __syncthreads();
+  if (is_last && threadIdx.x == 0) {
+    __threadfence();
+    double sum = 0.0;
+    for (int q = 0; q < kParSeg; ++q) sum += __ldcg(partials + (size_t)l * kParSeg + q);
+    out[l] = sum * scale;
+    counters[l] = 0u;
+  }
 }
 
 __global__ void k_zero_mode0(double2* f, int levels, int M) {
@@ -758,10 +782,13 @@ cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStrea
   return cudaGetLastError();
 }
 
+size_t parseval_partials(int levels) { return (size_t)levels * kParSeg; }
+
 cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
-                            double* out, cudaStream_t st) {
+                            double* out, Work& w, cudaStream_t st) {
   const double n2 = (double)p.d.Nx * (double)p.d.Nx;
-  k_parseval<<<levels, NT, 0, st>>>(p.d, a, b, out, 1.0 / (n2 * n2));
+  k_parseval<<<dim3(kParSeg, levels), NT, 0, st>>>(p.d, a, b, out, 1.0 / (n2 * n2), w.partials,
+                                                    w.counters);
   return cudaGetLastError();
 }
 
