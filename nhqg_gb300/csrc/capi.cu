@@ -146,8 +146,8 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   Params& p = c->p;
   p.d = make_dims(g->Nx, g->Nz);
   p.plan = plan;
-  p.plan_v = make_fft_plan(2 * g->Nz);
-  p.fast_dct = p.plan_v.npass > 0 && getenv("NHQG_DENSE_VERTICAL") == nullptr;
+  p.plan_v = make_fft_plan(g->Nz);
+  p.fast_dct = g->Nz % 2 == 0 && p.plan_v.npass > 0 && getenv("NHQG_DENSE_VERTICAL") == nullptr;
   p.advection = g->advection;
   p.closure = g->thermal_closure;
   p.exchange = g->exchange;
@@ -229,12 +229,14 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.perm, perm.data(), d.Nx);
   }
   if (p.fast_dct) {
-    const int L = 2 * d.Nz;
-    std::vector<double2> tw(L);
+    const int L = d.Nz;
+    std::vector<double2> tw(L), cs(L + 1);
     for (int k = 0; k < L; ++k) tw[k] = twiddle(k, L);
+    for (int j = 0; j <= L; ++j) cs[j] = twiddle(j, 2 * L);
     std::vector<int> perm(L);
     make_fft_perm(p.plan_v, perm.data());
     UP(t.tw_v, tw.data(), L);
+    UP(t.cs_v, cs.data(), L + 1);
     UP(t.perm_v, perm.data(), L);
   }
 
@@ -258,10 +260,12 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     std::vector<float2> twf = c32(tw);
     UP(t.tw_f, twf.data(), twf.size());
     if (p.fast_dct) {
-      std::vector<double2> twv(2 * (size_t)N);
-      for (int k = 0; k < 2 * N; ++k) twv[k] = twiddle(k, 2 * N);
-      std::vector<float2> twvf = c32(twv);
+      std::vector<double2> twv(N), csv(N + 1);
+      for (int k = 0; k < N; ++k) twv[k] = twiddle(k, N);
+      for (int j = 0; j <= N; ++j) csv[j] = twiddle(j, 2 * N);
+      std::vector<float2> twvf = c32(twv), csvf = c32(csv);
       UP(t.tw_v_f, twvf.data(), twvf.size());
+      UP(t.cs_v_f, csvf.data(), csvf.size());
     }
     if (p.has_sponge) {
       std::vector<float> v = f32(g->sponge_phys, (size_t)d.Nx * d.Nx);

@@ -1,13 +1,19 @@
-// Column-tile helpers shared by the vertical kernels (FP64).
+// Column-tile helpers shared by the vertical kernels.
 //
 // A CTA owns TM consecutive compact modes and holds their vertical columns in
 // shared memory as tiles [level][TM].  The Chebyshev <-> CGL transforms
-// V[j,n] = cos(pi j n / N) (nhqg/grid.py:192-201) run as a DCT-I through a
-// complex FFT of length 2N of the even extension:
-//   (V c)_j = ( DFT_2N(e)_j + c_0 + (-1)^j c_N ) / 2,  e = (c_0..c_N, c_{N-1}..c_1),
-// and V^-1 = (2/N) diag(1/w) V diag(1/w), w = (2, 1, .., 1, 2).  That is
-// ~5 (2N) log2(2N) flops per complex column instead of 4 (N+1)^2 for the
-// dense product; lengths whose 2N is not 2^a 3^b use the dense matrix.
+// V[j,n] = cos(pi j n / N) (nhqg/grid.py:192-201) run as a DCT-I through one
+// complex FFT of length N per complex column (N even, 2^a 3^b):
+//   z_j = (c_j + c_{N-j}) / 2 - sin(pi j / N) (c_j - c_{N-j}),   Z = FFT_N(z),
+//   (V c)_{2k}   = (Z_k + Z_{N-k}) / 2 + (c_0 + c_N) / 2,
+//   (V c)_{2k+1} = F_1 - sum_{m=1..k} D_m + (c_0 - c_N) / 2,
+//   D_m = -i (Z_m - Z_{N-m}) / 2,  F_1 = (c_0 - c_N) / 2 + sum_{j=1..N-1} c_j cos(pi j / N)
+// (the real-input DCT-I through a half-length FFT, Press et al., Numerical
+// Recipes, "cosft1", with the real and imaginary parts of the column carried
+// together: every step is real-linear), and V^-1 = (2/N) diag(1/w) V
+// diag(1/w), w = (2, 1, .., 1, 2).  That is ~5 N log2 N flops per complex
+// column instead of 4 (N+1)^2 for the dense product; other lengths use the
+// dense matrix.
 #pragma once
 #include "common.cuh"
 #include "fft.cuh"
@@ -21,16 +27,26 @@ constexpr int NT = 256;  // threads per CTA
 struct Dct {
   int N, P;
   bool fast;
-  FftPlan plan;               // length 2N
-  const double2* tw;          // [2N] global
-  const float2* tw_f;         // [2N] global, FP32 copy (mixed-precision path)
-  const int* perm;            // [2N] global
+  FftPlan plan;               // length N
+  const double2* tw;          // [N] FFT twiddles exp(-2 pi i k / N)
+  const float2* tw_f;         // [N] FP32 copy (mixed-precision path)
+  const double2* cs;          // [N+1] exp(-i pi j / N) = cos - i sin
+  const float2* cs_f;         // [N+1] FP32 copy
+  const int* perm;            // [N] position of frequency k in the FFT output
   const double *V, *Vinv;     // dense fallback [P*P]
 };
 
-// shared-memory words (double2) the DCT needs: work [TM][2N] + twiddles + perm
-__host__ __device__ inline int dct_smem_elems(const Dct& d) {
-  return d.fast ? (TM * 2 * d.N + 2 * d.N + (2 * d.N + 1) / 2) : 0;
+// shared memory of the fast DCT in units of the complex type C: work
+// [TM][N], FFT twiddles [N], cos/sin table [N+1], permutation [N] ints
+template <typename C>
+__host__ __device__ inline size_t dct_smem_bytes_t(const Dct& d) {
+  if (!d.fast) return 0;
+  const size_t n = (size_t)TM * d.N + d.N + d.N + 1;
+  const size_t c = (n * sizeof(C) + 15) / 16 * 16;
+  return c + ((size_t)d.N * sizeof(int) + 15) / 16 * 16;
+}
+__host__ __device__ inline size_t dct_smem_bytes(const Dct& d, bool f32 = false) {
+  return f32 ? dct_smem_bytes_t<float2>(d) : dct_smem_bytes_t<double2>(d);
 }
 
 __device__ __forceinline__ void tload(double2* b, const double2* __restrict__ src, int nlev,
@@ -223,6 +239,7 @@ template <typename C>
 struct DctSharedT {
   C* work;
   C* tw;
+  C* cs;
   int* perm;
 };
 using DctShared = DctSharedT<double2>;
@@ -231,18 +248,28 @@ template <typename C>
 __device__ __forceinline__ const C* dct_tw(const Dct& d);
 template <> __device__ __forceinline__ const double2* dct_tw<double2>(const Dct& d) { return d.tw; }
 template <> __device__ __forceinline__ const float2* dct_tw<float2>(const Dct& d) { return d.tw_f; }
+template <typename C>
+__device__ __forceinline__ const C* dct_cs(const Dct& d);
+template <> __device__ __forceinline__ const double2* dct_cs<double2>(const Dct& d) { return d.cs; }
+template <> __device__ __forceinline__ const float2* dct_cs<float2>(const Dct& d) { return d.cs_f; }
 
 template <typename C = double2>
 __device__ __forceinline__ DctSharedT<C> dct_shared(const Dct& d, void* base) {
   DctSharedT<C> s;
   s.work = reinterpret_cast<C*>(base);
-  s.tw = s.work + TM * 2 * d.N;
-  s.perm = reinterpret_cast<int*>(s.tw + 2 * d.N);
+  s.tw = s.work + TM * d.N;
+  s.cs = s.tw + d.N;
+  const size_t cbytes = ((size_t)(TM * d.N + d.N + d.N + 1) * sizeof(C) + 15) / 16 * 16;
+  s.perm = reinterpret_cast<int*>(reinterpret_cast<char*>(base) + cbytes);
   if (d.fast) {
     const C* tw = dct_tw<C>(d);
-    for (int i = threadIdx.x; i < 2 * d.N; i += blockDim.x) {
-      s.tw[i] = tw[i];
-      s.perm[i] = d.perm[i];
+    const C* cs = dct_cs<C>(d);
+    for (int i = threadIdx.x; i <= d.N; i += blockDim.x) {
+      if (i < d.N) {
+        s.tw[i] = tw[i];
+        s.perm[i] = d.perm[i];
+      }
+      s.cs[i] = cs[i];
     }
   }
   return s;
@@ -250,7 +277,8 @@ __device__ __forceinline__ DctSharedT<C> dct_shared(const Dct& d, void* base) {
 
 // out[0:nout] = V in (inverse == false) or V^-1 in (inverse == true), per column,
 // in the precision of C.  Caller syncs before (in ready) and after (out
-// ready).  out != in.  The FP32 instantiation requires d.fast.
+// ready).  out != in.  The FP32 instantiation requires d.fast.  Needs 2 TM
+// warps (the odd outputs are a prefix sum per (mode, re/im) column).
 template <typename C>
 __device__ __forceinline__ void tdct(C* out, const C* in, const Dct& d, const DctSharedT<C>& s,
                                      bool inverse, int nout) {
@@ -262,28 +290,77 @@ __device__ __forceinline__ void tdct(C* out, const C* in, const Dct& d, const Dc
       return;
     }
   }
-  const int L = 2 * N;
   const T half = T(0.5);
-  for (int idx = threadIdx.x; idx < TM * L; idx += blockDim.x) {
-    const int mm = idx / L, n = idx - mm * L;
-    const int src = n <= N ? n : L - n;
-    C v = in[src * TM + mm];
-    if (inverse && (src == 0 || src == N)) v = gscale(v, half);
-    s.work[idx] = v;
+  // input with the inverse's endpoint halving: c_n = in_n (x 1/2 at n = 0, N)
+  auto cin = [&](int n, int mm) {
+    C v = in[n * TM + mm];
+    if (inverse && (n == 0 || n == N)) v = gscale(v, half);
+    return v;
+  };
+  for (int idx = threadIdx.x; idx < TM * N; idx += blockDim.x) {
+    const int mm = idx / N, j = idx - mm * N;
+    const C cj = cin(j, mm), cr = cin(N - j, mm);
+    const T sn = -s.cs[j].y;  // sin(pi j / N)
+    const C sum = gadd(cj, cr), dif = gsub(cj, cr);
+    s.work[idx] = gmk<C>(fma(half, sum.x, -sn * dif.x), fma(half, sum.y, -sn * dif.y));
   }
   __syncthreads();
-  fft_dif_fwd(s.work, TM, L, d.plan, s.tw);
-  const T sc = inverse ? T(1.0 / N) : half;  // (2/N)/2 after the 1/2 of the DCT-I identity
-  for (int idx = threadIdx.x; idx < nout * TM; idx += blockDim.x) {
-    const int j = idx / TM, mm = idx - j * TM;
-    const C Y = s.work[mm * L + s.perm[j]];
-    C c0 = in[mm], cN = in[N * TM + mm];
-    if (inverse) { c0 = gscale(c0, half); cN = gscale(cN, half); }
-    C y = gadd(Y, c0);
-    y = (j & 1) ? gsub(y, cN) : gadd(y, cN);
+  fft_dif_fwd(s.work, TM, N, d.plan, s.tw);
+  const T sc = inverse ? T(2.0 / N) : T(1);
+  // even outputs j = 2k
+  for (int idx = threadIdx.x; idx < TM * (N / 2 + 1); idx += blockDim.x) {
+    const int k = idx / TM, mm = idx - k * TM;
+    const int j = 2 * k;
+    if (j >= nout) continue;
+    const C Zk = s.work[mm * N + s.perm[k % N]];
+    const C Zm = s.work[mm * N + s.perm[(N - k) % N]];
+    const C c0 = cin(0, mm), cN = cin(N, mm);
+    C y = gscale(gadd(gadd(Zk, Zm), gadd(c0, cN)), half);
     T f = sc;
     if (inverse && (j == 0 || j == N)) f *= half;
-    out[idx] = gscale(y, f);
+    out[j * TM + mm] = gscale(y, f);
+  }
+  // odd outputs j = 2k+1: one warp per (mode, re/im) column
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (w < 2 * TM) {
+    const int mm = w >> 1;
+    const bool im = w & 1;
+    auto part = [&](const C& v) { return im ? v.y : v.x; };
+    const T c0 = part(cin(0, mm)), cN = part(cin(N, mm));
+    // F_1 = (c_0 - c_N)/2 + sum_j c_j cos(pi j / N)
+    T f1 = T(0);
+    for (int j = 1 + lane; j < N; j += 32) f1 = fma(part(in[j * TM + mm]), s.cs[j].x, f1);
+    for (int o = 16; o > 0; o >>= 1) f1 += __shfl_xor_sync(0xffffffffu, f1, o);
+    f1 = fma(half, c0 - cN, f1);
+    // D_m (m = 1 .. N/2-1), re part = Im(Z_m - Z_{N-m})/2, im part = -Re(Z_m - Z_{N-m})/2
+    auto dm = [&](int m) {
+      const C a = s.work[mm * N + s.perm[m]], b = s.work[mm * N + s.perm[N - m]];
+      return im ? half * (b.x - a.x) : half * (a.y - b.y);
+    };
+    const int len = N / 2 - 1;
+    const int chunk = (len + 31) / 32;
+    const int m0 = 1 + lane * chunk, m1 = min(len + 1, m0 + chunk);
+    T run = T(0);
+    for (int m = m0; m < m1; ++m) run += dm(m);
+    T incl = run;
+    for (int o = 1; o < 32; o <<= 1) {
+      const T t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    T acc = incl - run;
+    const T tail = half * (c0 - cN);
+    auto put = [&](int k, T F) {
+      const int j = 2 * k + 1;
+      if (j < nout) {
+        const T v = (F + tail) * sc;
+        if (im) out[j * TM + mm].y = v; else out[j * TM + mm].x = v;
+      }
+    };
+    if (lane == 0) put(0, f1);
+    for (int m = m0; m < m1; ++m) {
+      acc += dm(m);
+      put(m, f1 - acc);
+    }
   }
 }
 

@@ -39,12 +39,8 @@ struct CV {
   __host__ __device__ int tmp2() const { return 5 * P; }
   __host__ __device__ int Aband() const { return 6 * P; }   // 5P: diag offsets -2..2
   __host__ __device__ int Bband() const { return 11 * P; }  // 5P
-  __host__ __device__ int dtb() const { return 16 * P; }    // legacy dTheta/dZ nodal
-  __host__ __device__ int Etb1() const { return 17 * P; }
-  __host__ __device__ int Etb2() const { return 18 * P; }
-  __host__ __device__ int Itb() const { return 19 * P; }
-  __host__ __device__ int fluxn() const { return 20 * P; }
-  __host__ __device__ int total() const { return 21 * P; }
+  __host__ __device__ int lu32() const { return 16 * P; }   // 3P doubles = 6P floats: FP32 LU band
+  __host__ __device__ int total() const { return 19 * P; }
 };
 
 struct CK {
@@ -91,6 +87,8 @@ __device__ __forceinline__ void tstencil(const CK& k, bool wbasis, double2* c, c
   }
 }
 // ------------------------------------------------------------ per-mode kernels
+// Predictor w and theta to nodal CGL values and to the SBP grid (FP64: the
+// mean exchange keeps FP64 in the mixed-precision path too).
 __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const double2* tp,
                                                  double2* wcgl, double2* wsbp, double2* tsbp) {
   extern __shared__ double2 sm[];
@@ -274,6 +272,14 @@ __device__ void d1_matvec(double* out, const double* D1, const double* x, int P)
 // The band is built and factored in shared memory: the factorisation is a
 // serial recurrence, and shared-memory operands keep each step at on-chip
 // latency.  Dynamic shared memory: 10 P doubles.
+// Builds the pentadiagonal corrector matrices A = I - h (boundary rows
+// identity) and B = I + h in FP64, and factors A in FP32 (LU without
+// pivoting: A is the identity plus an M-matrix-like term, diagonally
+// dominant, so the factors stay bounded).  The substitutions of
+// k_corr_tstep use the FP32 factors inside an FP64 iterative refinement: the
+// factorisation and the substitutions are serial recurrences, and on this
+// GPU a dependent FP64 operation costs about 14 times a dependent FP32 one
+// (a division about 90 times).  Dynamic shared memory: 10 P doubles.
 __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt) {
   const CV cv{k.P};
   const int P = k.P;
@@ -300,51 +306,52 @@ __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt)
     }
     A[idx] = a;
     B[idx] = b;
+    vec[cv.Aband() + idx] = a;
+    vec[cv.Bband() + idx] = b;
   }
   __syncthreads();
+  float* L = reinterpret_cast<float*>(band_sm + 5 * P);  // FP32 factors over the B copy
+  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) L[idx] = (float)A[idx];
+  __syncthreads();
   if (threadIdx.x == 0) {
-    // banded LU without pivoting (multipliers below the diagonal; the
-    // diagonal slot keeps 1/pivot for the substitutions).  Row i of the band
-    // is (a0, a1, a2, a3, a4) = A[i, i-2 .. i+2]; the running values of the
-    // two rows below the current pivot stay in registers.
-    double r1_0 = P > 1 ? A[1 * P + 1] : 0.0, r1_1 = P > 1 ? A[2 * P + 1] : 0.0;  // row col+1: cols col, col+1
-    double r1_2 = P > 1 ? A[3 * P + 1] : 0.0;                                     //            col+2
-    double piv = A[2 * P + 0], u1 = A[3 * P + 0], u2 = A[4 * P + 0];               // row col: diag, +1, +2
+    // banded LU: multipliers below the diagonal, 1/pivot in the diagonal
+    // slot.  Row i of the band is A[i, i-2 .. i+2]; the running values of
+    // the two rows below the current pivot stay in registers.
+    float r1_0 = P > 1 ? L[1 * P + 1] : 0.f, r1_1 = P > 1 ? L[2 * P + 1] : 0.f;
+    float r1_2 = P > 1 ? L[3 * P + 1] : 0.f;
+    float piv = L[2 * P + 0], u1 = L[3 * P + 0], u2 = L[4 * P + 0];
     for (int col = 0; col < P; ++col) {
-      const double rp = 1.0 / piv;
-      A[2 * P + col] = rp;
-      // row col+2 (enters now): cols col, col+1, col+2
-      double r2_0 = 0.0, r2_1 = 0.0, r2_2 = 0.0, r2_3 = 0.0;
+      const float rp = 1.0f / piv;
+      L[2 * P + col] = rp;
+      float r2_0 = 0.f, r2_1 = 0.f, r2_2 = 0.f, r2_3 = 0.f;
       if (col + 2 < P) {
-        r2_0 = A[0 * P + col + 2];
-        r2_1 = A[1 * P + col + 2];
-        r2_2 = A[2 * P + col + 2];
-        r2_3 = A[3 * P + col + 2];
+        r2_0 = L[0 * P + col + 2];
+        r2_1 = L[1 * P + col + 2];
+        r2_2 = L[2 * P + col + 2];
+        r2_3 = L[3 * P + col + 2];
       }
-      double n_piv = 0.0, n_u1 = 0.0, n_u2 = 0.0;
+      float n_piv = 0.f, n_u1 = 0.f, n_u2 = 0.f;
       if (col + 1 < P) {
-        const double l = r1_0 * rp;
-        A[1 * P + col + 1] = l;
-        n_piv = fma(-l, u1, r1_1);       // A[col+1, col+1]
-        n_u1 = fma(-l, u2, r1_2);        // A[col+1, col+2]
-        n_u2 = (col + 3 < P) ? A[4 * P + col + 1] : 0.0;  // A[col+1, col+3]
-        A[3 * P + col + 1] = n_u1;
+        const float l = r1_0 * rp;
+        L[1 * P + col + 1] = l;
+        n_piv = fmaf(-l, u1, r1_1);
+        n_u1 = fmaf(-l, u2, r1_2);
+        n_u2 = (col + 3 < P) ? L[4 * P + col + 1] : 0.f;
+        L[3 * P + col + 1] = n_u1;
       }
       if (col + 2 < P) {
-        const double l = r2_0 * rp;
-        A[0 * P + col + 2] = l;
-        r1_0 = fma(-l, u1, r2_1);        // A[col+2, col+1]
-        r1_1 = fma(-l, u2, r2_2);        // A[col+2, col+2]
-        r1_2 = r2_3;                     // A[col+2, col+3]
+        const float l = r2_0 * rp;
+        L[0 * P + col + 2] = l;
+        r1_0 = fmaf(-l, u1, r2_1);
+        r1_1 = fmaf(-l, u2, r2_2);
+        r1_2 = r2_3;
       }
       piv = n_piv; u1 = n_u1; u2 = n_u2;
     }
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) {
-    vec[cv.Aband() + idx] = A[idx];
-    vec[cv.Bband() + idx] = B[idx];
-  }
+  float* Lg = reinterpret_cast<float*>(vec + cv.lu32());
+  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) Lg[idx] = L[idx];
   // tb_sbp = c2s (V tbp)
   double* tmp = vec + cv.tmp();
   vec_dense(tmp, tbp, k.V, P, P, P);
@@ -352,8 +359,74 @@ __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt)
   vec_csr(vec + cv.tb_sbp(), tmp, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
 }
 
-// The LU band and the solution vector are staged in shared memory (6 P
-// doubles of dynamic shared memory) for the serial substitutions.
+// d = (LU)^-1 r with the FP32 factors: rf holds r in FP32 on entry and d on
+// exit.  Serial, thread 0; FP32 only, so each step costs FP32 latency.
+__device__ __forceinline__ void lu32_solve(const float* __restrict__ L, float* __restrict__ rf, int P) {
+  // operands are fetched 8 rows ahead of the dependent chain so that the
+  // shared-memory latency overlaps the FMAs
+  constexpr int U = 8;
+  float v1 = rf[0], v2 = 0.f;
+  int i = 1;
+  for (; i + U <= P; i += U) {
+    float a0[U], a1[U], r[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) { a0[q] = L[0 * P + i + q]; a1[q] = L[1 * P + i + q]; r[q] = rf[i + q]; }
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      float v = fmaf(-a1[q], v1, r[q]);
+      if (i + q >= 2) v = fmaf(-a0[q], v2, v);
+      rf[i + q] = v;
+      v2 = v1;
+      v1 = v;
+    }
+  }
+  for (; i < P; ++i) {
+    float v = fmaf(-L[1 * P + i], v1, rf[i]);
+    if (i >= 2) v = fmaf(-L[0 * P + i], v2, v);
+    rf[i] = v;
+    v2 = v1;
+    v1 = v;
+  }
+  float x1 = 0.f, x2 = 0.f;
+  int j = P - 1;
+  for (; j - U + 1 >= 0; j -= U) {
+    float d[U], u1[U], u2[U], r[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const int ii = j - q;
+      d[q] = L[2 * P + ii]; u1[q] = L[3 * P + ii]; u2[q] = L[4 * P + ii]; r[q] = rf[ii];
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const int ii = j - q;
+      float v = r[q];
+      if (ii + 1 < P) v = fmaf(-u1[q], x1, v);
+      if (ii + 2 < P) v = fmaf(-u2[q], x2, v);
+      v *= d[q];
+      rf[ii] = v;
+      x2 = x1;
+      x1 = v;
+    }
+  }
+  for (; j >= 0; --j) {
+    float v = rf[j];
+    if (j + 1 < P) v = fmaf(-L[3 * P + j], x1, v);
+    if (j + 2 < P) v = fmaf(-L[4 * P + j], x2, v);
+    v *= L[2 * P + j];
+    rf[j] = v;
+    x2 = x1;
+    x1 = v;
+  }
+}
+
+// Solves A tb_new = B tb_sbp - mu sub_dt D1 flux by FP64 iterative
+// refinement around the FP32 factors (Wilkinson's mixed-precision iterative
+// refinement): x_0 = (LU)^-1 b, x_{k+1} = x_k + (LU)^-1 (b - A x_k) with the
+// residual in FP64.  Each sweep divides the error by about
+// 1 / (cond(A) eps_32); kRefine sweeps reach FP64 round-off for the
+// corrector's well-conditioned A = I + (SPD-like) h.  Dynamic shared memory:
+// 5 P doubles (FP64 A band) + 3 P doubles (FP32 factors) + 3 P doubles.
+constexpr int kRefine = 2;
 __global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, double* tb_out) {
   const CV cv{k.P};
   const int P = k.P, N = k.N;
@@ -362,39 +435,52 @@ __global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, double*
   double* flux = vec + cv.flux();
   double* tbs = vec + cv.tb_sbp();
   double* gh = vec + cv.g_half();
-  double* rhs = band_sm + 5 * P;
+  double* A = band_sm;                                  // 5P FP64
+  float* L = reinterpret_cast<float*>(band_sm + 5 * P); // 5P FP32 (3P doubles)
+  double* b = band_sm + 8 * P;
+  double* rhs = band_sm + 9 * P;  // the solution
+  double* res = band_sm + 10 * P;
   double* t2 = vec + cv.tmp2();
-  double* A = band_sm;
   const double* B = vec + cv.Bband();
-  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) A[idx] = vec[cv.Aband() + idx];
-  // rhs = B tb_sbp - mu sub_dt D1 flux
-  band_matvec(rhs, B, tbs, P);
+  const float* Lg = reinterpret_cast<const float*>(vec + cv.lu32());
+  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) {
+    A[idx] = vec[cv.Aband() + idx];
+    L[idx] = Lg[idx];
+  }
+  // b = B tb_sbp - mu sub_dt D1 flux
+  band_matvec(b, B, tbs, P);
   d1_matvec(t2, k.D1, flux, P);
   __syncthreads();
   const double cf = k.mu * sub_dt;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) rhs[i] = (i == 0 || i == P - 1) ? 0.0 : fma(-cf, t2[i], rhs[i]);
-  __syncthreads();
-  if (threadIdx.x == 0) {  // forward / back substitution, the last two values in registers
-    double v1 = rhs[0], v2 = 0.0;  // v_{i-1}, v_{i-2}
-    for (int i = 1; i < P; ++i) {
-      double v = fma(-A[1 * P + i], v1, rhs[i]);
-      if (i >= 2) v = fma(-A[0 * P + i], v2, v);
-      rhs[i] = v;
-      v2 = v1;
-      v1 = v;
-    }
-    double x1 = 0.0, x2 = 0.0;  // x_{i+1}, x_{i+2}
-    for (int i = P - 1; i >= 0; --i) {
-      double v = rhs[i];
-      if (i + 1 < P) v = fma(-A[3 * P + i], x1, v);
-      if (i + 2 < P) v = fma(-A[4 * P + i], x2, v);
-      v *= A[2 * P + i];
-      rhs[i] = v;
-      x2 = x1;
-      x1 = v;
-    }
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    b[i] = (i == 0 || i == P - 1) ? 0.0 : fma(-cf, t2[i], b[i]);
+    res[i] = b[i];
+    rhs[i] = 0.0;
   }
-  __syncthreads();  // rhs = tb_new
+  __syncthreads();
+  float* rf = reinterpret_cast<float*>(res);  // FP32 view of the residual slot
+  for (int it = 0; it <= kRefine; ++it) {
+    double rv[4];
+    for (int q = 0, i = threadIdx.x; i < P; i += blockDim.x, ++q) rv[q] = res[i];
+    __syncthreads();
+    for (int q = 0, i = threadIdx.x; i < P; i += blockDim.x, ++q) rf[i] = (float)rv[q];
+    __syncthreads();
+    if (threadIdx.x == 0) lu32_solve(L, rf, P);
+    __syncthreads();
+    for (int i = threadIdx.x; i < P; i += blockDim.x) rhs[i] += (double)rf[i];
+    __syncthreads();
+    if (it == kRefine) break;
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {  // res = b - A x in FP64
+      double acc = b[i];
+      for (int d = 0; d < 5; ++d) {
+        const int j = i + d - 2;
+        if (j >= 0 && j < P) acc = fma(-A[d * P + i], rhs[j], acc);
+      }
+      res[i] = acc;
+    }
+    __syncthreads();
+  }
+  // rhs = tb_new
   for (int i = threadIdx.x; i < P; i += blockDim.x) t2[i] = tbs[i] + rhs[i];
   __syncthreads();
   d1_matvec(gh, k.D1, t2, P);
@@ -537,7 +623,7 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   const int nsub = p.substeps > 0 ? p.substeps : 1;
   const double sub_dt = a.total_dt / nsub;
   const int grid = (p.d.M + TM - 1) / TM;
-  const size_t dsm = (size_t)col::dct_smem_elems(k.dct) * sizeof(double2);
+  const size_t dsm = col::dct_smem_bytes(k.dct);
   const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2) + dsm;
   const size_t sm4 = 4 * (size_t)p.d.P * TM * sizeof(double2) + dsm;
   cudaFuncSetAttribute(k_corr_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
@@ -569,7 +655,7 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
       ++n;
     }
     pf.begin("corr_step_1d", st);
-    k_corr_tstep<<<1, NT, 6 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, sub_dt, last, a.tb_out);
+    k_corr_tstep<<<1, NT, 11 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, sub_dt, last, a.tb_out);
     pf.end(st);
     if (!last && fused_mid) {
       SubK sk{p.d.P, p.d.M, t.R_w, t.R_col, t.R_val, t.Fs, t.Us, w.vec + cv.g_half(), sub_dt};

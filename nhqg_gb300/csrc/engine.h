@@ -29,10 +29,11 @@ struct Tables {
   int* perm = nullptr;    // [Nx]
   // FP32 copies for the mixed-precision path (kx_f [Nx], ky_f [Nk] full layout)
   float *kx_f = nullptr, *ky_f = nullptr, *sponge_f = nullptr, *eta_phys_f = nullptr;
-  float2 *eta_f = nullptr, *tw_f = nullptr, *tw_v_f = nullptr;
-  // FFT over 2*Nz (DCT-I of the vertical columns)
-  double2* tw_v = nullptr;  // [2Nz]
-  int* perm_v = nullptr;    // [2Nz]
+  float2 *eta_f = nullptr, *tw_f = nullptr, *tw_v_f = nullptr, *cs_v_f = nullptr;
+  // FFT over Nz (DCT-I of the vertical columns)
+  double2* tw_v = nullptr;  // [Nz]   exp(-2 pi i k / Nz)
+  double2* cs_v = nullptr;  // [Nz+1] exp(-i pi j / Nz)
+  int* perm_v = nullptr;    // [Nz]
   // vertical operators
   double *V = nullptr, *Vinv = nullptr;        // [P*P]
   double *wst_a = nullptr, *wst_b = nullptr;   // mixed w stencil a_n, b_n [G]; null = Dirichlet
@@ -71,7 +72,7 @@ struct Tables {
 struct Params {
   Dims d;
   FftPlan plan;
-  FftPlan plan_v;  // length 2*Nz; npass <= 0 -> dense vertical transforms
+  FftPlan plan_v;  // length Nz (DCT-I); npass <= 0 -> dense vertical transforms
   bool fast_dct;
   int advection, closure, exchange, wbc, substeps;
   double dt, gamma_imex, Ra_sigma, sigma, beta, eps_sq;
@@ -90,6 +91,8 @@ inline col::Dct make_dct(const Params& p, const Tables& t) {
   d.plan = p.plan_v;
   d.tw = t.tw_v;
   d.tw_f = t.tw_v_f;
+  d.cs = t.cs_v;
+  d.cs_f = t.cs_v_f;
   d.perm = t.perm_v;
   d.V = t.V;
   d.Vinv = t.Vinv;
@@ -211,7 +214,7 @@ cudaError_t launch_vfwd_f32(const Params& p, const Tables& t, const double2* q, 
 cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st);
 // FP64 nodal fields (the corrector's w and theta) -> FP32, P*M elements each
 cudaError_t launch_to_f32(const Params& p, const double2* a, const double2* b, float2* fa,
-                          float2* fb, cudaStream_t st);
+                          float2* fb, cudaStream_t st);  // a/fa may be null
 // O(N) tau solve of the per-shell w system (the mixed-precision path's
 // replacement for the dense shell inverses)
 cudaError_t launch_tau_solve(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,

@@ -636,13 +636,7 @@ __global__ void k_zero_mode0(double2* f, int levels, int M) {
 // work area in FP64 or (f32_dct) FP32
 inline size_t vsmem(const Params& p, int nbuf, bool dct = false, bool f32_dct = false) {
   size_t b = (size_t)nbuf * p.d.P * TM * sizeof(double2);
-  if (dct) {
-    const col::Dct d = make_dct(p, Tables{});
-    if (f32_dct && d.fast)
-      b += (size_t)(TM + 1) * 2 * d.N * sizeof(float2) + (size_t)2 * d.N * sizeof(int);
-    else
-      b += (size_t)col::dct_smem_elems(d) * sizeof(double2);
-  }
+  if (dct) b += col::dct_smem_bytes(make_dct(p, Tables{}), f32_dct);
   return b;
 }
 inline int vgrid(const Params& p) { return (p.d.M + TM - 1) / TM; }
@@ -706,8 +700,11 @@ __global__ void k_to_f32(const double2* __restrict__ a, const double2* __restric
                          float2* __restrict__ fa, float2* __restrict__ fb, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const double2 x = a[i], y = b[i];
-    fa[i] = make_float2((float)x.x, (float)x.y);
+    if (a) {
+      const double2 x = a[i];
+      fa[i] = make_float2((float)x.x, (float)x.y);
+    }
+    const double2 y = b[i];
     fb[i] = make_float2((float)y.x, (float)y.y);
   }
 }
