@@ -6,8 +6,8 @@ Workload (the headline configuration): Nx=Ny=256, Nz=256, L = 10 L_c
 advection, 2/3-rule dealiasing, evolve_mean closure with the balanced SBP2
 predictor/corrector (4 substeps), ARS(2,2,2).  Input: the seeded theta'
 start (1e-3 N(0,1) sin(pi Z), PCG64 seed 0) -- synthetic -- spun up by
---spinup plain FP64 steps (100 by default; the precision study's 5000-step
-spin-up is available with --spinup 5000, about 4 minutes).  The step's work
+--spinup plain FP64 steps (1000 by default, about 40 s; the precision
+study's 5000-step spin-up is --spinup 5000, about 3 minutes).  The step's work
 does not depend on the state.  Every step streams several GB, far above the
 129 MB L2, so no explicit L2 flush is needed between steps.
 
@@ -301,27 +301,32 @@ def _rel(a, b) -> float:
 
 
 def _timed_arm(S, grid, eng, state, precision, args, ws):
-    """Warm up, then CUDA-event time exactly args.steps single-step calls
-    bracketed by barrier + synchronize; per-kernel profile of the same steps."""
+    """Warm up, then CUDA-event time exactly args.steps steps (one
+    step_inplace call, the way run() advances a state) bracketed by barrier +
+    synchronize; the NVTX range '<precision>_steps' marks them for profilers.
+    Then the same number of steps again with the engine's per-kernel event
+    profiler on, for the kernel shares."""
     import torch
     S.step_inplace(state, grid, max(3, args.warmup), check=True, precision=precision)
     torch.cuda.synchronize()
     barrier(ws)
     torch.cuda.synchronize()
-    eng.profile(True)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push(f"{precision}_steps")
     e0.record()
-    for _ in range(args.steps):
-        S.step_inplace(state, grid, 1, precision=precision)
+    S.step_inplace(state, grid, args.steps, precision=precision)  # one call, as run() drives it
     e1.record()
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     barrier(ws)
     ms = e0.elapsed_time(e1)
-    prof = eng.profile_report()
-    eng.profile(False)
     if eng.device_status() != 0:
         raise RuntimeError(f"device status set during the timed {precision} steps")
+    eng.profile(True)
+    S.step_inplace(state, grid, args.steps, precision=precision)
+    prof = eng.profile_report()
+    eng.profile(False)
     return allmax(ms, ws), prof
 
 
@@ -377,6 +382,11 @@ def run_ours(args, ws, rank, local):
     S.step_inplace(ref, grid, args.err_steps - 1, check=True)
     S.step_inplace(mix, grid, args.err_steps - 1, check=True, precision="mixed")
     errN = {n: _rel(a, b) for n, a, b in zip(names, mix, ref)}
+    from nhqg_gb300.diagnostics import compute_diagnostics
+    d_ref, d_mix = compute_diagnostics(ref, grid), compute_diagnostics(mix, grid)
+    diag_cmp = {k: {"plain": d_ref[k], "mixed": d_mix[k],
+                    "rel_diff": abs(d_mix[k] - d_ref[k]) / abs(d_ref[k]) if d_ref[k] else abs(d_mix[k])}
+                for k in ("Nusselt", "Nusselt_dealiased", "KE_tot", "KE_bt", "w_rms", "th_rms")}
     del ref, mix
 
     clocks = ClockSampler(local)
@@ -440,6 +450,7 @@ def run_ours(args, ws, rank, local):
         "data": (f"synthetic: seeded theta' 1e-3 N(0,1) sin(pi Z) (PCG64 seed 0), spun up by "
                  f"{args.spinup} plain FP64 steps"),
         "config": {"workload": workload_name(args.nx, args.nz), "path": "mixed", "Nx": args.nx, "Nz": args.nz,
+                   "timed": "one step_inplace call of `steps` steps on a device-resident state",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "state and per-step traffic >> 129 MB L2; no flush needed"},
         "plain_fp64": {"value": round(value_plain, 4), "unit": "steps/s",
@@ -447,7 +458,8 @@ def run_ours(args, ws, rank, local):
                        "kernels": shares(prof_plain), "roofline": roof_plain},
         "mixed_over_plain": round(value / value_plain, 3),
         "rel_err_vs_plain": {"after_1_step": err1, "increment_1_step": inc1,
-                             f"after_{args.err_steps}_steps": errN},
+                             f"after_{args.err_steps}_steps": errN,
+                             f"diagnostics_after_{args.err_steps}_steps": diag_cmp},
         "simulated_time_per_wall_hour": round(3600.0 * cfgd["dt"] * value / ws, 6),
         "gpu_launches": sum(n for n, _ in prof_mixed.values()),
         "roofline": dom,
@@ -496,9 +508,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--nz", type=int, default=256)
-    ap.add_argument("--spinup", type=int, default=100,
-                    help="plain FP64 steps from the seeded start before measuring")
-    ap.add_argument("--err-steps", type=int, default=100,
+    ap.add_argument("--spinup", type=int, default=1000,
+                    help="plain FP64 steps from the seeded start before measuring "
+                         "(the precision study's configuration uses 5000)")
+    ap.add_argument("--err-steps", type=int, default=500,
                     help="steps of the mixed-vs-plain accuracy comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -85,6 +85,9 @@ typedef struct nhqg_grid_desc {
                                                   shell's rounded |k|^2
                                                   (nhqg/grid.py:398-430); NULL
                                                   disables NHQG_PRECISION_MIXED */
+  const double *cc_weights;                    /* (P,) Clenshaw-Curtis weights on
+                                                  [0,1]; NULL disables
+                                                  nhqg_diagnostics */
 } nhqg_grid_desc;
 
 typedef struct nhqg_ctx nhqg_ctx;
@@ -187,6 +190,20 @@ int nhqg_sanitize(nhqg_ctx *ctx, nhqg_state *state, void *stream);
  * device) into out. */
 int nhqg_mean_temp_solve(nhqg_ctx *ctx, const double *R_th_bar, double *out,
                          int thermal_closure, void *stream);
+
+/* Scalar diagnostics of a state: the depth-integrated energies, rms values
+ * and Nusselt numbers of compute_diagnostics (nhqg/diagnostics.py:597-690;
+ * its spectra and budgets are not computed).  out: NHQG_DIAG_COUNT doubles
+ * in DEVICE memory, written stream-ordered in the NHQG_DIAG_* order.  The
+ * dealiased heat flux follows the mean equation's path (SBP grid for the
+ * balanced SBP2 exchange).  Needs cc_weights in the descriptor. */
+enum {
+  NHQG_DIAG_KE_BT = 0, NHQG_DIAG_KE_BC, NHQG_DIAG_KE_TOT, NHQG_DIAG_ENSTROPHY,
+  NHQG_DIAG_NUSSELT, NHQG_DIAG_NUSSELT_DEALIASED, NHQG_DIAG_VOL_AVG_TW,
+  NHQG_DIAG_VOL_AVG_TW_DEALIASED, NHQG_DIAG_Q_RMS, NHQG_DIAG_W_RMS, NHQG_DIAG_TH_RMS,
+  NHQG_DIAG_TH_BAR_MAX, NHQG_DIAG_COUNT
+};
+int nhqg_diagnostics(nhqg_ctx *ctx, const nhqg_state *state, double *out, void *stream);
 
 /* Latched device-side status of the last calls (after a stream sync);
  * reset = 1 clears it. */

@@ -19,4 +19,7 @@ def __getattr__(name):
     if name in ("State", "imex_step", "run", "step_inplace", "sanitize_state", "to_device", "to_host"):
         from . import solver
         return getattr(solver, name)
+    if name == "compute_diagnostics":
+        from . import diagnostics
+        return diagnostics.compute_diagnostics
     raise AttributeError(name)

@@ -21,7 +21,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libnhqg_gpu.so"
-SOURCES = ("horizontal.cu", "vertical.cu", "corrector.cu", "capi.cu", "noalloc.cu", "tau_solve.cu")
+SOURCES = ("horizontal.cu", "vertical.cu", "corrector.cu", "capi.cu", "noalloc.cu", "tau_solve.cu",
+           "diag.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
 
@@ -38,6 +39,8 @@ CLOSURE = {"fixed_conduction": 0, "evolve_mean": 1}
 EXCHANGE = {"legacy": 0, "balanced_sbp2": 1, "balanced_sbp2_pc": 2}
 WBC = {"dirichlet": 0, "neumann": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
+DIAG_KEYS = ("KE_bt", "KE_bc", "KE_tot", "enstrophy", "Nusselt", "Nusselt_dealiased",
+             "vol_avg_tw", "vol_avg_tw_dealiased", "q_rms", "w_rms", "th_rms", "th_bar_max")
 
 
 class NativeError(RuntimeError):
@@ -109,7 +112,7 @@ class GridDesc(ctypes.Structure):
         ("V", c_double_p), ("V_inv", c_double_p), ("w_stencil", c_double_p), ("G_Z", c_double_p),
         ("proj_dirichlet", c_double_p), ("sbp_D1", c_double_p), ("sbp_L", c_double_p),
         ("cgl_to_sbp", c_double_p), ("sbp_to_cgl", c_double_p), ("mean_solve", c_double_p),
-        ("shell_coef", c_double_p),
+        ("shell_coef", c_double_p), ("cc_weights", c_double_p),
     ]
 
 
@@ -145,6 +148,8 @@ SIGNATURES = {
     "nhqg_last_launch_count": (ctypes.c_int, [ctypes.c_void_p]),
     "nhqg_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nhqg_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "nhqg_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(StateDesc), ctypes.c_void_p,
+                                        ctypes.c_void_p]),
     "nhqg_profile_report": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "nhqg_version": (ctypes.c_char_p, []),
 }

@@ -28,6 +28,7 @@ struct nhqg_ctx {
   double *tb0, *tb1p, *tb1, *tb2p, *tb2, *E1tb, *E2tb, *Itb, *flux, *dtb;
   // mixed-precision path: FP32 nodal inputs and outputs of the horizontal
   // products, allocated by the first nhqg_set_precision(NHQG_PRECISION_MIXED)
+  double* diag_part = nullptr;  // diagnostics block partials
   int precision = NHQG_PRECISION_FP64;
   float2 *Qf = nullptr, *Wf = nullptr, *Tf = nullptr, *Aqf = nullptr, *Awf = nullptr, *Atf = nullptr;
 };
@@ -298,6 +299,11 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.GZ2, gz2.data(), (size_t)P * P);
   }
   if (g->mean_solve) UP(t.mean_solve, g->mean_solve, (size_t)P * P);
+  if (g->cc_weights) {
+    UP(t.cc, g->cc_weights, (size_t)P);
+    if (dalloc(c, &c->diag_part, (size_t)diag_blocks(p) * kDiagTerms) != cudaSuccess)
+      return fail(NHQG_ERR_CUDA);
+  }
   {
     CSR a = to_csr(g->cgl_to_sbp, P), b = to_csr(g->sbp_to_cgl, P);
     UP(t.c2s_ptr, a.ptr.data(), a.ptr.size()); UP(t.c2s_col, a.col.data(), a.col.size());
@@ -839,6 +845,28 @@ int nhqg_sbp2_corrector(nhqg_ctx* c, const nhqg_state* in, nhqg_state* out, doub
   ca.total_dt = total_dt;
   CK(run_corrector(c->p, c->t, c->w, ca, st, &c->launches));
   return scatter_fields(c, c->q0, c->w0, c->T1, c->tb1, out, st);
+}
+
+int nhqg_diagnostics(nhqg_ctx* c, const nhqg_state* s, double* out, void* stream) {
+  if (!c || !out) return NHQG_ERR_BAD_ARG;
+  if (!c->t.cc) return NHQG_ERR_UNSUPPORTED;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  int rc = gather_state(c, s, st);
+  if (rc) return rc;
+  const Params& p = c->p;
+  CK(launch_vfwd(p, c->t, c->q0, c->w0, c->t0, c->Qn, c->Wn, c->Tn, st));
+  CK(launch_diag_modes(p, c->t, c->Qn, c->Wn, c->Tn, c->diag_part, st));
+  const bool sbp = p.exchange == NHQG_EXCHANGE_BALANCED_SBP2 || p.exchange == NHQG_EXCHANGE_BALANCED_SBP2_PC;
+  if (sbp) {
+    CK(launch_corr_pre(p, c->t, c->w0, c->t0, c->Wcgl, c->Wsbp, c->Tsbp, st));
+    CK(launch_parseval(p, c->Wsbp, c->Tsbp, p.d.P, c->flux, c->w, st));
+  } else {
+    CK(launch_parseval(p, c->Wn, c->Tn, p.d.P, c->flux, c->w, st));
+  }
+  CK(launch_diag_final(p, c->t, c->diag_part, c->flux, sbp, c->tb0, out, st));
+  c->launches += sbp ? 5 : 4;
+  return NHQG_OK;
 }
 
 int nhqg_sanitize(nhqg_ctx* c, nhqg_state* s, void* stream) {

@@ -674,6 +674,15 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   return cudaGetLastError();
 }
 
+cudaError_t launch_corr_pre(const Params& p, const Tables& t, const double2* w, const double2* th,
+                            double2* wcgl, double2* wsbp, double2* tsbp, cudaStream_t st) {
+  CK k = make_ck(p, t);
+  const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2) + col::dct_smem_bytes(k.dct);
+  cudaFuncSetAttribute(k_corr_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  k_corr_pre<<<(p.d.M + TM - 1) / TM, NT, sm2, st>>>(k, w, th, wcgl, wsbp, tsbp);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mean_stage(const Params& p, const Tables& t, const MeanArgs& a, cudaStream_t st) {
   MK k;
   k.P = p.d.P; k.N = p.d.Nz;

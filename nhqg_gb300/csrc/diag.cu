@@ -1,0 +1,138 @@
+// Scalar diagnostics of a state (nhqg/diagnostics.py:597-690, the subset
+// without the shell spectra and budgets): Clenshaw-Curtis depth integrals of
+// |psi|^2, |q|^2, |w|^2, |theta|^2, Re(w theta*) and of the barotropic psi
+// per mode, weighted by the half-plane Parseval weights (1 at ky = 0, 2
+// elsewhere in the 2/3 band) and normalised by Nx^4.
+#include "engine.h"
+
+namespace nhqg {
+
+namespace {
+
+constexpr int kDiagThreads = 256;
+
+// one thread per compact mode, levels looped (level-major fields: coalesced)
+__global__ void __launch_bounds__(kDiagThreads) k_diag_modes(Dims d, const double* __restrict__ cc,
+                                                             const double* __restrict__ kx,
+                                                             const double* __restrict__ ky,
+                                                             const double* __restrict__ inv_denom,
+                                                             const double2* __restrict__ qn,
+                                                             const double2* __restrict__ wn,
+                                                             const double2* __restrict__ tn,
+                                                             double* __restrict__ partials) {
+  __shared__ double red[kDiagTerms][kDiagThreads / 32];
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[kDiagTerms] = {0, 0, 0, 0, 0, 0, 0};
+  if (m < d.M) {
+    const double idn = inv_denom[m];
+    double2 pbt = czero();
+    double spsi = 0.0, sq = 0.0, sw = 0.0, st = 0.0, swt = 0.0;
+    for (int j = 0; j < d.P; ++j) {
+      const double c = cc[j];
+      const size_t g = (size_t)j * d.M + m;
+      const double2 q = qn[g], w = wn[g], t = tn[g];
+      const double2 psi = cscale(q, -idn);
+      pbt = caxpy(c, psi, pbt);
+      spsi = fma(c, fma(psi.x, psi.x, psi.y * psi.y), spsi);
+      sq = fma(c, fma(q.x, q.x, q.y * q.y), sq);
+      sw = fma(c, fma(w.x, w.x, w.y * w.y), sw);
+      st = fma(c, fma(t.x, t.x, t.y * t.y), st);
+      swt = fma(c, fma(w.x, t.x, w.y * t.y), swt);
+    }
+    const int col = m % d.Mc;
+    const double wt = (col == 0) ? 1.0 : 2.0;
+    const double ksq = fma(kx[m], kx[m], ky[m] * ky[m]);
+    v[0] = 0.5 * wt * ksq * fma(pbt.x, pbt.x, pbt.y * pbt.y);  // KE_bt
+    v[1] = 0.5 * wt * ksq * spsi;                              // KE_tot
+    v[2] = wt * sq;
+    v[3] = wt * sw;
+    v[4] = wt * st;
+    v[5] = wt * swt;
+    v[6] = 0.0;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int k = 0; k < kDiagTerms; ++k) {
+    double x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) red[k][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < kDiagTerms) {
+    double x = 0.0;
+    for (int q = 0; q < kDiagThreads / 32; ++q) x += red[threadIdx.x][q];
+    partials[(size_t)blockIdx.x * kDiagTerms + threadIdx.x] = x;
+  }
+}
+
+// one CTA: sum the block partials in block order, the dealiased flux
+// (s2c flux on the SBP grid when flux_on_sbp) against the CC weights, and
+// max |th_bar|
+__global__ void k_diag_final(int nblocks, int P, double norm, const double* __restrict__ partials,
+                             const double* __restrict__ cc, const double* __restrict__ flux,
+                             const double* __restrict__ s2c, bool flux_on_sbp,
+                             const double* __restrict__ th_bar, double* __restrict__ out) {
+  __shared__ double tot[kDiagTerms];
+  __shared__ double red[32];
+  if (threadIdx.x < kDiagTerms) {
+    double x = 0.0;
+    for (int b = 0; b < nblocks; ++b) x += partials[(size_t)b * kDiagTerms + threadIdx.x];
+    tot[threadIdx.x] = x / norm;
+  }
+  // sum_j cc_j flux_cgl_j, flux_cgl = s2c flux (SBP) or flux
+  double acc = 0.0;
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    double f = flux[j];
+    if (flux_on_sbp) {
+      f = 0.0;
+      for (int i = 0; i < P; ++i) f = fma(s2c[(size_t)j * P + i], flux[i], f);
+    }
+    acc = fma(cc[j], f, acc);
+  }
+  const double voltw_d = block_sum(acc, red);
+  __syncthreads();
+  double mx = 0.0;
+  for (int j = threadIdx.x; j < P; j += blockDim.x) mx = fmax(mx, fabs(th_bar[j]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int q = 0; q < (int)(blockDim.x + 31) / 32; ++q) m = fmax(m, red[q]);
+    const double ke_bt = tot[0], ke_tot = tot[1], q2 = tot[2], w2 = tot[3], t2 = tot[4], wt = tot[5];
+    out[NHQG_DIAG_KE_BT] = ke_bt;
+    out[NHQG_DIAG_KE_BC] = ke_tot - ke_bt;
+    out[NHQG_DIAG_KE_TOT] = ke_tot;
+    out[NHQG_DIAG_ENSTROPHY] = 0.5 * q2;
+    out[NHQG_DIAG_NUSSELT] = 1.0 + wt;
+    out[NHQG_DIAG_NUSSELT_DEALIASED] = 1.0 + voltw_d;
+    out[NHQG_DIAG_VOL_AVG_TW] = wt;
+    out[NHQG_DIAG_VOL_AVG_TW_DEALIASED] = voltw_d;
+    out[NHQG_DIAG_Q_RMS] = sqrt(q2);
+    out[NHQG_DIAG_W_RMS] = sqrt(w2);
+    out[NHQG_DIAG_TH_RMS] = sqrt(t2);
+    out[NHQG_DIAG_TH_BAR_MAX] = m;
+  }
+}
+
+}  // namespace
+
+int diag_blocks(const Params& p) { return (p.d.M + kDiagThreads - 1) / kDiagThreads; }
+
+cudaError_t launch_diag_modes(const Params& p, const Tables& t, const double2* qn, const double2* wn,
+                              const double2* tn, double* partials, cudaStream_t st) {
+  if (!t.cc) return cudaErrorInvalidValue;
+  k_diag_modes<<<diag_blocks(p), kDiagThreads, 0, st>>>(p.d, t.cc, t.kx, t.ky, t.inv_denom, qn, wn,
+                                                        tn, partials);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_diag_final(const Params& p, const Tables& t, const double* partials,
+                              const double* flux, bool flux_on_sbp, const double* th_bar,
+                              double* out, cudaStream_t st) {
+  const double nx2 = (double)p.d.Nx * (double)p.d.Nx;
+  k_diag_final<<<1, 256, 0, st>>>(diag_blocks(p), p.d.P, nx2 * nx2, partials, t.cc, flux, t.s2c_d,
+                                  flux_on_sbp, th_bar, out);
+  return cudaGetLastError();
+}
+
+}  // namespace nhqg

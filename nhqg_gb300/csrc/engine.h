@@ -58,6 +58,8 @@ struct Tables {
   double* mean_solve = nullptr;  // [P*P] or null
   double* c2s_d = nullptr;  // [P*P] dense (1-D vectors)
   double* s2c_d = nullptr;  // [P*P]
+  // Clenshaw-Curtis weights [P] (diagnostics) or null
+  double* cc = nullptr;
   // shells
   double* shell_inv = nullptr;  // [n_shells*G*G]
   int* shell_start = nullptr;   // [n_shells+1]
@@ -268,5 +270,18 @@ struct CorrArgs {
 };
 cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrArgs& a,
                           cudaStream_t st, int* nlaunch);
+// w and theta (Galerkin) to nodal CGL (w only) and to the SBP grid
+cudaError_t launch_corr_pre(const Params& p, const Tables& t, const double2* w, const double2* th,
+                            double2* wcgl, double2* wsbp, double2* tsbp, cudaStream_t st);
+
+// diagnostics: per-block partial sums over modes of the depth integrals
+// (kDiagTerms doubles per block), then one CTA for the scalars
+constexpr int kDiagTerms = 7;
+int diag_blocks(const Params& p);
+cudaError_t launch_diag_modes(const Params& p, const Tables& t, const double2* qn, const double2* wn,
+                              const double2* tn, double* partials, cudaStream_t st);
+cudaError_t launch_diag_final(const Params& p, const Tables& t, const double* partials,
+                              const double* flux, bool flux_on_sbp, const double* th_bar,
+                              double* out, cudaStream_t st);
 
 }  // namespace nhqg

@@ -86,6 +86,7 @@ class Engine:
             d.mean_solve = arr("mean_solve", g.mean_solve)
         if getattr(g, "imex_shell_coef", None) is not None:
             d.shell_coef = arr("shell_coef", np.ravel(g.imex_shell_coef))
+        d.cc_weights = arr("cc_weights", g.cc_weights)
         self._desc = d
         handle = ctypes.c_void_p()
         nat.check(self.lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(handle)), "nhqg_ctx_create")
@@ -186,6 +187,14 @@ class Engine:
             self.handle, nat.ADV[advection], levels, psi.data_ptr(), q.data_ptr(), w.data_ptr(),
             th.data_ptr(), Aq.data_ptr(), Aw.data_ptr(), Ath.data_ptr(), _stream_handle()),
             "nhqg_triple_advection_23")
+
+    def diagnostics(self, q, w, th, tb) -> torch.Tensor:
+        """NHQG_DIAG_COUNT doubles on the device (order of _native.DIAG_KEYS)."""
+        s = self.state_desc(q, w, th, tb)
+        out = torch.empty(len(nat.DIAG_KEYS), dtype=torch.float64, device=q.device)
+        nat.check(self.lib.nhqg_diagnostics(self.handle, ctypes.byref(s), ctypes.c_void_p(out.data_ptr()),
+                                            _stream_handle()), "nhqg_diagnostics")
+        return out
 
     def sponge_product(self, f, out) -> None:
         nat.check(self.lib.nhqg_sponge_product_23(self.handle, int(f.shape[0]), f.data_ptr(),

@@ -30,4 +30,6 @@ from .nhqg_oracle import (  # noqa: F401
     triple_conservative_flux_divergence_23,
     triple_jacobian_23,
     sponge_product_23,
+    compute_diagnostics,
+    DIAG_KEYS,
 )

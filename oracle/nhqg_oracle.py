@@ -890,3 +890,53 @@ def theta_perturbation_state(grid: OracleGrid, seed: int = 0, amplitude: float =
     q = np.zeros((P, Nx, Nx // 2 + 1), dtype=np.complex128)
     w = np.zeros_like(th_gal)
     return sanitize_state(OracleState(q, w, th_gal, np.zeros(P)), grid)
+
+
+# ---------------------------------------------------------------------------
+# Scalar diagnostics -- nhqg/diagnostics.py:597-690 (the subset without the
+# shell spectra and budgets)
+# ---------------------------------------------------------------------------
+
+DIAG_KEYS = ("KE_bt", "KE_bc", "KE_tot", "enstrophy", "Nusselt", "Nusselt_dealiased",
+             "vol_avg_tw", "vol_avg_tw_dealiased", "q_rms", "w_rms", "th_rms", "th_bar_max")
+
+
+def compute_diagnostics(state: OracleState, grid: OracleGrid) -> dict:
+    """Depth-integrated (Clenshaw-Curtis) energies, rms values and Nusselt
+    numbers of ``state``.  Half-plane Parseval weights 1 at ky = 0 and the
+    Nyquist column, 2 elsewhere (nhqg/diagnostics.py:45-51), normalised by
+    Nx^4; the dealiased heat flux is the mean-equation's flux profile: on
+    the SBP grid mapped back to CGL for the balanced SBP2 exchange
+    (nhqg/diagnostics.py:232-248, nhqg/solver.py:370-374), on the CGL grid
+    otherwise (nhqg/diagnostics.py:272-281)."""
+    q, w, th, tb = state
+    Nx, Nk = grid.Nx, grid.Nk
+    cc = grid.cc_weights
+    psi_n = vmat(grid.V, invert_psi(q, grid.inv_denom))
+    q_n = vmat(grid.V, q)
+    w_n = vmat(grid.V, vmat(grid.w_stencil, w))
+    th_n = vmat(grid.V, vmat(grid.dirichlet_stencil, th))
+    wr = np.ones((Nx, Nk))
+    if Nk > 2:
+        wr[:, 1:Nk - 1] = 2.0
+    norm = float(Nx) ** 4
+    dint = lambda a: np.einsum("j,j...->...", cc, a)  # noqa: E731
+    psi_bt = dint(psi_n)
+    ksq = grid.ksq
+    KE_bt = 0.5 * np.sum(ksq * np.abs(psi_bt) ** 2 * wr) / norm
+    KE_tot = 0.5 * np.sum(ksq * dint(np.abs(psi_n) ** 2) * wr) / norm
+    q_sq = np.sum(dint(np.abs(q_n) ** 2) * wr) / norm
+    w_sq = np.sum(dint(np.abs(w_n) ** 2) * wr) / norm
+    th_sq = np.sum(dint(np.abs(th_n) ** 2) * wr) / norm
+    vol_tw = np.sum(dint(np.real(w_n * np.conj(th_n))) * wr) / norm
+    if grid.mean_exchange_discretization in ("balanced_sbp2", "balanced_sbp2_pc"):
+        c2s = grid.cgl_to_sbp
+        flux = grid.sbp_to_cgl @ horizontal_mean(vmat(c2s, w_n), vmat(c2s, th_n), Nx, grid.Npad)
+    else:
+        flux = horizontal_mean(w_n, th_n, Nx, grid.Npad)
+    vol_tw_d = float(np.sum(cc * flux))
+    out = dict(KE_bt=KE_bt, KE_bc=KE_tot - KE_bt, KE_tot=KE_tot, enstrophy=0.5 * q_sq,
+               Nusselt=1.0 + vol_tw, Nusselt_dealiased=1.0 + vol_tw_d, vol_avg_tw=vol_tw,
+               vol_avg_tw_dealiased=vol_tw_d, q_rms=np.sqrt(q_sq), w_rms=np.sqrt(w_sq),
+               th_rms=np.sqrt(th_sq), th_bar_max=float(np.max(np.abs(tb))))
+    return {k: float(v) for k, v in out.items()}

@@ -67,3 +67,10 @@ def state_from(arrays: dict, prefix: str):
 
 
 CASES = ("prod16", "fixed16", "jac16", "polar16", "radix24", "legacy16")
+
+
+def load_diagnostics() -> dict:
+    """Reference compute_diagnostics scalars: ``<case>.<state>`` -> values in
+    the order of ``keys`` (tests/golden/diagnostics.npz)."""
+    with np.load(GOLDEN_DIR / "diagnostics.npz") as z:
+        return {k: np.array(z[k]) for k in z.files}

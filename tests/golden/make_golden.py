@@ -4,6 +4,7 @@ Run in a checkout that has the reference mounted (it is NOT needed to run the
 tests)::
 
     python tests/golden/make_golden.py /path/to/NHQG
+    python tests/golden/make_golden.py /path/to/NHQG --diagnostics
 
 The reference (``nhqg/*.py``, unmodified, read-only) is imported under the
 NumPy stand-in for ``jax`` in ``tests/golden/refshim``.  Every case records
@@ -221,5 +222,44 @@ def main(ref_root: str) -> None:
     print(f"grid96: {(HERE / 'grid96.npz').stat().st_size / 1024:.0f} KiB")
 
 
+DIAG_KEYS = ("KE_bt", "KE_bc", "KE_tot", "enstrophy", "Nusselt", "Nusselt_dealiased",
+             "vol_avg_tw", "vol_avg_tw_dealiased", "q_rms", "w_rms", "th_rms", "th_bar_max")
+
+
+def diagnostics_main(ref_root: str) -> None:
+    """Reference ``compute_diagnostics`` (nhqg/diagnostics.py:597-690) scalars
+    at the ``r`` and ``s0`` states of every case -> ``diagnostics.npz``
+    (``<case>.<state>`` = values in ``DIAG_KEYS`` order)."""
+    sys.path.insert(0, str(HERE / "refshim"))
+    sys.path.insert(0, ref_root)
+    from nhqg import diagnostics, solver  # noqa: E402
+    from nhqg.config import NHQGConfig  # noqa: E402
+    from nhqg.grid import make_grid  # noqa: E402
+    import jax.numpy as jnp  # the stand-in  # noqa: E402
+
+    global jnp_asarray
+    jnp_asarray = jnp.asarray
+    out = {}
+    for name, over in CASES.items():
+        cfgd = dict(BASE)
+        cfgd.update(over)
+        override = cfgd.pop("_override_eta_sponge", False)
+        grid = make_grid(NHQGConfig(**cfgd))
+        if override:
+            eta_hat, sponge_phys = smooth_eta_sponge(grid)
+            grid = grid._replace(eta_hat=jnp.asarray(eta_hat), sponge_phys=jnp.asarray(sponge_phys))
+        for label, st in (("r", rich_state(grid, solver, seed=0)),
+                          ("s0", theta_init(grid, solver, seed=0))):
+            d = diagnostics.compute_diagnostics(st, grid)
+            out[f"{name}.{label}"] = np.array([float(np.asarray(d[k])) for k in DIAG_KEYS])
+    np.savez_compressed(HERE / "diagnostics.npz", keys=np.array(DIAG_KEYS), **out)
+    print(f"diagnostics: {len(out)} entries")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    if "--diagnostics" in sys.argv:
+        diagnostics_main(root)
+    else:
+        main(root)

@@ -94,3 +94,17 @@ def test_seeded_trajectory(case):
     for _ in range(meta["n_steps"]):
         s = oracle.imex_step(s, grid)
     assert_state_close(s, _state(arrays, "sN"), 1e-11, th_bar_abs=1e-16)
+
+
+@pytest.mark.parametrize("case", fixtures.CASES)
+def test_oracle_diagnostics_golden(case):
+    """Scalar diagnostics against the reference's compute_diagnostics
+    (tests/golden/diagnostics.npz, nhqg/diagnostics.py:597-690)."""
+    meta, arrays = fixtures.load_case(case)
+    grid = _grid(meta, arrays)
+    gd = fixtures.load_diagnostics()
+    for label in ("r", "s0"):
+        got = oracle.compute_diagnostics(_state(arrays, label), grid)
+        ref = gd[f"{case}.{label}"]
+        for i, key in enumerate(oracle.DIAG_KEYS):
+            assert abs(got[key] - ref[i]) <= 1e-12 * max(abs(ref[i]), 1e-300) + 1e-300, (case, label, key)
