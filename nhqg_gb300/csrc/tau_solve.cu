@@ -190,22 +190,56 @@ __global__ void __launch_bounds__(4 * kMB) k_tau_solve(TK k, const double2* __re
   __syncwarp();
   // Thomas forward and back substitution in the class, then the boundary-row
   // dot products of the particular solution y
+  // The per-shell tables are scattered L2 reads; each block of kPF rows is
+  // loaded into registers before its dependent chain runs, so the loads of a
+  // block overlap one another instead of each one stalling the chain.
   double b0 = 0.0, b1 = 0.0;
   if (!s_zero) {
+    constexpr int kPF = 8;
+    const int cnt = (N - 2 - p) / 2;  // rows n = p+2, p+4, .., last
+    const int last = p + 2 * cnt;
     double d = 0.0;
-    int last = p;
-    for (int n = p + 2; n <= N - 2; n += 2) {
-      d = fma(-Lrm[n], d, y[n] * rm[n]);
-      y[n] = d;
-      last = n;
+    for (int r0 = 0; r0 < cnt; r0 += kPF) {
+      double lr[kPF], rr[kPF], yy[kPF];
+#pragma unroll
+      for (int q = 0; q < kPF; ++q) {
+        const int n = p + 2 + 2 * (r0 + q);
+        const bool in = r0 + q < cnt;
+        lr[q] = in ? __ldg(Lrm + n) : 0.0;
+        rr[q] = in ? __ldg(rm + n) : 0.0;
+        yy[q] = in ? y[n] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < kPF; ++q) {
+        if (r0 + q < cnt) {
+          d = fma(-lr[q], d, yy[q] * rr[q]);
+          y[p + 2 + 2 * (r0 + q)] = d;
+        }
+      }
     }
     double nxt = 0.0;
-    for (int n = last; n >= p + 2; n -= 2) {
-      const double v = (n == last) ? y[n] : fma(-cp[n], nxt, y[n]);
-      y[n] = v;
-      nxt = v;
-      b0 = fma(uW1[n], v, b0);
-      b1 = fma(uW2[n], v, b1);
+    for (int r0 = cnt - 1; r0 >= 0; r0 -= kPF) {
+      double cc[kPF], yy[kPF], w1[kPF], w2[kPF];
+#pragma unroll
+      for (int q = 0; q < kPF; ++q) {
+        const int n = p + 2 + 2 * (r0 - q);
+        const bool in = r0 - q >= 0;
+        cc[q] = in ? __ldg(cp + n) : 0.0;
+        yy[q] = in ? y[n] : 0.0;
+        w1[q] = in ? __ldg(uW1 + n) : 0.0;
+        w2[q] = in ? __ldg(uW2 + n) : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < kPF; ++q) {
+        if (r0 - q >= 0) {
+          const int n = p + 2 + 2 * (r0 - q);
+          const double v = (n == last) ? yy[q] : fma(-cc[q], nxt, yy[q]);
+          y[n] = v;
+          nxt = v;
+          b0 = fma(w1[q], v, b0);
+          b1 = fma(w2[q], v, b1);
+        }
+      }
     }
   }
   b0 += __shfl_xor_sync(0xffffffffu, b0, 1);  // partner lane: same column, other parity
@@ -220,7 +254,7 @@ __global__ void __launch_bounds__(4 * kMB) k_tau_solve(TK k, const double2* __re
     // e = y + x z on the class (y_p = 0, z_p = 1), then c in place with a
     // sliding window over e_{n-2}, e_n, e_{n+2}
     y[p] = x;
-    for (int n = p + 2; n <= N - 2; n += 2) y[n] = fma(x, z[n], y[n]);
+    for (int n = p + 2; n <= N - 2; n += 2) y[n] = fma(x, __ldg(z + n), y[n]);
     double em2 = 0.0, e0 = y[p];
     for (int n = p; n <= N - 2; n += 2) {
       const double ep2 = (n + 2 <= N - 2) ? y[n + 2] : 0.0;
