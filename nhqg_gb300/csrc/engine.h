@@ -79,6 +79,10 @@ struct Params {
   int advection, closure, exchange, wbc, substeps;
   double dt, gamma_imex, Ra_sigma, sigma, beta, eps_sq;
   bool has_eta, has_sponge;
+  // horizontal-product tile budgets in KiB per precision [0] FP64, [1] FP32:
+  // column tiles of H1/H3 and the row tile of H2 (0 = built-in default);
+  // set by nhqg_autotune
+  int h_col_kib[2], h_row_kib[2];
 };
 
 }  // namespace nhqg

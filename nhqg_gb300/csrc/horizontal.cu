@@ -355,8 +355,9 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
   const size_t budget = 200 * 1024;
   // FP64: the FP64 pipe is the limit, large tiles amortise the tables; FP32:
   // shared-memory latency is the limit, small tiles keep 4 CTAs per SM
-  const size_t tile = sizeof(T) == 8 ? 96 * 1024 : 44 * 1024;
-  const size_t budget2 = sizeof(T) == 8 ? budget : 52 * 1024;
+  const int pi = sizeof(T) == 8 ? 0 : 1;
+  const size_t tile = (size_t)1024 * (p.h_col_kib[pi] > 0 ? p.h_col_kib[pi] : (pi == 0 ? 96 : 44));
+  const size_t budget2 = (size_t)1024 * (p.h_row_kib[pi] > 0 ? p.h_row_kib[pi] : (pi == 0 ? 200 : 52));
   int CB1 = (int)(tile / ((size_t)k.nf1 * d.Nx * sizeof(C)));
   CB1 = max(1, min(CB1, k.cols_in));
   size_t sm1 = tb + (size_t)k.nf1 * CB1 * d.Nx * sizeof(C);
