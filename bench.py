@@ -480,6 +480,95 @@ def run_ours(args, ws, rank, local):
     return line
 
 
+ENSEMBLE_CLASSES = ((64, 32), (96, 48), (128, 64))  # 16 members each
+
+
+def ensemble_configs(seed: int = 0):
+    """The batched-ensemble workload: 16 x 64^2x32, 16 x 96^2x48, 16 x 128^2x64,
+    L = 10 L_c, dt = 5e-5, Ra ~ U(40, 120) per member from default_rng(seed),
+    production recipe (evolve_mean + SBP2-PC, 4 substeps)."""
+    rng = np.random.default_rng(seed)
+    ras = rng.uniform(40.0, 120.0, 16 * len(ENSEMBLE_CLASSES))
+    out = []
+    for ci, (nx, nz) in enumerate(ENSEMBLE_CLASSES):
+        for j in range(16):
+            c = workload(nx, nz)
+            c.update(Ra_tilde=float(ras[16 * ci + j]), dt=5e-5)
+            out.append(c)
+    return out
+
+
+def run_ensemble(args, ws, rank):
+    """48 independent instances advanced by one CUDA graph per
+    `steps_per_launch` steps, against the same members stepped one after
+    another through the single-instance API."""
+    import torch
+    from nhqg_gb300 import NHQGConfig, make_grid, theta_perturbation_state
+    from nhqg_gb300 import solver as S
+    from nhqg_gb300.ensemble import Ensemble
+
+    t0 = time.perf_counter()
+    cfgs = ensemble_configs()
+    grids = [make_grid(NHQGConfig(**c)) for c in cfgs]
+    states = [S.to_device(theta_perturbation_state(g, seed=i)) for i, g in enumerate(grids)]
+    t_build = time.perf_counter() - t0
+    results = {}
+    for prec in ("fp64", "mixed"):
+        ens = Ensemble(grids, precision=prec, steps_per_launch=10, autotune=True)
+        for i, st in enumerate(states):
+            ens.load(i, st)
+        ens.step(max(3, args.warmup))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ens.step(args.steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        for i, eng in enumerate(ens.engines):
+            if eng.device_status() != 0:
+                raise RuntimeError(f"device status set for member {i}")
+        tiles = {f"{k[0]}^2x{k[1]} {k[2]}": v for k, v in ens.tiles.items()}
+        ens.close()
+        # the same members one after another, each through step_inplace on one stream
+        seq = [S.State(*(t.clone() for t in st)) for st in states]
+        for g, st in zip(grids, seq):
+            S.step_inplace(st, g, max(3, args.warmup), precision=prec)
+        torch.cuda.synchronize()
+        n_seq = max(1, args.steps // 10)
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record()
+        for g, st in zip(grids, seq):
+            S.step_inplace(st, g, n_seq, precision=prec)
+        s1.record()
+        torch.cuda.synchronize()
+        ms_seq = s0.elapsed_time(s1)
+        results[prec] = {
+            "instance_steps_per_s": round(len(grids) * args.steps / (ms * 1e-3), 2),
+            "ms_per_ensemble_step": round(ms / args.steps, 4),
+            "sequential_instance_steps_per_s": round(len(grids) * n_seq / (ms_seq * 1e-3), 2),
+            "batching_speedup": round((len(grids) * args.steps / ms) / (len(grids) * n_seq / ms_seq), 3),
+            "autotuned_tiles_kib": tiles,
+        }
+        del seq
+    if rank != 0:
+        return None
+    return {
+        "metric": "NHQG ensemble instance-steps/s: 48 instances (16 x 64^2x32, 16 x 96^2x48, "
+                  "16 x 128^2x64), one CUDA graph per 10 steps",
+        "value": results["mixed"]["instance_steps_per_s"], "unit": "instance-steps/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": max(3, args.warmup),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "mixed (value); fp64 in fp64", "data": "synthetic: seeded theta' per member (seed = index)",
+        "config": {"workload": "ensemble 16x64^2x32 + 16x96^2x48 + 16x128^2x64, L=10Lc, dt=5e-5, "
+                               "Ra~U(40,120) default_rng(0), evolve_mean SBP2-PC sub4",
+                   "members": len(grids)},
+        "fp64": results["fp64"], "mixed": results["mixed"], "grid_build_s": round(t_build, 1),
+    }
+
+
 def run_reference(args, ws, rank):
     """CPU arm: the oracle port of the reference step on the host cores, on
     this arm's workload, metric and units; rank 0 only."""
@@ -514,10 +603,14 @@ def main():
     ap.add_argument("--err-steps", type=int, default=500,
                     help="steps of the mixed-vs-plain accuracy comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ensemble", action="store_true",
+                    help="time the 48-member batched ensemble instead (its own JSON line)")
     args = ap.parse_args()
     ws, rank, local = dist_init()
     if args.impl == "reference":
         line = run_reference(args, ws, rank)
+    elif args.ensemble:
+        line = run_ensemble(args, ws, rank)
     else:
         line = run_ours(args, ws, rank, local)
     if rank == 0 and line is not None:

@@ -218,6 +218,35 @@ int nhqg_last_launch_count(const nhqg_ctx *ctx);
 int nhqg_profile_enable(nhqg_ctx *ctx, int on);
 int nhqg_profile_report(nhqg_ctx *ctx, char *buf, int buflen);
 
+/* ---- Tiles and autotuning (no reference counterpart) ----
+ * The horizontal-product kernels size their tiles from shared-memory budgets:
+ * tiles[0], tiles[1] = FP64 column / row budget in KiB, tiles[2], tiles[3] =
+ * the FP32 ones; 0 selects the built-in default.  nhqg_autotune times
+ * candidate budgets on the context's own buffers (both precisions once the
+ * mixed path is enabled) and keeps the fastest; it synchronises the stream. */
+int nhqg_get_tiles(const nhqg_ctx *ctx, int *tiles);
+int nhqg_set_tiles(nhqg_ctx *ctx, const int *tiles);
+int nhqg_autotune(nhqg_ctx *ctx, void *stream);
+
+/* ---- Batched ensemble (no reference counterpart) ----
+ * Independent contexts (any sizes, parameters and precisions) stepped
+ * together.  The steps of all members are captured once into a CUDA graph,
+ * each member on its own stream forked from and joined into the graph's
+ * origin, and one graph launch advances every member by steps_per_launch
+ * steps (a second, single-step graph takes the remainder).  A member keeps
+ * its state inside its context between calls: nhqg_batch_load copies a state
+ * in (the band check of nhqg_step applies), nhqg_batch_store copies it out.
+ * Changing a member's precision or tiles recaptures the graphs at the next
+ * nhqg_batch_step.  The contexts must outlive the batch and must not be
+ * stepped through other entry points while the batch is in use. */
+typedef struct nhqg_batch nhqg_batch;
+int nhqg_batch_create(nhqg_ctx *const *members, int n, int steps_per_launch, nhqg_batch **out);
+int nhqg_batch_destroy(nhqg_batch *batch);
+int nhqg_batch_load(nhqg_batch *batch, int member, const nhqg_state *state, void *stream);
+int nhqg_batch_store(nhqg_batch *batch, int member, nhqg_state *state, void *stream);
+int nhqg_batch_step(nhqg_batch *batch, int n_steps, void *stream);
+int nhqg_batch_size(const nhqg_batch *batch);
+
 /* Engine build identification string (static storage). */
 const char *nhqg_version(void);
 

@@ -150,6 +150,18 @@ SIGNATURES = {
     "nhqg_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nhqg_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(StateDesc), ctypes.c_void_p,
                                         ctypes.c_void_p]),
+    "nhqg_get_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "nhqg_set_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "nhqg_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "nhqg_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "nhqg_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "nhqg_batch_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(StateDesc),
+                                       ctypes.c_void_p]),
+    "nhqg_batch_store": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(StateDesc),
+                                        ctypes.c_void_p]),
+    "nhqg_batch_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "nhqg_batch_size": (ctypes.c_int, [ctypes.c_void_p]),
     "nhqg_profile_report": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "nhqg_version": (ctypes.c_char_p, []),
 }

@@ -26,11 +26,14 @@ struct nhqg_ctx {
   double2 *Q1, *W1, *T1p, *T1, *Q2, *W2, *T2p, *T2, *Wcgl, *Wsbp, *Tsbp, *Tcgl;
   // 1-D vectors [P]
   double *tb0, *tb1p, *tb1, *tb2p, *tb2, *E1tb, *E2tb, *Itb, *flux, *dtb;
+  double* diag_part = nullptr;  // diagnostics block partials
   // mixed-precision path: FP32 nodal inputs and outputs of the horizontal
   // products, allocated by the first nhqg_set_precision(NHQG_PRECISION_MIXED)
-  double* diag_part = nullptr;  // diagnostics block partials
   int precision = NHQG_PRECISION_FP64;
   float2 *Qf = nullptr, *Wf = nullptr, *Tf = nullptr, *Aqf = nullptr, *Awf = nullptr, *Atf = nullptr;
+  // bumped whenever the launch sequence of a step changes (precision, tiles):
+  // captured step graphs of a batch compare it
+  unsigned version = 0;
 };
 
 namespace {
@@ -516,6 +519,7 @@ int nhqg_profile_report(nhqg_ctx* c, char* buf, int buflen) {
 int nhqg_set_precision(nhqg_ctx* c, int precision) {
   if (!c) return NHQG_ERR_BAD_ARG;
   if (precision == NHQG_PRECISION_FP64) {
+    if (c->precision != precision) ++c->version;
     c->precision = precision;
     return NHQG_OK;
   }
@@ -532,6 +536,7 @@ int nhqg_set_precision(nhqg_ctx* c, int precision) {
       if (cudaMemset(*b, 0, fe * sizeof(float2)) != cudaSuccess) return NHQG_ERR_CUDA;
     }
   }
+  if (c->precision != precision) ++c->version;
   c->precision = precision;
   return NHQG_OK;
 }
@@ -946,5 +951,215 @@ int nhqg_sponge_product_23(nhqg_ctx* c, int levels, const void* f, void* out, vo
   }
   return NHQG_OK;
 }
+
+}  // extern "C"
+
+// ============================================================== batches and tiles
+struct nhqg_batch {
+  std::vector<nhqg_ctx*> members;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaStream_t origin = nullptr;
+  cudaEvent_t fork = nullptr;
+  int spl = 1;  // steps per graph launch
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    int steps = 0;
+    std::vector<unsigned> versions;
+  } g_many, g_one;
+};
+
+namespace {
+
+void drop_graph(nhqg_batch::Graph& g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  g.exec = nullptr;
+  g.versions.clear();
+}
+
+bool graph_current(const nhqg_batch* b, const nhqg_batch::Graph& g) {
+  if (!g.exec || g.versions.size() != b->members.size()) return false;
+  for (size_t i = 0; i < b->members.size(); ++i)
+    if (g.versions[i] != b->members[i]->version) return false;
+  return true;
+}
+
+// Capture `steps` steps of every member, each on its own stream forked from
+// and joined into the origin stream, into one executable graph.
+int capture(nhqg_batch* b, nhqg_batch::Graph& g, int steps) {
+  drop_graph(g);
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed));
+  int rc = NHQG_OK;
+  if (cudaEventRecord(b->fork, b->origin) != cudaSuccess) rc = NHQG_ERR_CUDA;
+  for (size_t i = 0; i < b->members.size() && rc == NHQG_OK; ++i) {
+    nhqg_ctx* c = b->members[i];
+    cudaStream_t st = b->streams[i];
+    const bool prof = c->w.prof.on;
+    c->w.prof.on = false;  // no event records inside a graph
+    if (cudaStreamWaitEvent(st, b->fork, 0) != cudaSuccess) rc = NHQG_ERR_CUDA;
+    for (int k = 0; k < steps && rc == NHQG_OK; ++k) rc = one_step(c, st);
+    if (rc == NHQG_OK && cudaEventRecord(b->joins[i], st) != cudaSuccess) rc = NHQG_ERR_CUDA;
+    if (rc == NHQG_OK && cudaStreamWaitEvent(b->origin, b->joins[i], 0) != cudaSuccess) rc = NHQG_ERR_CUDA;
+    c->w.prof.on = prof;
+  }
+  const cudaError_t e = cudaStreamEndCapture(b->origin, &graph);
+  if (rc != NHQG_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return rc != NHQG_OK ? rc : NHQG_ERR_CUDA;
+  }
+  const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return NHQG_ERR_CUDA;
+  g.steps = steps;
+  for (nhqg_ctx* c : b->members) g.versions.push_back(c->version);
+  return NHQG_OK;
+}
+
+// time one horizontal-product evaluation (ms, median of 3) with the current tiles
+float time_products(nhqg_ctx* c, bool f32, cudaStream_t st) {
+  cudaEvent_t a, z;
+  cudaEventCreate(&a);
+  cudaEventCreate(&z);
+  float best = -1.f;
+  std::vector<float> t;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(a, st);
+    const int rc = f32 ? horizontal_step_f32(c, c->Qf, c->Wf, c->Tf, st)
+                       : horizontal_step(c, c->Qn, c->Wn, c->Tn, st);
+    cudaEventRecord(z, st);
+    if (rc != NHQG_OK || cudaEventSynchronize(z) != cudaSuccess) {
+      cudaGetLastError();
+      t.clear();
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, z);
+    if (rep > 0) t.push_back(ms);  // the first run warms up
+  }
+  if (t.size() == 3) {
+    std::sort(t.begin(), t.end());
+    best = t[1];
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(z);
+  return best;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nhqg_get_tiles(const nhqg_ctx* c, int* tiles) {
+  if (!c || !tiles) return NHQG_ERR_BAD_ARG;
+  tiles[0] = c->p.h_col_kib[0]; tiles[1] = c->p.h_row_kib[0];
+  tiles[2] = c->p.h_col_kib[1]; tiles[3] = c->p.h_row_kib[1];
+  return NHQG_OK;
+}
+
+int nhqg_set_tiles(nhqg_ctx* c, const int* tiles) {
+  if (!c || !tiles) return NHQG_ERR_BAD_ARG;
+  for (int i = 0; i < 4; ++i)
+    if (tiles[i] < 0 || tiles[i] > 200) return NHQG_ERR_BAD_ARG;
+  c->p.h_col_kib[0] = tiles[0]; c->p.h_row_kib[0] = tiles[1];
+  c->p.h_col_kib[1] = tiles[2]; c->p.h_row_kib[1] = tiles[3];
+  ++c->version;
+  return NHQG_OK;
+}
+
+int nhqg_autotune(nhqg_ctx* c, void* stream) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  const bool prof = c->w.prof.on;
+  c->w.prof.on = false;
+  static const int col64[] = {48, 96, 144}, row64[] = {100, 200};
+  static const int col32[] = {12, 24, 44, 64, 96}, row32[] = {26, 52, 104};
+  for (int pi = 0; pi < 2; ++pi) {
+    const bool f32 = pi == 1;
+    if (f32 && !c->Qf) continue;  // FP32 buffers exist once the mixed path is enabled
+    const int* cols = f32 ? col32 : col64;
+    const int* rows = f32 ? row32 : row64;
+    const int nc = f32 ? 5 : 3, nr = f32 ? 3 : 2;
+    int best_c = 0, best_r = 0;
+    float best = -1.f;
+    for (int i = 0; i < nc; ++i)
+      for (int j = 0; j < nr; ++j) {
+        c->p.h_col_kib[pi] = cols[i];
+        c->p.h_row_kib[pi] = rows[j];
+        const float ms = time_products(c, f32, st);
+        if (ms > 0.f && (best < 0.f || ms < best)) { best = ms; best_c = cols[i]; best_r = rows[j]; }
+      }
+    c->p.h_col_kib[pi] = best_c;  // 0 (built-in default) if nothing ran
+    c->p.h_row_kib[pi] = best_r;
+  }
+  c->w.prof.on = prof;
+  ++c->version;
+  return cudaGetLastError() == cudaSuccess ? NHQG_OK : NHQG_ERR_CUDA;
+}
+
+int nhqg_batch_create(nhqg_ctx* const* members, int n, int steps_per_launch, nhqg_batch** out) {
+  if (!members || n <= 0 || steps_per_launch <= 0 || !out) return NHQG_ERR_BAD_ARG;
+  *out = nullptr;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j)
+      if (!members[i] || members[i] == members[j]) return NHQG_ERR_BAD_ARG;
+  nhqg_batch* b = new (std::nothrow) nhqg_batch();
+  if (!b) return NHQG_ERR_BAD_ARG;
+  b->members.assign(members, members + n);
+  b->spl = steps_per_launch;
+  bool ok = cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; i < n && ok; ++i) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+    if (ok) { b->streams.push_back(st); b->joins.push_back(ev); }
+  }
+  if (!ok) { nhqg_batch_destroy(b); return NHQG_ERR_CUDA; }
+  *out = b;
+  return NHQG_OK;
+}
+
+int nhqg_batch_destroy(nhqg_batch* b) {
+  if (!b) return NHQG_ERR_BAD_ARG;
+  if (b->origin) cudaStreamSynchronize(b->origin);
+  drop_graph(b->g_many);
+  drop_graph(b->g_one);
+  for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : b->joins) cudaEventDestroy(ev);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->origin) cudaStreamDestroy(b->origin);
+  delete b;
+  return NHQG_OK;
+}
+
+int nhqg_batch_load(nhqg_batch* b, int member, const nhqg_state* s, void* stream) {
+  if (!b || member < 0 || member >= (int)b->members.size()) return NHQG_ERR_BAD_ARG;
+  nhqg_ctx* c = b->members[member];
+  c->launches = 0;
+  return gather_state(c, s, S(stream));
+}
+
+int nhqg_batch_store(nhqg_batch* b, int member, nhqg_state* s, void* stream) {
+  if (!b || member < 0 || member >= (int)b->members.size()) return NHQG_ERR_BAD_ARG;
+  nhqg_ctx* c = b->members[member];
+  return scatter_fields(c, c->q0, c->w0, c->t0, c->tb0, s, S(stream));
+}
+
+int nhqg_batch_step(nhqg_batch* b, int n_steps, void* stream) {
+  if (!b || n_steps < 0) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  const int q = n_steps / b->spl, r = n_steps % b->spl;
+  int rc;
+  if (q > 0 && !graph_current(b, b->g_many) && (rc = capture(b, b->g_many, b->spl))) return rc;
+  if (r > 0 && !graph_current(b, b->g_one) && (rc = capture(b, b->g_one, 1))) return rc;
+  for (int i = 0; i < q; ++i) CK(cudaGraphLaunch(b->g_many.exec, st));
+  for (int i = 0; i < r; ++i) CK(cudaGraphLaunch(b->g_one.exec, st));
+  return NHQG_OK;
+}
+
+int nhqg_batch_size(const nhqg_batch* b) { return b ? (int)b->members.size() : -1; }
 
 }  // extern "C"

@@ -196,6 +196,23 @@ class Engine:
                                             _stream_handle()), "nhqg_diagnostics")
         return out
 
+    def tiles(self) -> tuple[int, int, int, int]:
+        """Horizontal-product tile budgets in KiB (FP64 col, FP64 row, FP32 col,
+        FP32 row); 0 = built-in default."""
+        t = (ctypes.c_int * 4)()
+        nat.check(self.lib.nhqg_get_tiles(self.handle, t), "nhqg_get_tiles")
+        return tuple(t)
+
+    def set_tiles(self, tiles) -> None:
+        t = (ctypes.c_int * 4)(*[int(v) for v in tiles])
+        nat.check(self.lib.nhqg_set_tiles(self.handle, t), "nhqg_set_tiles")
+
+    def autotune(self) -> tuple[int, int, int, int]:
+        """Time candidate tiles on this context's buffers (both precisions once
+        the mixed path is enabled), keep the fastest, return them."""
+        nat.check(self.lib.nhqg_autotune(self.handle, _stream_handle()), "nhqg_autotune")
+        return self.tiles()
+
     def sponge_product(self, f, out) -> None:
         nat.check(self.lib.nhqg_sponge_product_23(self.handle, int(f.shape[0]), f.data_ptr(),
                                                   out.data_ptr(), _stream_handle()),
