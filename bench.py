@@ -367,6 +367,11 @@ def run_ours(args, ws, rank, local):
     state = S.to_device(host0)
     eng = engine_for(grid)
     peaks = {"fp64": dgemm_peak_tflops(), "fp32": sgemm_peak_tflops(), "hbm": measured_hbm_gbs()}
+    tiles = None
+    if not args.no_autotune:  # horizontal-product tiles for both precisions, before any timing
+        eng.set_precision("mixed")
+        tiles = eng.autotune()
+        eng.set_precision("fp64")
 
     # spin-up (plain FP64) from the seeded start, then the accuracy of the
     # mixed step against the plain step from the same state
@@ -465,6 +470,7 @@ def run_ours(args, ws, rank, local):
         "roofline": dom,
         "kernels": shares(prof_mixed),
         "roofline_by_kernel": roof_mixed,
+        "autotuned_tiles_kib": tiles,
         "peaks": {"fp64_tflops": round(peaks["fp64"], 4), "fp32_tflops": round(peaks["fp32"], 3),
                   "hbm_gbs": peaks["hbm"], "fp32_nominal_tflops": round(NOMINAL_FP32_TFLOPS, 1)},
         "clocks": clk,
@@ -569,6 +575,87 @@ def run_ensemble(args, ws, rank):
     }
 
 
+def _tail_fraction(g, q_hat, n0: int) -> float:
+    """psi-KE fraction above Chebyshev mode n0: sum_{n>n0} sum_k w_k k^2 |psi_n|^2
+    over sum_n (...), half-plane weights w_k (1 at ky = 0 and Nyquist, else 2)."""
+    import torch
+    ksq = torch.from_numpy(np.asarray(g.ksq)).to(q_hat.device)
+    idn = torch.from_numpy(np.asarray(g.inv_denom)).to(q_hat.device)
+    w = torch.full_like(ksq, 2.0)
+    w[:, 0] = 1.0
+    w[:, -1] = 1.0
+    e = (w * ksq * idn ** 2)[None] * q_hat.abs() ** 2
+    per_n = e.sum(dim=(1, 2))
+    return float(per_n[n0 + 1:].sum() / per_n.sum())
+
+
+def run_closure(args, ws, rank):
+    """Learned vertical-tail closure, reduced form of its study: fine runs at
+    128^2x256 (the closure's data source), coarse runs at 128^2x64 with and
+    without the closure, on the first 64 Chebyshev modes of q."""
+    import torch
+    from nhqg_gb300 import NHQGConfig, make_grid, theta_perturbation_state
+    from nhqg_gb300 import closure as CL
+    from nhqg_gb300 import solver as S
+    from nhqg_gb300.engine import Engine
+
+    def cfg(nz):
+        c = workload(128, nz)
+        c.update(dt=5e-5)
+        return c
+    fine, coarse = make_grid(NHQGConfig(**cfg(256))), make_grid(NHQGConfig(**cfg(64)))
+    runs = []
+    for r in range(args.closure_runs):
+        s = S.to_device(theta_perturbation_state(fine, seed=r, amplitude=args.closure_amp))
+        snaps = []
+        for _ in range(args.closure_steps // 40):
+            S.step_inplace(s, fine, 40)
+            snaps.append(S.State(*(x.clone() for x in s)))
+        runs.append(snaps)
+    train = [st for run in runs[:-1] for st in run]
+    held = runs[-1]
+    data, sc = CL.training_columns(fine, coarse, train, ncoef=64)
+    hdata, _ = CL.training_columns(fine, coarse, held, scales=sc)
+    model = CL.TailClosure(sc, seed=0)
+    zero_h = model.evaluate(hdata["x"], hdata["q"], hdata["t"])
+    t0 = time.perf_counter()
+    hist = model.fit(data, epochs=args.closure_epochs, batch=2048, lr=1e-3)
+    torch.cuda.synchronize()
+    t_fit = time.perf_counter() - t0
+    train_ratio = hist[-1] / hist[0] if hist[0] > 0 else None
+    held_ratio = model.evaluate(hdata["x"], hdata["q"], hdata["t"]) / zero_h
+    # a posteriori: from the first held-out snapshot, fine vs coarse with / without the closure
+    k = args.closure_post_steps
+    s_f = S.State(*(x.clone() for x in held[0]))
+    s_plain = S.State(*(x.clone() for x in CL.truncate(held[0], coarse)))
+    s_cl = S.State(*(x.clone() for x in s_plain))
+    e_plain, e_cl = Engine(coarse), Engine(coarse)
+    model.attach(e_cl)
+    S.step_inplace(s_f, fine, k)
+    e_plain.step(*s_plain, n_steps=k)
+    e_cl.step(*s_cl, n_steps=k)
+    ref = s_f.q_hat[:coarse.Nz + 1]
+    err = lambda s: float(torch.linalg.norm(s.q_hat - ref) / torch.linalg.norm(ref))  # noqa: E731
+    if rank != 0:
+        return None
+    return {
+        "metric": "learned q-tail closure at 128^2x64 vs 128^2x256: held-out a-priori error ratio",
+        "value": round(held_ratio, 4), "unit": "ratio (closure / no closure)", "n_gpus": ws,
+        "higher_is_better": False, "vs_baseline": None, "dtype": "bf16 weights, fp32 accumulation",
+        "data": (f"{args.closure_runs} fine runs of {args.closure_steps} steps from seeded theta' "
+                 f"(amplitude {args.closure_amp}), snapshots every 40 steps; the last run held out"),
+        "config": {"workload": "closure study, fine 128^2x256, coarse 128^2x64, ncoef 64, dt=5e-5, "
+                               "evolve_mean SBP2-PC sub4", "params": CL.n_params()},
+        "train_loss_first_last_epoch": [round(hist[0], 5), round(hist[-1], 5)],
+        "train_ratio": None if train_ratio is None else round(train_ratio, 4),
+        "fit_seconds": round(t_fit, 2), "columns": int(data["x"].shape[0]),
+        "a_posteriori": {"steps": k, "q_rel_err_no_closure": err(s_plain), "q_rel_err_closure": err(s_cl),
+                         "tail_fraction_above_48": {"fine": _tail_fraction(fine, ref, 48),
+                                                    "coarse": _tail_fraction(coarse, s_plain.q_hat, 48),
+                                                    "coarse_closure": _tail_fraction(coarse, s_cl.q_hat, 48)}},
+    }
+
+
 def run_reference(args, ws, rank):
     """CPU arm: the oracle port of the reference step on the host cores, on
     this arm's workload, metric and units; rank 0 only."""
@@ -603,6 +690,15 @@ def main():
     ap.add_argument("--err-steps", type=int, default=500,
                     help="steps of the mixed-vs-plain accuracy comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the built-in horizontal-product tiles")
+    ap.add_argument("--closure", action="store_true",
+                    help="run the learned-closure study instead (its own JSON line)")
+    ap.add_argument("--closure-runs", type=int, default=3)
+    ap.add_argument("--closure-steps", type=int, default=400)
+    ap.add_argument("--closure-amp", type=float, default=1e-3)
+    ap.add_argument("--closure-epochs", type=int, default=30)
+    ap.add_argument("--closure-post-steps", type=int, default=200)
     ap.add_argument("--ensemble", action="store_true",
                     help="time the 48-member batched ensemble instead (its own JSON line)")
     args = ap.parse_args()
@@ -611,6 +707,8 @@ def main():
         line = run_reference(args, ws, rank)
     elif args.ensemble:
         line = run_ensemble(args, ws, rank)
+    elif args.closure:
+        line = run_closure(args, ws, rank)
     else:
         line = run_ours(args, ws, rank, local)
     if rank == 0 and line is not None:

@@ -247,6 +247,38 @@ int nhqg_batch_store(nhqg_batch *batch, int member, nhqg_state *state, void *str
 int nhqg_batch_step(nhqg_batch *batch, int n_steps, void *stream);
 int nhqg_batch_size(const nhqg_batch *batch);
 
+/* ---- Learned vertical-tail closure for q (no reference counterpart) ----
+ * An opt-in extra q tendency C_n = -s (r_n + i rho_n) q_n on the first ncoef
+ * (<= 64) Chebyshev coefficients of every horizontal mode, with (r, rho) =
+ * MLP(features of the column): features log1p(|q_n|^2 / sq_n) (n < 64),
+ * |k| / kmax and log1p(sum_n |k|^2 |psi_n|^2 / se).  MLP 66 -> 256 -> 128 ->
+ * 128 (r_n at n, rho_n at 64 + n), tanh hidden units,
+ * nhqg_closure_param_count() BF16 parameters (layer-major: W1 [256][66], b1,
+ * W2 [128][256], b2, W3 [128][128], b3), FP32 accumulation.
+ * nhqg_closure_set attaches DEVICE pointers owned by the caller (weights and
+ * sq [64]) to a context: every later explicit RHS and step adds C to E_q;
+ * w_bf16 = NULL detaches.  nhqg_closure_apply writes C for a state as a
+ * (Nz+1, Nx, Nk) complex128 plane set.  nhqg_closure_features writes the
+ * features (x [M][66] FP32) and columns (q [M][64] complex FP32) of a state's
+ * M = nhqg_mode_count() in-band modes.  nhqg_closure_train_step runs one
+ * forward/backward pass over a batch (x [B][66], q and target [B][64] complex
+ * FP32), writes the mean loss sum_n |C_n - t_n|^2 / target_norm and the FP32
+ * gradient, and (lr > 0) one Adam step on the FP32 master weights that also
+ * refreshes the BF16 copy (step counts from 1).  nhqg_gather_q copies a
+ * state's q to the compact (Nz+1) x M layout of the context. */
+int nhqg_mode_count(const nhqg_ctx *ctx);
+int nhqg_closure_param_count(void);
+int nhqg_closure_set(nhqg_ctx *ctx, const void *w_bf16, const float *sq, int ncoef, float se,
+                     float kmax, float out_scale);
+int nhqg_closure_apply(nhqg_ctx *ctx, const nhqg_state *state, void *out_q, void *stream);
+int nhqg_closure_features(nhqg_ctx *ctx, const nhqg_state *state, const float *sq, int ncoef,
+                          float se, float kmax, float *x, float *qcols, void *stream);
+int nhqg_closure_train_step(const void *w_bf16, float *w_master, float *adam_m, float *adam_v,
+                            float *grad, float *loss, int batch, const float *x, const float *q,
+                            const float *target, float out_scale, float target_norm, float lr,
+                            int step, void *stream);
+int nhqg_gather_q(nhqg_ctx *ctx, const nhqg_state *state, void *out_compact, void *stream);
+
 /* Engine build identification string (static storage). */
 const char *nhqg_version(void);
 

@@ -22,7 +22,7 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libnhqg_gpu.so"
 SOURCES = ("horizontal.cu", "vertical.cu", "corrector.cu", "capi.cu", "noalloc.cu", "tau_solve.cu",
-           "diag.cu")
+           "diag.cu", "closure.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
 
@@ -162,6 +162,19 @@ SIGNATURES = {
                                         ctypes.c_void_p]),
     "nhqg_batch_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "nhqg_batch_size": (ctypes.c_int, [ctypes.c_void_p]),
+    "nhqg_mode_count": (ctypes.c_int, [ctypes.c_void_p]),
+    "nhqg_closure_param_count": (ctypes.c_int, []),
+    "nhqg_closure_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+    "nhqg_closure_apply": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(StateDesc), ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+    "nhqg_closure_features": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(StateDesc), ctypes.c_void_p,
+                                             ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_void_p]),
+    "nhqg_closure_train_step": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.c_int] + [ctypes.c_void_p] * 3 +
+                                [ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_void_p]),
+    "nhqg_gather_q": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(StateDesc), ctypes.c_void_p,
+                                     ctypes.c_void_p]),
     "nhqg_profile_report": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "nhqg_version": (ctypes.c_char_p, []),
 }

@@ -31,6 +31,9 @@ struct nhqg_ctx {
   // products, allocated by the first nhqg_set_precision(NHQG_PRECISION_MIXED)
   int precision = NHQG_PRECISION_FP64;
   float2 *Qf = nullptr, *Wf = nullptr, *Tf = nullptr, *Aqf = nullptr, *Awf = nullptr, *Atf = nullptr;
+  // learned closure (null weights: off) and its tendency buffer [P*M]
+  ClosureModel closure{};
+  double2* Cq = nullptr;
   // bumped whenever the launch sequence of a step changes (precision, tiles):
   // captured step graphs of a batch compare it
   unsigned version = 0;
@@ -635,8 +638,17 @@ int explicit_front(nhqg_ctx* c, const double2* q, const double2* w, const double
   return horizontal_step(c, c->Qn, c->Wn, c->Tn, st);
 }
 
+// the closure tendency of the q state the following vback reads
+int closure_front(nhqg_ctx* c, const double2* q, cudaStream_t st) {
+  if (!c->closure.w) return NHQG_OK;
+  PCK("closure", launch_closure_apply(c->p, c->t, c->closure, q, c->Cq, st));
+  c->launches += 1;
+  return NHQG_OK;
+}
+
 VArgs base_vargs(nhqg_ctx* c) {
   VArgs a{};
+  a.Cq = c->closure.w ? c->Cq : nullptr;
   a.Aq = c->Aq; a.Aw = c->Aw; a.At = c->At;
   if (mixed(c)) { a.Aqf = c->Aqf; a.Awf = c->Awf; a.Atf = c->Atf; }
   a.E1q = c->E1q; a.E1w = c->E1w; a.E1t = c->E1t;
@@ -674,6 +686,7 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
   // ---------------- stage 1
   rc = explicit_front(c, c->q0, c->w0, c->t0, c->tb0, legacy_mean, c->E1tb, nullptr, true, st);
   if (rc) return rc;
+  if ((rc = closure_front(c, c->q0, st))) return rc;
   VArgs a = base_vargs(c);
   a.q0 = c->q0; a.w0 = c->w0; a.t0 = c->t0;
   a.dtb_nodal = legacy_mean ? c->dtb : nullptr;
@@ -719,6 +732,7 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
     rc = explicit_front(c, c->Q1, c->W1, t1, tb1, legacy_mean, c->E2tb, c->Itb, true, st);
     if (rc) return rc;
   }
+  if ((rc = closure_front(c, c->Q1, st))) return rc;
   a = base_vargs(c);
   a.q0 = c->q0; a.w0 = c->w0; a.t0 = c->t0;
   a.q1 = c->Q1; a.w1 = c->W1; a.t1 = t1; a.t1p = c->T1p;
@@ -789,6 +803,7 @@ int nhqg_explicit_rhs(nhqg_ctx* c, const nhqg_state* in, nhqg_state* out, int cl
   if (legacy_mean && !c->t.mean_solve) return NHQG_ERR_UNSUPPORTED;
   rc = explicit_front(c, c->q0, c->w0, c->t0, c->tb0, legacy_mean, c->E1tb, nullptr, true, st);
   if (rc) return rc;
+  if ((rc = closure_front(c, c->q0, st))) return rc;
   VArgs a = base_vargs(c);
   a.q0 = c->q0; a.w0 = c->w0; a.t0 = c->t0;
   a.dtb_nodal = legacy_mean ? c->dtb : nullptr;
@@ -1073,14 +1088,14 @@ int nhqg_autotune(nhqg_ctx* c, void* stream) {
   cudaStream_t st = S(stream);
   const bool prof = c->w.prof.on;
   c->w.prof.on = false;
-  static const int col64[] = {48, 96, 144}, row64[] = {100, 200};
-  static const int col32[] = {12, 24, 44, 64, 96}, row32[] = {26, 52, 104};
+  static const int col64[] = {24, 48, 96, 144}, row64[] = {25, 50, 100, 200};
+  static const int col32[] = {6, 12, 24, 44, 64}, row32[] = {13, 26, 52, 104};
   for (int pi = 0; pi < 2; ++pi) {
     const bool f32 = pi == 1;
     if (f32 && !c->Qf) continue;  // FP32 buffers exist once the mixed path is enabled
     const int* cols = f32 ? col32 : col64;
     const int* rows = f32 ? row32 : row64;
-    const int nc = f32 ? 5 : 3, nr = f32 ? 3 : 2;
+    const int nc = f32 ? 5 : 4, nr = 4;
     int best_c = 0, best_r = 0;
     float best = -1.f;
     for (int i = 0; i < nc; ++i)
@@ -1161,5 +1176,69 @@ int nhqg_batch_step(nhqg_batch* b, int n_steps, void* stream) {
 }
 
 int nhqg_batch_size(const nhqg_batch* b) { return b ? (int)b->members.size() : -1; }
+
+}  // extern "C"
+
+// ============================================================== learned closure
+extern "C" {
+
+int nhqg_mode_count(const nhqg_ctx* c) { return c ? c->p.d.M : -1; }
+
+int nhqg_closure_set(nhqg_ctx* c, const void* w_bf16, const float* sq, int ncoef, float se,
+                     float kmax, float out_scale) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  if (!w_bf16) {
+    if (c->closure.w) ++c->version;
+    c->closure = ClosureModel{};
+    return NHQG_OK;
+  }
+  if (!sq || ncoef < 1 || ncoef > 64 || ncoef > c->p.d.P || !(se > 0.f) || !(kmax > 0.f))
+    return NHQG_ERR_BAD_ARG;
+  if (!c->Cq && dalloc(c, &c->Cq, (size_t)c->p.d.P * c->p.d.M) != cudaSuccess) return NHQG_ERR_CUDA;
+  c->closure.w = w_bf16;
+  c->closure.sq = sq;
+  c->closure.ncoef = ncoef;
+  c->closure.se = se;
+  c->closure.kmax = kmax;
+  c->closure.s = out_scale;
+  ++c->version;
+  return NHQG_OK;
+}
+
+int nhqg_closure_apply(nhqg_ctx* c, const nhqg_state* s, void* out_q, void* stream) {
+  if (!c || !s || !out_q) return NHQG_ERR_BAD_ARG;
+  if (!c->closure.w) return NHQG_ERR_UNSUPPORTED;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  int rc = gather_state(c, s, st);
+  if (rc) return rc;
+  CK(launch_closure_apply(c->p, c->t, c->closure, c->q0, c->Cq, st));
+  CK(launch_scatter(c->p, c->Cq, (double2*)out_q, c->p.d.P, st));
+  c->launches += 2;
+  return NHQG_OK;
+}
+
+int nhqg_closure_features(nhqg_ctx* c, const nhqg_state* s, const float* sq, int ncoef, float se,
+                          float kmax, float* x, float* qcols, void* stream) {
+  if (!c || !s || !sq || !x || !qcols || ncoef < 1 || ncoef > 64 || ncoef > c->p.d.P)
+    return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  int rc = gather_state(c, s, st);
+  if (rc) return rc;
+  ClosureModel cm{};
+  cm.sq = sq; cm.ncoef = ncoef; cm.se = se; cm.kmax = kmax;
+  CK(launch_closure_features(c->p, c->t, cm, c->q0, x, reinterpret_cast<float2*>(qcols), st));
+  return NHQG_OK;
+}
+
+int nhqg_gather_q(nhqg_ctx* c, const nhqg_state* s, void* out_compact, void* stream) {
+  if (!c || !s || !out_compact) return NHQG_ERR_BAD_ARG;
+  cudaStream_t st = S(stream);
+  int rc = gather_state(c, s, st);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(out_compact, c->q0, (size_t)c->p.d.P * c->p.d.M * sizeof(double2),
+                     cudaMemcpyDeviceToDevice, st));
+  return NHQG_OK;
+}
 
 }  // extern "C"

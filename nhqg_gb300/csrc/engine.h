@@ -190,6 +190,19 @@ cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const H
 cudaError_t launch_horizontal_f32(const Params& p, const Tables& t, Work& w,
                                   const HorizArgsT<float2, float2>& a, cudaStream_t st, int* nlaunch);
 
+// learned vertical-tail closure for q (csrc/closure.cu)
+struct ClosureModel {
+  const void* w = nullptr;    // BF16 parameters, nhqg_closure_param_count() values
+  const float* sq = nullptr;  // [64] feature scales of |q_n|^2
+  int ncoef = 0;              // coefficients the closure acts on (<= 64)
+  float se = 1.f, kmax = 1.f, s = 0.f;
+};
+int closure_param_count();
+cudaError_t launch_closure_apply(const Params& p, const Tables& t, const ClosureModel& cm,
+                                 const double2* q, double2* cq, cudaStream_t st);
+cudaError_t launch_closure_features(const Params& p, const Tables& t, const ClosureModel& cm,
+                                    const double2* q, float* x, float2* qc, cudaStream_t st);
+
 // vertical / column engine
 enum VBackMode { VB_RHS = 0, VB_STAGE1 = 1, VB_STAGE2 = 2, VB_SOLVE = 3 };
 struct VArgs {
@@ -201,6 +214,8 @@ struct VArgs {
   const double2 *Aq, *Aw, *At;
   const float2 *Aqf, *Awf, *Atf;
   double2 *E1q, *E1w, *E1t;
+  // learned closure tendency of q (added to E_q) or null
+  const double2* Cq;
   // nodal w (legacy exchange product), dtb nodal vector
   const double2* Wn;
   const double* dtb_nodal;  // [P] or null

@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
         const double2 qv = qs[(size_t)l * Ms + m];
         e = make_double2(fma(-s, qv.y, e.x), fma(s, qv.x, e.y));
       }
+      if (a.Cq) e = cadd(e, a.Cq[(size_t)l * Ms + m]);  // learned closure
       b1[i] = e;
     }
     __syncthreads();
