@@ -16,7 +16,8 @@ from .initial import theta_perturbation_state  # noqa: F401
 
 def __getattr__(name):
     # torch-backed API loads lazily so that make_grid works without CUDA
-    if name in ("State", "imex_step", "run", "step_inplace", "sanitize_state", "to_device", "to_host"):
+    if name in ("State", "imex_step", "run", "step_inplace", "sanitize_state", "to_device", "to_host",
+                "make_initial_state"):
         from . import solver
         return getattr(solver, name)
     if name == "compute_diagnostics":

@@ -2,7 +2,7 @@
 
 Same names, argument meaning and return structure as the reference's
 ``nhqg.solver`` (nhqg/solver.py): ``State`` (q_hat, w_hat, th_hat, th_bar),
-``imex_step(state, grid) -> State``, ``explicit_rhs``,
+``imex_step(state, grid) -> State``, ``make_initial_state``, ``explicit_rhs``,
 ``explicit_rhs_dispatch``, ``implicit_tendency``, ``imex_implicit_solve``,
 ``imex_mean_temp_solve``, ``sanitize_state`` and ``run``.  Fields are CUDA
 torch tensors (complex128 / float64) in the reference layout; NumPy arrays
@@ -162,6 +162,14 @@ def apply_balanced_sbp2_corrector(state, grid: Grid, total_dt) -> State:
     eng.corrector(src, out, float(total_dt))
     _check_band(eng, "apply_balanced_sbp2_corrector")
     return out
+
+
+def make_initial_state(grid: Grid, seed: int = 0, amplitude: float = 1e-3) -> State:
+    """The reference's random q' start with JAX's PRNG stream
+    (nhqg/solver.py:1343-1376; see ``initial.make_initial_state``), on the
+    device."""
+    from .initial import make_initial_state as _mis
+    return to_device(_mis(grid, seed=seed, amplitude=amplitude))
 
 
 def run(grid: Grid, state, n_steps: int, save_interval: int, use_imex: bool = True,

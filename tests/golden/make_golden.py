@@ -256,10 +256,38 @@ def diagnostics_main(ref_root: str) -> None:
     print(f"diagnostics: {len(out)} entries")
 
 
+# the reference's own bitwise regression (tests/test_mixed_bc_plumbing.py:99-117):
+# make_initial_state(seed=0, amplitude=1e-3) with JAX's PRNG, then 20 steps
+JAXPRNG_CFG = dict(Nx=32, Nz=16, L=20.0, Ra_tilde=100.0, sigma=1.0, beta=0.0, Ld=float("inf"),
+                   dt=1e-3, float_dtype="float64", nu_q=1.0, nu_w=1.0, nu_theta=1.0, hyper_order=1,
+                   nonlinear_advection="flux", horizontal_dealiasing="23_rule",
+                   thermal_closure="evolve_mean", mean_exchange_discretization="balanced_sbp2_pc",
+                   sbp_corrector_substeps=2)
+
+
+def jaxprng_main(ref_root: str) -> None:
+    """Pack the reference's data file tests/data/m2b_dirichlet_evolvemean_ref.npz
+    (generated by the reference with JAX on CPU) into jaxprng_m2b.npz."""
+    z = np.load(Path(ref_root) / "tests" / "data" / "m2b_dirichlet_evolvemean_ref.npz")
+    out = {}
+    for f in ("q_hat", "w_hat", "th_hat"):
+        a = np.asarray(z[f])
+        assert out_of_band_max(a, JAXPRNG_CFG["Nx"]) == 0.0, f
+        out[f"sN.{f}__packed"] = pack(a, JAXPRNG_CFG["Nx"])
+    out["sN.th_bar"] = np.asarray(z["th_bar"], dtype=np.float64)
+    meta = dict(cfg=JAXPRNG_CFG, n_steps=20, seed=0, amplitude=1e-3,
+                source="reference tests/data/m2b_dirichlet_evolvemean_ref.npz",
+                generator="tests/golden/make_golden.py --jaxprng")
+    np.savez_compressed(HERE / "jaxprng_m2b.npz", meta=json.dumps(meta), **out)
+    print(f"jaxprng_m2b: {(HERE / 'jaxprng_m2b.npz').stat().st_size / 1024:.0f} KiB")
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else "/root/reference"
     if "--diagnostics" in sys.argv:
         diagnostics_main(root)
+    elif "--jaxprng" in sys.argv:
+        jaxprng_main(root)
     else:
         main(root)

@@ -189,3 +189,14 @@ def test_config1_100_steps(recipe):
     s = S.to_device(s0)
     S.step_inplace(s, g, 100, check=True)
     assert_state_close(_host(s), os_, 1e-9, th_bar_abs=1e-18)
+
+
+def test_make_initial_state_reference_regression():
+    """make_initial_state with JAX's PRNG stream, then 20 GPU steps, against
+    the reference's own bitwise regression data
+    (tests/test_mixed_bc_plumbing.py:99-117)."""
+    meta, arrays = fixtures.load_case("jaxprng_m2b")
+    g = make_grid(NHQGConfig(**dict(meta["cfg"])))
+    s = S.make_initial_state(g, seed=meta["seed"], amplitude=meta["amplitude"])
+    S.step_inplace(s, g, meta["n_steps"], check=True)
+    assert_state_close(_host(s), fixtures.state_from(arrays, "sN"), 1e-12, th_bar_abs=1e-18)
