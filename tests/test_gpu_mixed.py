@@ -155,3 +155,21 @@ def test_config1_100_steps_mixed():
     s = S.to_device(s0)
     S.step_inplace(s, g, 100, check=True, precision="mixed")
     assert_state_close(_host(s), os_, 1e-6, th_bar_abs=1e-18)
+
+
+@pytest.mark.parametrize("nx", [64, 128, 256])
+def test_explicit_rhs_fp32_row_products_sizes(nx):
+    """The FP32 row products at power-of-two row lengths (radix-4 and mixed
+    radix-4/2 plans): mixed explicit RHS against the plain one on a random
+    state whose spectrum fills the 2/3-rule band."""
+    cfg = dict(Nx=nx, Nz=16, L=10 * L_C, Ra_tilde=100.0, dt=5e-5, nonlinear_advection="flux",
+               horizontal_dealiasing="23_rule", float_dtype="float64", thermal_closure="fixed_conduction")
+    g = make_grid(NHQGConfig(**cfg))
+    rng = np.random.default_rng(nx)
+    P, G, Nk = g.Nz + 1, g.Nz - 1, g.Nk
+    env = np.exp(-np.asarray(g.ksq) / (2.0 * float(np.max(g.ksq)) / 9.0))
+    fld = lambda n: 0.3 * (rng.standard_normal((n, nx, Nk)) + 1j * rng.standard_normal((n, nx, Nk))) * env[None]  # noqa: E731
+    s = S.sanitize_state((fld(P), fld(G), fld(G), np.zeros(P)), g)
+    E64 = _host(S.explicit_rhs(s, g))
+    E32 = _host(S.explicit_rhs(s, g, precision="mixed"))
+    assert_state_close(E32, E64, 2e-5, th_bar_abs=1e-14)
