@@ -129,6 +129,27 @@ int nhqg_step(nhqg_ctx *ctx, nhqg_state *state, int n_steps, void *stream);
  * modes) each. */
 int nhqg_set_precision(nhqg_ctx *ctx, int precision);
 
+/* Engine of the mixed path's Chebyshev <-> nodal transforms (the FP32 part of
+ * _to_nodal / _to_coeffs, nhqg/solver.py:45-52).  tensor_cores = 1: dense
+ * parity-folded products on the tcgen05 tensor cores, TF32 hi/lo split
+ * operands with FP32 accumulation (the default where available); 0: FP32
+ * fast DCT-I on the CUDA cores.  NHQG_ERR_UNSUPPORTED for 1 when Nz is odd or
+ * above 256, the w basis is the open-top one, or the descriptor has no
+ * shell_coef.  The environment variable NHQG_TC_VERTICAL=0 makes 0 the
+ * context's default. */
+int nhqg_set_mixed_vertical(nhqg_ctx *ctx, int tensor_cores);
+/* 1 if the mixed path's vertical transforms run on the tensor cores. */
+int nhqg_get_mixed_vertical(const nhqg_ctx *ctx);
+/* The tensor-core transforms alone, on M = nhqg_mode_count() columns.
+ * nhqg_tc_to_nodal: field 0 (q, Chebyshev coefficients, (Nz+1) x M), 1 (w) or
+ * 2 (theta) (Galerkin coefficients, (Nz-1) x M), complex128, to the
+ * (Nz+1) x M complex64 nodal values of _to_nodal(_dirichlet_to_cheb(.)).
+ * nhqg_tc_to_coef: (Nz+1) x M complex64 nodal values to Chebyshev
+ * coefficients (_to_coeffs), in place.  NHQG_ERR_UNSUPPORTED where
+ * nhqg_set_mixed_vertical(ctx, 1) is. */
+int nhqg_tc_to_nodal(nhqg_ctx *ctx, int field, const void *coef, void *nodal, void *stream);
+int nhqg_tc_to_coef(nhqg_ctx *ctx, void *nodal_inout, void *stream);
+
 /* explicit_rhs (nhqg/solver.py:510-599) at `in`, written to `out`.
  * closure/exchange select the Grid flavour the reference call would see
  * (the split steppers evaluate it on the fixed_conduction/legacy base grid,

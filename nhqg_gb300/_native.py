@@ -22,7 +22,7 @@ INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libnhqg_gpu.so"
 SOURCES = ("horizontal.cu", "vertical.cu", "corrector.cu", "capi.cu", "noalloc.cu", "tau_solve.cu",
-           "diag.cu", "closure.cu")
+           "diag.cu", "closure.cu", "tc_vertical.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
 
@@ -148,6 +148,11 @@ SIGNATURES = {
     "nhqg_last_launch_count": (ctypes.c_int, [ctypes.c_void_p]),
     "nhqg_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nhqg_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "nhqg_set_mixed_vertical": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "nhqg_get_mixed_vertical": (ctypes.c_int, [ctypes.c_void_p]),
+    "nhqg_tc_to_nodal": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p]),
+    "nhqg_tc_to_coef": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "nhqg_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(StateDesc), ctypes.c_void_p,
                                         ctypes.c_void_p]),
     "nhqg_get_tiles": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),

@@ -423,6 +423,25 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     }
   }
 
+  // ---- tensor-core vertical transforms of the mixed-precision path ----
+  if (g->shell_coef) {
+    TcHostImage img[4];
+    if (tc_vertical_images(g, img)) {
+      for (int i = 0; i < 4; ++i) {
+        uint8_t* b = nullptr;
+        float* x = nullptr;
+        UP(b, img[i].bytes.data(), img[i].bytes.size());
+        UP(x, img[i].xrow.data(), img[i].xrow.size());
+        t.tc.img[i] = b;
+        t.tc.xrow[i] = x;
+        t.tc.K[i] = img[i].K;
+        t.tc.nch[i] = img[i].nch;
+      }
+      const char* e = getenv("NHQG_TC_VERTICAL");
+      p.tc_vertical = !(e && e[0] == '0');
+    }
+  }
+
   // ---- work buffers ----
   Work& w = c->w;
   const size_t fe = (size_t)P * M;
@@ -544,6 +563,37 @@ int nhqg_set_precision(nhqg_ctx* c, int precision) {
   return NHQG_OK;
 }
 
+int nhqg_set_mixed_vertical(nhqg_ctx* c, int tensor_cores) {
+  if (!c) return NHQG_ERR_BAD_ARG;
+  const bool on = tensor_cores != 0;
+  if (on && !c->t.tc.img[0]) return NHQG_ERR_UNSUPPORTED;
+  if (c->p.tc_vertical != on) ++c->version;
+  c->p.tc_vertical = on;
+  return NHQG_OK;
+}
+
+int nhqg_get_mixed_vertical(const nhqg_ctx* c) { return c && c->p.tc_vertical ? 1 : 0; }
+
+int nhqg_tc_to_nodal(nhqg_ctx* c, int field, const void* coef, void* nodal, void* stream) {
+  if (!c || !coef || !nodal || field < 0 || field > 2) return NHQG_ERR_BAD_ARG;
+  if (!c->t.tc.img[0]) return NHQG_ERR_UNSUPPORTED;
+  const double2* in[3] = {nullptr, nullptr, nullptr};
+  float2* out[3] = {nullptr, nullptr, nullptr};
+  in[field] = static_cast<const double2*>(coef);
+  out[field] = static_cast<float2*>(nodal);
+  CK(launch_tc_to_nodal(c->p, c->t, c->w, in[0], in[1], in[2], out[0], out[1], out[2],
+                        static_cast<cudaStream_t>(stream)));
+  return NHQG_OK;
+}
+
+int nhqg_tc_to_coef(nhqg_ctx* c, void* nodal_inout, void* stream) {
+  if (!c || !nodal_inout) return NHQG_ERR_BAD_ARG;
+  if (!c->t.tc.img[0]) return NHQG_ERR_UNSUPPORTED;
+  CK(launch_tc_to_coef(c->p, c->t, c->w, static_cast<float2*>(nodal_inout), nullptr, nullptr,
+                       static_cast<cudaStream_t>(stream)));
+  return NHQG_OK;
+}
+
 }  // extern "C"
 
 // ============================================================== orchestration
@@ -595,6 +645,23 @@ int horizontal_step_f32(nhqg_ctx* c, const float2* qn, const float2* wn, const f
   a.psi = nullptr; a.q = qn; a.w = wn; a.th = tn;
   a.Aq = c->Aqf; a.Aw = c->Awf; a.Ath = c->Atf;
   CK(launch_horizontal_f32(p, c->t, c->w, a, st, &c->launches));
+  if (p.tc_vertical) {  // nodal A -> Chebyshev coefficients on the tensor cores
+    PCK("tc_to_coef", launch_tc_to_coef(p, c->t, c->w, c->Aqf, c->Awf, c->Atf, st));
+    c->launches += 1;
+  }
+  return NHQG_OK;
+}
+
+// FP32 nodal fields of the mixed path from FP64 coefficients (null = skip)
+int to_nodal_f32(nhqg_ctx* c, const double2* q, const double2* w, const double2* t, cudaStream_t st) {
+  const Params& p = c->p;
+  if (p.tc_vertical) {
+    PCK("tc_to_nodal", launch_tc_to_nodal(p, c->t, c->w, q, w, t, q ? c->Qf : nullptr,
+                                          w ? c->Wf : nullptr, t ? c->Tf : nullptr, st));
+  } else {
+    PCK("vfwd_f32", launch_vfwd_f32(p, c->t, q, w, t, c->Qf, c->Wf, c->Tf, st));
+  }
+  c->launches += 1;
   return NHQG_OK;
 }
 
@@ -623,8 +690,8 @@ int explicit_front(nhqg_ctx* c, const double2* q, const double2* w, const double
   const Params& p = c->p;
   if (mixed(c)) {
     if (legacy_mean) return NHQG_ERR_UNSUPPORTED;
-    PCK("vfwd_f32", launch_vfwd_f32(p, c->t, need_q ? q : nullptr, w, t, c->Qf, c->Wf, c->Tf, st));
-    c->launches += 1;
+    int rc = to_nodal_f32(c, need_q ? q : nullptr, w, t, st);
+    if (rc) return rc;
     return horizontal_step_f32(c, c->Qf, c->Wf, c->Tf, st);
   }
   PCK("vfwd", launch_vfwd(p, c->t, need_q ? q : nullptr, w, t, c->Qn, c->Wn, c->Tn, st));
@@ -650,7 +717,10 @@ VArgs base_vargs(nhqg_ctx* c) {
   VArgs a{};
   a.Cq = c->closure.w ? c->Cq : nullptr;
   a.Aq = c->Aq; a.Aw = c->Aw; a.At = c->At;
-  if (mixed(c)) { a.Aqf = c->Aqf; a.Awf = c->Awf; a.Atf = c->Atf; }
+  if (mixed(c)) {
+    a.Aqf = c->Aqf; a.Awf = c->Awf; a.Atf = c->Atf;
+    a.af_coef = c->p.tc_vertical;
+  }
   a.E1q = c->E1q; a.E1w = c->E1w; a.E1t = c->E1t;
   a.Wn = c->Wn;
   a.Rq = c->Rq; a.Rt = c->Rt; a.rhs_w = c->rhs;
@@ -719,9 +789,9 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
   if (have_nodal_wt) {
     // nodal w and theta of state1 come out of the corrector
     if (mixed(c)) {
-      PCK("vfwd_f32", launch_vfwd_f32(p, c->t, c->Q1, nullptr, nullptr, c->Qf, nullptr, nullptr, st));
+      if ((rc = to_nodal_f32(c, c->Q1, nullptr, nullptr, st))) return rc;
       PCK("to_f32", launch_to_f32(p, c->Wcgl, c->Tcgl, c->Wf, c->Tf, st));
-      c->launches += 2;
+      c->launches += 1;
       if ((rc = horizontal_step_f32(c, c->Qf, c->Wf, c->Tf, st))) return rc;
     } else {
       PCK("vfwd", launch_vfwd(p, c->t, c->Q1, nullptr, nullptr, c->Qn, nullptr, nullptr, st));

@@ -1,6 +1,7 @@
 // Internal engine interface: device tables, work buffers, kernel launchers.
 #pragma once
 #include <cuda_runtime.h>
+#include <cstdint>
 #include <vector>
 
 #include "common.cuh"
@@ -12,6 +13,21 @@ namespace nhqg {
 // bits of the device status word
 constexpr int NHQG_STATUS_BIT_OOB = 0;      // input content outside the 2/3 band
 constexpr int NHQG_STATUS_BIT_TIMEOUT = 1;  // a bounded device wait ran out
+
+// Tensor-core vertical transforms (csrc/tc_vertical.cu): per transform
+// (0 forward q: V, 1 forward w: V S_w, 2 forward theta: V S, 3 inverse V^-1)
+// the parity-folded TF32 hi/lo matrix image in shared-memory order, the
+// CUDA-core row, the input rows K and the number of k-chunks.
+struct TcHostImage {
+  std::vector<uint8_t> bytes;
+  std::vector<float> xrow;
+  int K = 0, nch = 0;
+};
+struct TcTables {
+  const uint8_t* img[4] = {};
+  const float* xrow[4] = {};
+  int K[4] = {}, nch[4] = {};
+};
 
 // Device-resident tables, uploaded once by nhqg_ctx_create.
 struct Tables {
@@ -69,6 +85,8 @@ struct Tables {
   // O(N) tau solve of the mixed-precision path (null: not available)
   int* mode_shell = nullptr;  // [M] shell of each compact mode (order of shell_inv)
   double *tau_tab = nullptr, *tau_par = nullptr, *tau_uni = nullptr;
+  // tensor-core vertical transforms of the mixed-precision path (img null: absent)
+  TcTables tc;
 };
 
 struct Params {
@@ -83,6 +101,8 @@ struct Params {
   // column tiles of H1/H3 and the row tile of H2 (0 = built-in default);
   // set by nhqg_autotune
   int h_col_kib[2], h_row_kib[2];
+  // mixed-precision vertical transforms on the tensor cores (else FP32 DCT)
+  bool tc_vertical;
 };
 
 }  // namespace nhqg
@@ -213,6 +233,7 @@ struct VArgs {
   // passes A in FP32 (Aqf, Awf, Atf non-null) instead
   const double2 *Aq, *Aw, *At;
   const float2 *Aqf, *Awf, *Atf;
+  bool af_coef;  // Aqf/Awf/Atf already hold Chebyshev coefficients (tensor-core inverse)
   double2 *E1q, *E1w, *E1t;
   // learned closure tendency of q (added to E_q) or null
   const double2* Cq;
@@ -233,6 +254,16 @@ cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, cons
 cudaError_t launch_vfwd_f32(const Params& p, const Tables& t, const double2* q, const double2* w,
                             const double2* th, float2* qn, float2* wn, float2* tn, cudaStream_t st);
 cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st);
+// tensor-core vertical transforms (csrc/tc_vertical.cu).  Host images: false
+// when Nz is odd or above 256, or a matrix lacks the mirror parity.
+bool tc_vertical_images(const nhqg_grid_desc* g, TcHostImage img[4]);
+// FP64 Chebyshev (q) / Galerkin (w, theta) coefficients -> FP32 nodal values
+cudaError_t launch_tc_to_nodal(const Params& p, const Tables& t, const Work& w, const double2* q,
+                               const double2* wf, const double2* th, float2* qn, float2* wn,
+                               float2* tn, cudaStream_t st);
+// FP32 nodal values -> FP32 Chebyshev coefficients, in place
+cudaError_t launch_tc_to_coef(const Params& p, const Tables& t, const Work& w, float2* aq,
+                              float2* aw, float2* at, cudaStream_t st);
 // FP64 nodal fields (the corrector's w and theta) -> FP32, P*M elements each
 cudaError_t launch_to_f32(const Params& p, const double2* a, const double2* b, float2* fa,
                           float2* fb, cudaStream_t st);  // a/fa may be null

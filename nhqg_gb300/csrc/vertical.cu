@@ -122,15 +122,27 @@ __global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const doubl
   }
 }
 
-// Chebyshev coefficients (FP64 tile out) of the nodal explicit operand A,
-// read in FP64 (Ad) or FP32 (Af, inverse DCT in FP32); tmp is a free tile.
-template <bool F32A, typename DS>
+// form of the explicit operand A that k_vback reads
+enum AKind {
+  AK_F64 = 0,       // FP64 nodal values (plain path)
+  AK_F32_NODAL = 1, // FP32 nodal values, inverse DCT in FP32
+  AK_F32_COEF = 2,  // FP32 Chebyshev coefficients (tensor-core inverse ran before)
+};
+
+// Chebyshev coefficients (FP64 tile out) of the explicit operand A, read in
+// the form AK; tmp is a free tile.
+template <int AK, typename DS>
 __device__ __forceinline__ void a_to_coef(const VK& k, const DS& ds, const double2* Ad,
                                           const float2* Af, double2* tmp, double2* out, int m0) {
-  if constexpr (!F32A) {
+  if constexpr (AK == AK_F64) {
     tload(tmp, Ad, k.P, m0, k.M);
     __syncthreads();
     tdct(out, tmp, k.dct, ds, true, k.P);
+  } else if constexpr (AK == AK_F32_COEF) {
+    float2* fi = reinterpret_cast<float2*>(tmp);
+    tload(fi, Af, k.P, m0, k.M);
+    __syncthreads();
+    tcvt(out, fi, k.P);
   } else {
     float2* fi = reinterpret_cast<float2*>(tmp);
     float2* fo = fi + k.P * TM;
@@ -143,20 +155,21 @@ __device__ __forceinline__ void a_to_coef(const VK& k, const DS& ds, const doubl
 }
 
 // =========================================================== back + stage + solve-pre
-template <int MODE, bool F32A>
+template <int MODE, int AK>
 __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   extern __shared__ double2 sm[];
   const int PT = k.P * TM;
   double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT, *b4 = sm + 4 * PT;
-  using CA = typename std::conditional<F32A, float2, double2>::type;
-  const col::DctSharedT<CA> ds = col::dct_shared<CA>(k.dct, sm + 5 * PT);
+  using CA = typename std::conditional<AK == AK_F32_NODAL, float2, double2>::type;
+  col::DctSharedT<CA> ds{};
+  if constexpr (AK != AK_F32_COEF) ds = col::dct_shared<CA>(k.dct, sm + 5 * PT);
   const int m0 = blockIdx.x * TM;
   const int P = k.P, G = k.G, M = k.M;
   const size_t Ms = (size_t)M;
 
   // ------------------------------------------------------------- q
   if (MODE != VB_SOLVE) {
-    a_to_coef<F32A>(k, ds, a.Aq, a.Aqf, b0, b1, m0);
+    a_to_coef<AK>(k, ds, a.Aq, a.Aqf, b0, b1, m0);
     __syncthreads();
     // E_q = -Aq - i beta kx psi, psi = -inv_denom * q_state
     const double2* qs = (MODE == VB_STAGE2) ? a.q1 : a.q0;
@@ -226,7 +239,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
 
   // ------------------------------------------------------------- w
   if (MODE != VB_SOLVE) {
-    a_to_coef<F32A>(k, ds, a.Aw, a.Awf, b0, b1, m0);
+    a_to_coef<AK>(k, ds, a.Aw, a.Awf, b0, b1, m0);
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
     __syncthreads();
@@ -280,7 +293,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
 
   // ------------------------------------------------------------- theta
   if (MODE != VB_SOLVE) {
-    if constexpr (!F32A) {
+    if constexpr (AK == AK_F64) {
       tload(b0, a.At, P, m0, M);
       __syncthreads();
       if (a.dtb_nodal != nullptr) {  // legacy evolve_mean: + (dTheta/dZ)_nodal * w_nodal
@@ -292,7 +305,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
       }
       tdct(b1, b0, k.dct, ds, true, P);
     } else {  // the mixed path has no legacy evolve_mean term
-      a_to_coef<true>(k, ds, nullptr, a.Atf, b0, b1, m0);
+      a_to_coef<AK>(k, ds, nullptr, a.Atf, b0, b1, m0);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
@@ -652,10 +665,16 @@ cudaError_t vfwd_t(const Params& p, const Tables& t, const double2* q, const dou
   return cudaGetLastError();
 }
 
-template <int MODE, bool F32A>
+template <int MODE, int AK>
 void vback_t(const VK& k, const VArgs& a, size_t sm, int grid, cudaStream_t st) {
-  cudaFuncSetAttribute(k_vback<MODE, F32A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_vback<MODE, F32A><<<grid, NT, sm, st>>>(k, a);
+  cudaFuncSetAttribute(k_vback<MODE, AK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_vback<MODE, AK><<<grid, NT, sm, st>>>(k, a);
+}
+template <int MODE>
+void vback_ak(int ak, const VK& k, const VArgs& a, size_t sm, int grid, cudaStream_t st) {
+  if (ak == AK_F64) vback_t<MODE, AK_F64>(k, a, sm, grid, st);
+  else if (ak == AK_F32_NODAL) vback_t<MODE, AK_F32_NODAL>(k, a, sm, grid, st);
+  else vback_t<MODE, AK_F32_COEF>(k, a, sm, grid, st);
 }
 
 }  // namespace
@@ -674,23 +693,16 @@ cudaError_t launch_vfwd_f32(const Params& p, const Tables& t, const double2* q, 
 cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st) {
   VK k = make_vk(p, t);
   const bool f32 = a.Aqf != nullptr;
-  const size_t sm = vsmem(p, 5, true, f32 && mode != VB_SOLVE);
+  const int ak = (!f32 || mode == VB_SOLVE) ? AK_F64 : (a.af_coef ? AK_F32_COEF : AK_F32_NODAL);
+  const size_t sm = ak == AK_F32_COEF ? vsmem(p, 5) : vsmem(p, 5, true, ak == AK_F32_NODAL);
   const int g = vgrid(p);
-  if (f32 && (!p.fast_dct || !t.tw_v_f || a.dtb_nodal || !a.Awf || !a.Atf))
-    return cudaErrorInvalidValue;
+  if (f32 && (a.dtb_nodal || !a.Awf || !a.Atf)) return cudaErrorInvalidValue;
+  if (ak == AK_F32_NODAL && (!p.fast_dct || !t.tw_v_f)) return cudaErrorInvalidValue;
   switch (mode) {
-    case VB_RHS:
-      if (f32) vback_t<VB_RHS, true>(k, a, sm, g, st); else vback_t<VB_RHS, false>(k, a, sm, g, st);
-      break;
-    case VB_STAGE1:
-      if (f32) vback_t<VB_STAGE1, true>(k, a, sm, g, st); else vback_t<VB_STAGE1, false>(k, a, sm, g, st);
-      break;
-    case VB_STAGE2:
-      if (f32) vback_t<VB_STAGE2, true>(k, a, sm, g, st); else vback_t<VB_STAGE2, false>(k, a, sm, g, st);
-      break;
-    default:
-      vback_t<VB_SOLVE, false>(k, a, sm, g, st);
-      break;
+    case VB_RHS: vback_ak<VB_RHS>(ak, k, a, sm, g, st); break;
+    case VB_STAGE1: vback_ak<VB_STAGE1>(ak, k, a, sm, g, st); break;
+    case VB_STAGE2: vback_ak<VB_STAGE2>(ak, k, a, sm, g, st); break;
+    default: vback_t<VB_SOLVE, AK_F64>(k, a, sm, g, st); break;
   }
   return cudaGetLastError();
 }

@@ -139,6 +139,29 @@ class Engine:
                       f"nhqg_set_precision({precision!r})")
             self.precision = precision
 
+    @property
+    def tensor_core_vertical(self) -> bool:
+        """True if the mixed path's Chebyshev <-> nodal transforms run on the
+        tensor cores (else the FP32 fast DCT)."""
+        return bool(self.lib.nhqg_get_mixed_vertical(self.handle))
+
+    @tensor_core_vertical.setter
+    def tensor_core_vertical(self, on: bool) -> None:
+        nat.check(self.lib.nhqg_set_mixed_vertical(self.handle, int(bool(on))),
+                  "nhqg_set_mixed_vertical")
+
+    def tc_to_nodal(self, field: int, coef: torch.Tensor, nodal: torch.Tensor) -> None:
+        """Tensor-core _to_nodal of compact coefficients (complex128, field 0 q
+        (Nz+1, M), 1 w / 2 theta (Nz-1, M)) into nodal (Nz+1, M) complex64."""
+        nat.check(self.lib.nhqg_tc_to_nodal(self.handle, int(field), ctypes.c_void_p(coef.data_ptr()),
+                                            ctypes.c_void_p(nodal.data_ptr()), _stream_handle()),
+                  "nhqg_tc_to_nodal")
+
+    def tc_to_coef(self, nodal: torch.Tensor) -> None:
+        """Tensor-core _to_coeffs of compact nodal values (Nz+1, M) complex64, in place."""
+        nat.check(self.lib.nhqg_tc_to_coef(self.handle, ctypes.c_void_p(nodal.data_ptr()),
+                                           _stream_handle()), "nhqg_tc_to_coef")
+
     # ------------------------------------------------------------- entry points
     def step(self, q, w, th, tb, n_steps: int = 1, precision: str = "fp64") -> None:
         self.set_precision(precision)
