@@ -25,17 +25,19 @@
 // Work decomposition.  One CTA owns 128 real columns (64 complex modes; the
 // matrices are real, so real and imaginary parts are independent columns)
 // and every level.  The fold index (K) runs in chunks of 8 (one MMA k-step)
-// through a 4-stage shared-memory ring:
+// through a 4-stage shared-memory ring; per stage
 //   A chunk: E_hi, E_lo, O_hi, O_lo (4 tiles of 128 x 8 TF32), laid out by the
 //     host in the canonical no-swizzle K-major core-matrix order and fetched
-//     by one cp.async.bulk per chunk on the stage's "full" mbarrier;
-//   raw input: 16 rows of the CTA's columns by per-thread cp.async (thread t
-//     copies and later reads column t only);
-//   B chunk: the threads fold, split and store the input in the same order.
-// Thread 0 issues six MMAs per chunk (E and O accumulators, 128 TMEM columns
-// each) and commits them to the stage's "empty" mbarrier, which releases the
-// stage.  The epilogue reads the accumulators with tcgen05.ld (warp w owns
-// TMEM lanes 32w..32w+31) and writes FP32 rows.  Every mbarrier wait is
+//     by one cp.async.bulk on the stage's "full" mbarrier;
+//   B chunk: 16 converter warps (4 groups x 128 columns) fold, split and
+//     store their input rows in the same order, then arrive on the stage's
+//     "ready" mbarrier.  Each converter streams its own input elements into
+//     registers 4 chunks ahead (coalesced across the warp).
+// A control warp owns TMEM; its lane 0 issues the bulk copies and six MMAs
+// per chunk (E and O accumulators, 128 TMEM columns each) and commits them to
+// the stage's "empty" mbarrier, which releases the stage.  The epilogue reads
+// the accumulators with tcgen05.ld (warp w owns TMEM lanes 32(w%4)..+31) and
+// writes FP32 rows through a shared-memory transpose.  Every mbarrier wait is
 // bounded (one second); a wait that runs out sets the timeout bit of the
 // status word, drains the copies and MMAs in flight, frees TMEM and returns.
 #include <algorithm>
@@ -60,7 +62,8 @@ constexpr int kGroups = kThreads / 128;    // thread groups per column (2 fold i
 static_assert(2 * kGroups == 8, "each group converts two fold indices of a chunk");
 constexpr int kTile = kFold * kKc * 4;     // one 128 x 8 TF32 operand tile, bytes
 constexpr int kAB = 4 * kTile;             // hi/lo x even/odd tiles of one chunk
-constexpr int kRaw = 16;                   // input rows per chunk
+constexpr int kAhead = 4;                  // chunks of input prefetched into registers
+static_assert(kAhead == kStages, "the register ring and the stage ring share their index");
 constexpr uint32_t kTmemCols = 256;        // E accumulator [0,128), O [128,256)
 constexpr uint64_t kWaitNs = 1000000000ull;
 constexpr int kXrow = 512;                 // CUDA-core row table (zero-padded)
@@ -78,7 +81,7 @@ constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kCo
                             ((uint32_t)(kFold >> 4) << 24);
 
 template <bool INV>
-__host__ __device__ constexpr int stage_bytes() { return 2 * kAB + kRaw * kCols * (INV ? 4 : 8); }
+__host__ __device__ constexpr int stage_bytes() { return 2 * kAB; }
 template <bool INV>
 constexpr size_t tc_smem() {
   return 1024 + (size_t)kStages * stage_bytes<INV>() + 128 + (kGroups * 128 + kXrow) * sizeof(float);
@@ -127,23 +130,8 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
       "l"(src), "r"(bytes), "r"(mbar)
       : "memory");
 }
-// cp.async of B bytes, or B zero bytes when v is false (nothing is read)
-template <int B>
-__device__ __forceinline__ void cp_async_zfill(uint32_t dst, const void* src, bool v) {
-  static_assert(B == 4 || B == 8, "cp.async size");
-  const uint32_t n = v ? (uint32_t)B : 0u;
-  if constexpr (B == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(n) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(n) : "memory");
-}
 __device__ __forceinline__ void mbar_arrive(uint32_t a) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -240,7 +228,7 @@ struct TcArgs {
 };
 
 template <bool INV>
-__global__ void __launch_bounds__(kThreads + 32, 1) k_tc_vertical(const __grid_constant__ TcArgs a) {
+__global__ void __launch_bounds__(kThreads + 64, 1) k_tc_vertical(const __grid_constant__ TcArgs a) {
   using In = typename std::conditional<INV, float, double>::type;
   constexpr int SB = stage_bytes<INV>();
   extern __shared__ uint8_t tc_smem_raw[];
@@ -248,12 +236,13 @@ __global__ void __launch_bounds__(kThreads + 32, 1) k_tc_vertical(const __grid_c
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kStages * SB);  // full, ready, empty
   uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 3 * kStages);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(slot + 1);
+  volatile int* progress = abort_flag + 1;  // [0] chunks committed, [1] matrix copies issued
   float* red = reinterpret_cast<float*>(sm + kStages * SB + 128);   // [kGroups][kCols]
   float* xr = red + kGroups * kCols;                                 // [kXrow]
 
   const TcField& F = a.f[blockIdx.y];
   const int tid = threadIdx.x;
-  const bool control = tid >= kThreads;  // warp 16: TMEM, bulk copies, MMAs
+  const bool control = tid >= kThreads;  // warp 16: TMEM and MMAs; warp 17: matrix copies
   const int t = tid & (kCols - 1);       // converters: column of the tile
   const int grp = (tid / kCols) & (kGroups - 1);  // fold indices 2 grp, 2 grp + 1 of a chunk
   const int col0 = blockIdx.x * kCols;
@@ -272,9 +261,10 @@ __global__ void __launch_bounds__(kThreads + 32, 1) k_tc_vertical(const __grid_c
       mbar_init(empty0 + 8 * s, 1);
     }
     *abort_flag = 0;
+    progress[0] = progress[1] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (control) {
+  if (tid >= kThreads && tid < kThreads + 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      saddr(slot)),
                  "r"(kTmemCols)
@@ -287,89 +277,78 @@ __global__ void __launch_bounds__(kThreads + 32, 1) k_tc_vertical(const __grid_c
   tc_fence_after();
   const uint32_t tmem = *slot;
 
-  int committed = 0;  // control: chunks whose MMAs were committed
-  int a_issued = 0;   // control: chunks whose A copy was issued
   float xacc = 0.f;   // converters: CUDA-core row, this thread's share of column t
   if (!control) {
-    // raw rows of chunk c that this thread converts, zero-filled outside the
-    // matrix: forward rows 16c + 4grp + q (q = 0..3: even, odd, even, odd),
-    // inverse rows j = 8c + 2grp + q and N - j (q = 0, 1)
-    constexpr int RS = kCols * (int)sizeof(In);
-    constexpr int EB = (int)sizeof(In);
-    auto issue_raw = [&](int c, int s) {
-      const uint32_t dst = sbase + s * SB + 2 * kAB + t * EB;
+    // Input rows of chunk c that this thread converts (column t), loaded
+    // straight into registers kAhead chunks ahead: forward rows 16c + 4grp + q
+    // (q = 0..3: even, odd, even, odd), inverse rows j = 8c + 2grp + h and
+    // N - j (h = 0, 1).  Rows outside the matrix read as zero.
+    In pre[kAhead][4];
+    auto load = [&](int c, In (&v)[4]) {
       if constexpr (!INV) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          const int r = 4 * grp + q, n = 16 * c + r;
-          const bool v = cval && n < K;
-          cp_async_zfill<EB>(dst + r * RS, src + (v ? (size_t)n * ld : 0), v);
+          const int n = 16 * c + 4 * grp + q;
+          v[q] = (cval && n < K) ? __ldcs(src + (size_t)n * ld) : In(0);
         }
       } else {
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          const int r = 2 * grp + q, j = 8 * c + r;
-          const bool vt = cval && j <= H, vb = cval && j < H;
-          cp_async_zfill<EB>(dst + r * RS, src + (vt ? (size_t)j * ld : 0), vt);
-          cp_async_zfill<EB>(dst + (8 + r) * RS, src + (vb ? (size_t)(N - j) * ld : 0), vb);
+        for (int h = 0; h < 2; ++h) {
+          const int j = 8 * c + 2 * grp + h;
+          v[2 * h] = (cval && j <= H) ? __ldcs(src + (size_t)j * ld) : In(0);
+          v[2 * h + 1] = (cval && j < H) ? __ldcs(src + (size_t)(N - j) * ld) : In(0);
         }
       }
     };
-    for (int c = 0; c < kStages; ++c) {
-      if (c < nch) issue_raw(c, c);
-      cp_commit();
-    }
-    for (int c = 0; c < nch; ++c) {
-      const int s = c % kStages;
-      if (*abort_flag) break;
-      // the stage's previous MMAs (chunk c - kStages) must be done before B is rewritten
-      if (c >= kStages && !mbar_wait(empty0 + 8 * s, ((c / kStages) - 1) & 1)) {
-        *abort_flag = 1;
-        break;
-      }
-      cp_wait<kStages - 1>();
-      const In* raw = reinterpret_cast<const In*>(sm + s * SB + 2 * kAB) + t;
-      float ve[2], vo[2];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        if constexpr (!INV) {
-          const int r = 4 * grp + 2 * h, n = 16 * c + r;
-          ve[h] = f64_to_f32_trunc(raw[r * kCols]);
-          vo[h] = f64_to_f32_trunc(raw[(r + 1) * kCols]);
-          xacc = fmaf(xr[n], ve[h], fmaf(xr[n + 1], vo[h], xacc));
-        } else {
-          const int r = 2 * grp + h, j = 8 * c + r;
-          const float top = raw[r * kCols], bot = raw[(8 + r) * kCols];
-          ve[h] = top + bot;  // j == H: bot is zero-filled; beyond H both are
-          vo[h] = top - bot;  // (the odd matrix is zero at and beyond column H)
-          xacc = fmaf(xr[j], top, fmaf(xr[N - j], bot, xacc));
+    for (int d = 0; d < kAhead; ++d)
+      if (d < nch) load(d, pre[d]);
+    for (int c0 = 0; c0 < nch; c0 += kAhead) {
+#pragma unroll
+      for (int d = 0; d < kAhead; ++d) {
+        const int c = c0 + d;  // stage d
+        if (c >= nch || *abort_flag) break;
+        // the stage's previous MMAs (chunk c - kStages) must be done before B is rewritten
+        if (c >= kStages && !mbar_wait(empty0 + 8 * d, ((c / kStages) - 1) & 1)) {
+          *abort_flag = 1;
+          break;
         }
-      }
-      float eh[2], el[2], oh[2], ol[2];
+        float ve[2], vo[2];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        tf32_split_f(ve[h], eh[h], el[h]);
-        tf32_split_f(vo[h], oh[h], ol[h]);
+        for (int h = 0; h < 2; ++h) {
+          if constexpr (!INV) {
+            const int n = 16 * c + 4 * grp + 2 * h;
+            ve[h] = f64_to_f32_trunc(pre[d][2 * h]);
+            vo[h] = f64_to_f32_trunc(pre[d][2 * h + 1]);
+            const float2 x = *reinterpret_cast<const float2*>(xr + n);
+            xacc = fmaf(x.x, ve[h], fmaf(x.y, vo[h], xacc));
+          } else {
+            const int j = 8 * c + 2 * grp + h;
+            const float top = pre[d][2 * h], bot = pre[d][2 * h + 1];
+            ve[h] = top + bot;  // j == H: bot reads zero; beyond H both do
+            vo[h] = top - bot;  // (the odd matrix is zero at and beyond column H)
+            xacc = fmaf(xr[j], top, fmaf(xr[N - j], bot, xacc));
+          }
+        }
+        if (c + kAhead < nch) load(c + kAhead, pre[d]);
+        float eh[2], el[2], oh[2], ol[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          tf32_split_f(ve[h], eh[h], el[h]);
+          tf32_split_f(vo[h], oh[h], ol[h]);
+        }
+        uint8_t* bst = sm + d * SB + kAB + tile_off(t, 2 * grp);
+        *reinterpret_cast<float2*>(bst + 0 * kTile) = make_float2(eh[0], eh[1]);
+        *reinterpret_cast<float2*>(bst + 1 * kTile) = make_float2(el[0], el[1]);
+        *reinterpret_cast<float2*>(bst + 2 * kTile) = make_float2(oh[0], oh[1]);
+        *reinterpret_cast<float2*>(bst + 3 * kTile) = make_float2(ol[0], ol[1]);
+        fence_async_smem();
+        mbar_arrive(ready0 + 8 * d);
       }
-      uint8_t* bst = sm + s * SB + kAB + tile_off(t, 2 * grp);
-      *reinterpret_cast<float2*>(bst + 0 * kTile) = make_float2(eh[0], eh[1]);
-      *reinterpret_cast<float2*>(bst + 1 * kTile) = make_float2(el[0], el[1]);
-      *reinterpret_cast<float2*>(bst + 2 * kTile) = make_float2(oh[0], oh[1]);
-      *reinterpret_cast<float2*>(bst + 3 * kTile) = make_float2(ol[0], ol[1]);
-      if (c + kStages < nch) issue_raw(c + kStages, s);
-      cp_commit();
-      fence_async_smem();
-      mbar_arrive(ready0 + 8 * s);
     }
-    cp_wait<0>();
     red[grp * kCols + t] = xacc;
   } else if (tid == kThreads) {
-    auto issue_A = [&](int c, int s) {
-      const uint32_t fb = full0 + 8 * s;
-      mbar_expect_tx(fb, kAB);
-      bulk_g2s(sbase + s * SB, F.img + (size_t)c * kAB, kAB, fb);
-    };
-    for (; a_issued < kStages && a_issued < nch; ++a_issued) issue_A(a_issued, a_issued);
+    // MMA issuer: both operands of chunk c present -> six MMAs -> release the stage
     for (int c = 0; c < nch; ++c) {
       const int s = c % kStages;
       const uint32_t ph = (c / kStages) & 1;
@@ -387,21 +366,25 @@ __global__ void __launch_bounds__(kThreads + 32, 1) k_tc_vertical(const __grid_c
       tc_mma(tmem + 128, sdesc(a0 + 2 * kTile), sdesc(b0 + 3 * kTile), 1u);     // O_hi B_lo
       tc_mma(tmem + 128, sdesc(a0 + 3 * kTile), sdesc(b0 + 2 * kTile), 1u);     // O_lo B_hi
       tc_commit(empty0 + 8 * s);
-      committed = c + 1;
-      // refill the stage of chunk c-1 once its MMAs are done
-      if (c >= 1 && a_issued < nch) {
-        const int s2 = (c - 1) % kStages;
-        if (!mbar_wait(empty0 + 8 * s2, ((c - 1) / kStages) & 1)) {
-          *abort_flag = 1;
-          break;
-        }
-        issue_A(a_issued, s2);
-        ++a_issued;
-      }
+      progress[0] = c + 1;
     }
-    if (committed == nch && !*abort_flag &&
+    if (progress[0] == nch && !*abort_flag &&
         !mbar_wait(empty0 + 8 * ((nch - 1) % kStages), ((nch - 1) / kStages) & 1))
       *abort_flag = 1;
+  } else if (tid == kThreads + 32) {
+    // matrix producer: chunk c's A into its stage once the stage's previous MMAs are done
+    for (int c = 0; c < nch; ++c) {
+      const int s = c % kStages;
+      if (*abort_flag) break;
+      if (c >= kStages && !mbar_wait(empty0 + 8 * s, ((c / kStages) - 1) & 1)) {
+        *abort_flag = 1;
+        break;
+      }
+      const uint32_t fb = full0 + 8 * s;
+      mbar_expect_tx(fb, kAB);
+      bulk_g2s(sbase + s * SB, F.img + (size_t)c * kAB, kAB, fb);
+      progress[1] = c + 1;
+    }
   }
   __syncthreads();
   const bool ok = !*abort_flag;
@@ -414,26 +397,26 @@ __global__ void __launch_bounds__(kThreads + 32, 1) k_tc_vertical(const __grid_c
     const int warp = tid >> 5, lane = tid & 31;
     const int lq = warp & 3, cc = 32 * (warp >> 2);
     const uint32_t tl = tmem + ((uint32_t)(lq * 32) << 16);
-    float* t1 = reinterpret_cast<float*>(sm) + warp * (2 * 32 * 33);
-    float* t2 = t1 + 32 * 33;
+    float* tt = reinterpret_cast<float*>(sm) + warp * (32 * 33);
     const int nrow = min(32, H - lq * 32);  // valid fold rows of this lane quarter
     float e[32], o[32];
     tc_ld32(tl + cc, e);
     tc_ld32(tl + 128 + cc, o);
-#pragma unroll
-    for (int q = 0; q < 32; ++q) {
-      t1[lane * 33 + q] = INV ? e[q] : e[q] + o[q];
-      t2[lane * 33 + q] = INV ? o[q] : e[q] - o[q];
-    }
-    __syncwarp();
     const int cg = col0 + cc + lane;
-    if (cg < a.ncols) {
-      for (int r = 0; r < nrow; ++r) {
-        const int i = lq * 32 + r;
-        const int r1 = INV ? 2 * i : i, r2 = INV ? 2 * i + 1 : N - i;
-        F.out[(size_t)r1 * ld + cg] = t1[r * 33 + lane];
-        F.out[(size_t)r2 * ld + cg] = t2[r * 33 + lane];
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {  // rows 2i / i, then 2i+1 / N-i
+#pragma unroll
+      for (int q = 0; q < 32; ++q)
+        tt[lane * 33 + q] = INV ? (pass ? o[q] : e[q]) : (pass ? e[q] - o[q] : e[q] + o[q]);
+      __syncwarp();
+      if (cg < a.ncols) {
+        for (int r = 0; r < nrow; ++r) {
+          const int i = lq * 32 + r;
+          const int row = INV ? 2 * i + pass : (pass ? N - i : i);
+          F.out[(size_t)row * ld + cg] = tt[r * 33 + lane];
+        }
       }
+      __syncwarp();
     }
     if (grp == 0 && cval) {
       const float x = ((red[t] + red[kCols + t]) + red[2 * kCols + t]) + red[3 * kCols + t];
@@ -442,14 +425,15 @@ __global__ void __launch_bounds__(kThreads + 32, 1) k_tc_vertical(const __grid_c
   } else if (!ok && tid == kThreads) {
     atomicOr(a.status, 1 << NHQG_STATUS_BIT_TIMEOUT);
     // drain the bulk copies and MMAs still in flight (bounded)
-    for (int cc = committed; cc < a_issued; ++cc)
+    const int committed = progress[0], issued = progress[1];
+    for (int cc = committed; cc < issued; ++cc)
       mbar_wait(full0 + 8 * (cc % kStages), (cc / kStages) & 1);
     if (committed > 0)
       mbar_wait(empty0 + 8 * ((committed - 1) % kStages), ((committed - 1) / kStages) & 1);
   }
   tc_fence_before();
   __syncthreads();
-  if (control) {
+  if (tid >= kThreads && tid < kThreads + 32) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kTmemCols)
@@ -562,7 +546,7 @@ cudaError_t tc_launch(const TcArgs& a, int nf, cudaStream_t st) {
                                        (int)sm);
   if (e != cudaSuccess) return e;
   dim3 grid((a.ncols + kCols - 1) / kCols, nf);
-  k_tc_vertical<INV><<<grid, kThreads + 32, sm, st>>>(a);
+  k_tc_vertical<INV><<<grid, kThreads + 64, sm, st>>>(a);
   return cudaGetLastError();
 }
 }  // namespace
