@@ -123,7 +123,7 @@ class ClockSampler:
 NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # FFMA lanes x 2 flops x max SM clock
 
 
-def kernel_work(name: str, g, launches_per_step: int) -> tuple[float, float, str]:
+def kernel_work(name: str, g, launches_per_step: int, tc: bool = False) -> tuple[float, float, str]:
     """(algorithmic flops, algorithmic DRAM bytes, limiting pipe) per launch of
     one kernel class, for the algorithm the engine runs.
 
@@ -162,7 +162,14 @@ def kernel_work(name: str, g, launches_per_step: int) -> tuple[float, float, str
         nf = 3 if launches_per_step <= 1 else 2  # 3 fields at stage 1, 1 at stage 2
         return nf * dct * M, nf * (field64 + field), pipe
     if name in ("vback_stage1", "vback_stage2"):
-        # 3 inverse DCTs of A (FP32 in the mixed step) + FP64 stage algebra
+        # 3 inverse DCTs of A (FP32 in the mixed step) + FP64 stage algebra.
+        # After the tensor-core inverse (tc) the kernel reads coefficients and
+        # only the stage algebra is left: stencils, G_Z and pinv recurrences and
+        # stage combinations, counted from the kernel's operations (FMA = 2
+        # flops) per level and mode over the three fields: 42 at stage 1, 108
+        # at stage 2.
+        if tc:
+            return (42.0 if name == "vback_stage1" else 108.0) * P * M, 12 * field64, "fp64"
         return 3 * dct * M, 12 * field64, "fp64"
     if name == "shell_solve":
         n_in = len(np.unique(g.imex_shell_row[g.imex_shell_row >= 0]))
@@ -179,6 +186,15 @@ def kernel_work(name: str, g, launches_per_step: int) -> tuple[float, float, str
         return dct * M + 2 * 16.0 * P * M, 4 * field64, "fp64"
     if name == "to_f32":
         return 0.0, 2 * P * M * (16.0 + 8.0), "hbm"
+    # tensor-core vertical transforms: two parity-folded GEMMs of Nz/2 rows
+    # per field, three TF32 split products each (12 (Nz/2) K M flops);
+    # designed HBM-bound: FP64 coefficients in / FP32 nodal out, or FP32 in
+    # and out in place
+    if name == "tc_to_nodal":
+        nf = 3 if launches_per_step <= 1 else 2  # 3 fields at stage 1, 1 at stage 2
+        return nf * 12.0 * (Nz // 2) * P * M, nf * (P * M * 16.0 + P * M * 8.0), "hbm"
+    if name == "tc_to_coef":
+        return 3 * 12.0 * (Nz // 2) * P * M, 3 * 2 * P * M * 8.0, "hbm"
     return 0.0, 0.0, "fp64"
 
 
@@ -300,7 +316,7 @@ def _rel(a, b) -> float:
     return num / den if den > 0 else num
 
 
-def _timed_arm(S, grid, eng, state, precision, args, ws):
+def _timed_arm(S, grid, eng, state, precision, args, ws, label=None):
     """Warm up, then CUDA-event time exactly args.steps steps (one
     step_inplace call, the way run() advances a state) bracketed by barrier +
     synchronize; the NVTX range '<precision>_steps' marks them for profilers.
@@ -313,7 +329,7 @@ def _timed_arm(S, grid, eng, state, precision, args, ws):
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.nvtx.range_push(f"{precision}_steps")
+    torch.cuda.nvtx.range_push(f"{label or precision}_steps")
     e0.record()
     S.step_inplace(state, grid, args.steps, precision=precision)  # one call, as run() drives it
     e1.record()
@@ -334,8 +350,9 @@ def _roofline(prof, grid, steps, peaks):
     """Per kernel class: achieved rate of its limiting pipe against the
     measured peak of that pipe, plus the HBM rate at algorithmic bytes."""
     out = {}
+    tc = "tc_to_coef" in prof
     for name, (n, ms) in prof.items():
-        flops, bytes_, pipe = kernel_work(name, grid, n // max(1, steps))
+        flops, bytes_, pipe = kernel_work(name, grid, n // max(1, steps), tc)
         avg = ms / n
         entry = {"launches": n, "avg_launch_ms": round(avg, 4), "pipe": pipe,
                  "hbm_gbs_at_algorithmic_bytes": round(bytes_ / (avg * 1e-3) / 1e9, 1)}
@@ -398,6 +415,13 @@ def run_ours(args, ws, rank, local):
     clocks.start()
     ms_plain, prof_plain = _timed_arm(S, grid, eng, S.State(*(t.clone() for t in state)), "fp64", args, ws)
     ms_mixed, prof_mixed = _timed_arm(S, grid, eng, state, "mixed", args, ws)
+    tc = eng.tensor_core_vertical
+    ms_dct = None
+    if tc:  # the same mixed step with the vertical transforms on the CUDA cores (FP32 DCT)
+        eng.tensor_core_vertical = False
+        ms_dct, _ = _timed_arm(S, grid, eng, S.State(*(t.clone() for t in state)), "mixed", args, ws,
+                               label="mixed_dct")
+        eng.tensor_core_vertical = True
     clk = clocks.stop()
     finite = all(bool(torch.isfinite(torch.view_as_real(t) if t.is_complex() else t).all()) for t in state)
     value = ws * args.steps / (ms_mixed * 1e-3)
@@ -451,7 +475,7 @@ def run_ours(args, ws, rank, local):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 products/transforms + f64 solves/exchange",
+        "dtype": "f32 products + tf32x3 tensor-core vertical transforms + f64 solves/exchange",
         "data": (f"synthetic: seeded theta' 1e-3 N(0,1) sin(pi Z) (PCG64 seed 0), spun up by "
                  f"{args.spinup} plain FP64 steps"),
         "config": {"workload": workload_name(args.nx, args.nz), "path": "mixed", "Nx": args.nx, "Nz": args.nz,
@@ -462,6 +486,11 @@ def run_ours(args, ws, rank, local):
                        "ms_per_step": round(ms_plain / args.steps, 4),
                        "kernels": shares(prof_plain), "roofline": roof_plain},
         "mixed_over_plain": round(value / value_plain, 3),
+        "vertical_transforms": ("tcgen05 kind::tf32 tensor cores, TF32 hi/lo split operands (3 products), "
+                                "FP32 accumulation" if tc else "FP32 fast DCT-I on the CUDA cores"),
+        "mixed_cuda_core_dct": (None if ms_dct is None else
+                                {"value": round(ws * args.steps / (ms_dct * 1e-3), 4), "unit": "steps/s",
+                                 "ms_per_step": round(ms_dct / args.steps, 4)}),
         "rel_err_vs_plain": {"after_1_step": err1, "increment_1_step": inc1,
                              f"after_{args.err_steps}_steps": errN,
                              f"diagnostics_after_{args.err_steps}_steps": diag_cmp},
