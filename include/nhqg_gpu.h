@@ -226,6 +226,21 @@ enum {
 };
 int nhqg_diagnostics(nhqg_ctx *ctx, const nhqg_state *state, double *out, void *stream);
 
+/* Spectra of a state, unnormalised like the reference's:
+ *   out[0 : 3 n_bins]   energy_spectrum (nhqg/diagnostics.py:80-101) of psi:
+ *                       E_bt, E_bc, E_tot per horizontal shell;
+ *   then (Nz+1) + (Nz-1) + (Nz-1) values: vertical_mode_energy (:583-585)
+ *                       of q_hat, w_hat, th_hat per Chebyshev index;
+ *   then (Nz+1) values: the psi kinetic energy per Chebyshev index,
+ *                       sum_k w_k |k|^2 |psi_n(k)|^2 (w_k the rfft weights).
+ * mode_bin: DEVICE int array of nhqg_mode_count() entries, the shell of each
+ * compact mode (row r = kx index 0..2K with K = Nx/3, rows above K holding
+ * kx = r - (2K+1); column c = ky index 0..K; m = r (K+1) + c) under the
+ * reference's test i dk <= |k| < (i+1) dk, or -1.  out in DEVICE memory,
+ * written stream-ordered.  Needs cc_weights in the descriptor. */
+int nhqg_spectra(nhqg_ctx *ctx, const nhqg_state *state, const int *mode_bin, int n_bins,
+                 double *out, void *stream);
+
 /* Latched device-side status of the last calls (after a stream sync);
  * reset = 1 clears it. */
 int nhqg_get_device_status(nhqg_ctx *ctx, int reset);

@@ -149,6 +149,8 @@ SIGNATURES = {
     "nhqg_profile_enable": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nhqg_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "nhqg_set_mixed_vertical": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "nhqg_spectra": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_void_p]),
     "nhqg_get_mixed_vertical": (ctypes.c_int, [ctypes.c_void_p]),
     "nhqg_tc_to_nodal": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p]),

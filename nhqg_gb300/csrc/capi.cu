@@ -27,6 +27,7 @@ struct nhqg_ctx {
   // 1-D vectors [P]
   double *tb0, *tb1p, *tb1, *tb2p, *tb2, *E1tb, *E2tb, *Itb, *flux, *dtb;
   double* diag_part = nullptr;  // diagnostics block partials
+  double* spec_mode = nullptr;  // spectra: per-mode energies [2*M], allocated on first use
   // mixed-precision path: FP32 nodal inputs and outputs of the horizontal
   // products, allocated by the first nhqg_set_precision(NHQG_PRECISION_MIXED)
   int precision = NHQG_PRECISION_FP64;
@@ -956,6 +957,23 @@ int nhqg_diagnostics(nhqg_ctx* c, const nhqg_state* s, double* out, void* stream
   }
   CK(launch_diag_final(p, c->t, c->diag_part, c->flux, sbp, c->tb0, out, st));
   c->launches += sbp ? 5 : 4;
+  return NHQG_OK;
+}
+
+int nhqg_spectra(nhqg_ctx* c, const nhqg_state* s, const int* mode_bin, int n_bins, double* out,
+                 void* stream) {
+  if (!c || !out || !mode_bin || n_bins <= 0) return NHQG_ERR_BAD_ARG;
+  if (!c->t.cc) return NHQG_ERR_UNSUPPORTED;
+  cudaStream_t st = S(stream);
+  c->launches = 0;
+  if (!c->spec_mode && dalloc(c, &c->spec_mode, 2 * (size_t)c->p.d.M) != cudaSuccess)
+    return NHQG_ERR_CUDA;
+  int rc = gather_state(c, s, st);
+  if (rc) return rc;
+  const Params& p = c->p;
+  CK(launch_vfwd(p, c->t, c->q0, nullptr, nullptr, c->Qn, nullptr, nullptr, st));
+  CK(launch_spectra(p, c->t, c->Qn, c->q0, c->w0, c->t0, mode_bin, n_bins, c->spec_mode, out, st));
+  c->launches += 4;
   return NHQG_OK;
 }
 

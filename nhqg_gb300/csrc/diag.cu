@@ -1,8 +1,9 @@
-// Scalar diagnostics of a state (nhqg/diagnostics.py:597-690, the subset
-// without the shell spectra and budgets): Clenshaw-Curtis depth integrals of
+// Diagnostics of a state.  Scalars (nhqg/diagnostics.py:597-690, the subset
+// without the budgets): Clenshaw-Curtis depth integrals of
 // |psi|^2, |q|^2, |w|^2, |theta|^2, Re(w theta*) and of the barotropic psi
 // per mode, weighted by the half-plane Parseval weights (1 at ky = 0, 2
-// elsewhere in the 2/3 band) and normalised by Nx^4.
+// elsewhere in the 2/3 band) and normalised by Nx^4.  Spectra: the shell
+// energy spectrum and the vertical mode energies (k_spec_*, k_vspec).
 #include "engine.h"
 
 namespace nhqg {
@@ -114,9 +115,94 @@ __global__ void k_diag_final(int nblocks, int P, double norm, const double* __re
   }
 }
 
+// Shell spectra (nhqg/diagnostics.py:80-101): per compact mode the weighted
+// barotropic and depth-integrated psi energies 0.5 w_k |k|^2 |psi_bt|^2 and
+// 0.5 w_k |k|^2 sum_j cc_j |psi_j|^2 (unnormalised, as the reference sums them)
+__global__ void __launch_bounds__(kDiagThreads) k_spec_modes(Dims d, const double* __restrict__ cc,
+                                                             const double* __restrict__ kx,
+                                                             const double* __restrict__ ky,
+                                                             const double* __restrict__ inv_denom,
+                                                             const double2* __restrict__ qn,
+                                                             double* __restrict__ per_mode) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= d.M) return;
+  const double idn = inv_denom[m];
+  double2 pbt = czero();
+  double spsi = 0.0;
+  for (int j = 0; j < d.P; ++j) {
+    const double2 psi = cscale(qn[(size_t)j * d.M + m], -idn);
+    pbt = caxpy(cc[j], psi, pbt);
+    spsi = fma(cc[j], fma(psi.x, psi.x, psi.y * psi.y), spsi);
+  }
+  const double wt = (m % d.Mc == 0) ? 1.0 : 2.0;
+  const double ksq = fma(kx[m], kx[m], ky[m] * ky[m]);
+  per_mode[m] = 0.5 * wt * ksq * fma(pbt.x, pbt.x, pbt.y * pbt.y);
+  per_mode[d.M + m] = 0.5 * wt * ksq * spsi;
+}
+
+// one CTA per shell: sum the modes of the shell in a fixed order
+__global__ void k_spec_bins(int M, const int* __restrict__ bin, const double* __restrict__ per_mode,
+                            int n_bins, double* __restrict__ out) {
+  __shared__ double red[32];
+  const int b = blockIdx.x;
+  double eb = 0.0, et = 0.0;
+  for (int m = threadIdx.x; m < M; m += blockDim.x)
+    if (bin[m] == b) {
+      eb += per_mode[m];
+      et += per_mode[M + m];
+    }
+  eb = block_sum(eb, red);
+  __syncthreads();
+  et = block_sum(et, red);
+  if (threadIdx.x == 0) {
+    out[b] = eb;
+    out[n_bins + b] = et - eb;
+    out[2 * n_bins + b] = et;
+  }
+}
+
+// vertical spectra (nhqg/diagnostics.py:583-585): CTA (n, f) sums over the
+// modes |f_n|^2 for f = q, w, theta (unweighted, as the reference sums the
+// whole rfft array) and w_k |k|^2 |psi_n|^2 for f = 3
+__global__ void k_vspec(Dims d, const double2* __restrict__ q, const double2* __restrict__ w,
+                        const double2* __restrict__ t, const double* __restrict__ kx,
+                        const double* __restrict__ ky, const double* __restrict__ inv_denom,
+                        double* __restrict__ out) {
+  __shared__ double red[32];
+  const int n = blockIdx.x, f = blockIdx.y;
+  const int levels = (f == 1 || f == 2) ? d.G : d.P;
+  if (n >= levels) return;
+  const double2* src = (f == 1) ? w : (f == 2) ? t : q;
+  double acc = 0.0;
+  for (int m = threadIdx.x; m < d.M; m += blockDim.x) {
+    const double2 x = src[(size_t)n * d.M + m];
+    double a2 = fma(x.x, x.x, x.y * x.y);
+    if (f == 3) {
+      const double wt = (m % d.Mc == 0) ? 1.0 : 2.0;
+      const double ksq = fma(kx[m], kx[m], ky[m] * ky[m]);
+      a2 *= wt * ksq * inv_denom[m] * inv_denom[m];
+    }
+    acc += a2;
+  }
+  acc = block_sum(acc, red);
+  const int off = (f == 0) ? 0 : (f == 1) ? d.P : (f == 2) ? d.P + d.G : d.P + 2 * d.G;
+  if (threadIdx.x == 0) out[off + n] = acc;
+}
+
 }  // namespace
 
 int diag_blocks(const Params& p) { return (p.d.M + kDiagThreads - 1) / kDiagThreads; }
+
+cudaError_t launch_spectra(const Params& p, const Tables& t, const double2* qn, const double2* q,
+                           const double2* w, const double2* th, const int* mode_bin, int n_bins,
+                           double* per_mode, double* out, cudaStream_t st) {
+  if (!t.cc || n_bins <= 0) return cudaErrorInvalidValue;
+  k_spec_modes<<<diag_blocks(p), kDiagThreads, 0, st>>>(p.d, t.cc, t.kx, t.ky, t.inv_denom, qn, per_mode);
+  k_spec_bins<<<n_bins, kDiagThreads, 0, st>>>(p.d.M, mode_bin, per_mode, n_bins, out);
+  k_vspec<<<dim3(p.d.P, 4), kDiagThreads, 0, st>>>(p.d, q, w, th, t.kx, t.ky, t.inv_denom,
+                                                    out + 3 * (size_t)n_bins);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_diag_modes(const Params& p, const Tables& t, const double2* qn, const double2* wn,
                               const double2* tn, double* partials, cudaStream_t st) {

@@ -333,5 +333,10 @@ cudaError_t launch_diag_modes(const Params& p, const Tables& t, const double2* q
 cudaError_t launch_diag_final(const Params& p, const Tables& t, const double* partials,
                               const double* flux, bool flux_on_sbp, const double* th_bar,
                               double* out, cudaStream_t st);
+// shell energy spectrum (3 n_bins) then vertical spectra (P, G, G, P) into out;
+// qn: FP64 nodal q; per_mode: 2 M doubles of scratch
+cudaError_t launch_spectra(const Params& p, const Tables& t, const double2* qn, const double2* q,
+                           const double2* w, const double2* th, const int* mode_bin, int n_bins,
+                           double* per_mode, double* out, cudaStream_t st);
 
 }  // namespace nhqg

@@ -219,6 +219,17 @@ class Engine:
                                             _stream_handle()), "nhqg_diagnostics")
         return out
 
+    def spectra(self, q, w, th, tb, mode_bin: torch.Tensor, n_bins: int) -> torch.Tensor:
+        """3 n_bins shell energies then the vertical spectra of q, w, theta and
+        the psi kinetic energy, on the device (layout of nhqg_spectra)."""
+        s = self.state_desc(q, w, th, tb)
+        P, G = int(q.shape[0]), int(w.shape[0])
+        out = torch.empty(3 * n_bins + 2 * P + 2 * G, dtype=torch.float64, device=q.device)
+        nat.check(self.lib.nhqg_spectra(self.handle, ctypes.byref(s), ctypes.c_void_p(mode_bin.data_ptr()),
+                                        int(n_bins), ctypes.c_void_p(out.data_ptr()), _stream_handle()),
+                  "nhqg_spectra")
+        return out
+
     def tiles(self) -> tuple[int, int, int, int]:
         """Horizontal-product tile budgets in KiB (FP64 col, FP64 row, FP32 col,
         FP32 row); 0 = built-in default."""

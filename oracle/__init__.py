@@ -32,4 +32,10 @@ from .nhqg_oracle import (  # noqa: F401
     sponge_product_23,
     compute_diagnostics,
     DIAG_KEYS,
+    energy_spectrum,
+    vertical_mode_energy,
+    high_mode_fraction,
+    psi_ke_vertical_spectrum,
+    shell_bin_index,
+    spectra,
 )

@@ -940,3 +940,94 @@ def compute_diagnostics(state: OracleState, grid: OracleGrid) -> dict:
                vol_avg_tw_dealiased=vol_tw_d, q_rms=np.sqrt(q_sq), w_rms=np.sqrt(w_sq),
                th_rms=np.sqrt(th_sq), th_bar_max=float(np.max(np.abs(tb))))
     return {k: float(v) for k, v in out.items()}
+
+
+# ---------------------------------------------------------------------------
+# Spectra -- nhqg/diagnostics.py:48-101 (energy_spectrum and its helpers) and
+# :583-594 (vertical_mode_energy, high_mode_fraction)
+# ---------------------------------------------------------------------------
+
+def horizontal_rfft_weight(ksq: np.ndarray) -> np.ndarray:
+    """rfft2 Parseval weights: 2 on columns 1..Nk-2, 1 on ky = 0 and the
+    Nyquist column (nhqg/diagnostics.py:48-53)."""
+    Nk = ksq.shape[1]
+    w = np.ones_like(ksq)
+    if Nk > 2:
+        w[:, 1:Nk - 1] = 2.0
+    return w
+
+
+def shell_bins(ksq: np.ndarray, L: float, n_bins: int | None = None):
+    """(|k|, dk, bin centres): dk = 2 pi / L, n_bins = int(k_max / dk) + 1 by
+    default (nhqg/diagnostics.py:56-65)."""
+    k_mag = np.sqrt(ksq)
+    dk = 2.0 * np.pi / L
+    k_max = np.sqrt(np.max(ksq))
+    if n_bins is None:
+        n_bins = int(float(k_max / dk)) + 1
+    return k_mag, dk, np.arange(n_bins) * dk + dk / 2
+
+
+def shell_bin_index(ksq: np.ndarray, L: float, n_bins: int | None = None) -> np.ndarray:
+    """Shell of every mode under the reference's test i dk <= |k| < (i+1) dk
+    (nhqg/diagnostics.py:68-77), -1 where no shell holds the mode."""
+    k_mag, dk, k_bins = shell_bins(ksq, L, n_bins)
+    idx = np.full(ksq.shape, -1, dtype=np.int64)
+    for i in range(k_bins.shape[0]):
+        idx[(k_mag >= i * dk) & (k_mag < (i + 1) * dk)] = i
+    return idx
+
+
+def shell_bin_sum(q: np.ndarray, ksq: np.ndarray, L: float, n_bins: int | None = None):
+    """Sum of a per-mode quantity over each shell (nhqg/diagnostics.py:68-77)."""
+    k_mag, dk, k_bins = shell_bins(ksq, L, n_bins)
+    spec = np.zeros_like(k_bins)
+    for i in range(k_bins.shape[0]):
+        spec[i] = np.sum(np.where((k_mag >= i * dk) & (k_mag < (i + 1) * dk), q, 0.0))
+    return k_bins, spec
+
+
+def energy_spectrum(psi_nodal: np.ndarray, ksq: np.ndarray, cc_weights: np.ndarray, L: float,
+                    n_bins: int | None = None):
+    """Barotropic, baroclinic and total kinetic energy per horizontal shell
+    (k_bins, E_bt, E_bc, E_tot), unnormalised (nhqg/diagnostics.py:80-101)."""
+    psi_bt = np.einsum("j,j...->...", cc_weights, psi_nodal)
+    e_bt = 0.5 * ksq * np.abs(psi_bt) ** 2
+    e_tot = 0.5 * ksq * np.einsum("j,j...->...", cc_weights, np.abs(psi_nodal) ** 2)
+    w = horizontal_rfft_weight(ksq)
+    k_bins, E_bt = shell_bin_sum(e_bt * w, ksq, L, n_bins)
+    _, E_tot = shell_bin_sum(e_tot * w, ksq, L, n_bins)
+    return k_bins, E_bt, E_tot - E_bt, E_tot
+
+
+def vertical_mode_energy(field_hat: np.ndarray) -> np.ndarray:
+    """Sum over the horizontal modes of |f_n|^2 per Chebyshev index
+    (nhqg/diagnostics.py:583-585)."""
+    return np.sum(np.abs(field_hat) ** 2, axis=(1, 2))
+
+
+def high_mode_fraction(spec: np.ndarray, frac: float = 0.25) -> float:
+    """Share of the top max(1, int(n frac)) entries (nhqg/diagnostics.py:588-594)."""
+    n = spec.shape[0]
+    n_tail = max(1, int(n * frac))
+    total = np.sum(spec)
+    return float(np.sum(spec[-n_tail:]) / total) if total > 0 else 0.0
+
+
+def psi_ke_vertical_spectrum(q_hat: np.ndarray, grid: OracleGrid) -> np.ndarray:
+    """psi kinetic energy per Chebyshev index, sum_k w_k |k|^2 |psi_n(k)|^2 with
+    the rfft weights w_k: the vertical-tail measure of the learned-closure study
+    (a reported number in the reference, not one of its functions)."""
+    psi = invert_psi(q_hat, grid.inv_denom)
+    return np.sum(horizontal_rfft_weight(grid.ksq) * grid.ksq * np.abs(psi) ** 2, axis=(1, 2))
+
+
+def spectra(state: OracleState, grid: OracleGrid, n_bins: int | None = None) -> dict:
+    """energy_spectrum of the state's psi and the vertical mode energies of q,
+    w, theta and of the psi kinetic energy."""
+    q, w, th, _ = state
+    psi_n = vmat(grid.V, invert_psi(q, grid.inv_denom))
+    k_bins, E_bt, E_bc, E_tot = energy_spectrum(psi_n, grid.ksq, grid.cc_weights, grid.cfg.L, n_bins)
+    return dict(k_bins=k_bins, E_bt=E_bt, E_bc=E_bc, E_tot=E_tot, q=vertical_mode_energy(q),
+                w=vertical_mode_energy(w), th=vertical_mode_energy(th),
+                psi_ke=psi_ke_vertical_spectrum(q, grid))

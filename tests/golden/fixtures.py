@@ -74,3 +74,13 @@ def load_diagnostics() -> dict:
     the order of ``keys`` (tests/golden/diagnostics.npz)."""
     with np.load(GOLDEN_DIR / "diagnostics.npz") as z:
         return {k: np.array(z[k]) for k in z.files}
+
+
+SPEC_KEYS = ("k_bins", "E_bt", "E_bc", "E_tot", "q", "w", "th")
+
+
+def load_spectra() -> dict:
+    """Reference energy_spectrum and vertical_mode_energy outputs:
+    ``<case>.<state>.<key>`` (tests/golden/spectra.npz)."""
+    with np.load(GOLDEN_DIR / "spectra.npz") as z:
+        return {k: np.array(z[k]) for k in z.files}

@@ -5,6 +5,7 @@ tests)::
 
     python tests/golden/make_golden.py /path/to/NHQG
     python tests/golden/make_golden.py /path/to/NHQG --diagnostics
+    python tests/golden/make_golden.py /path/to/NHQG --spectra
 
 The reference (``nhqg/*.py``, unmodified, read-only) is imported under the
 NumPy stand-in for ``jax`` in ``tests/golden/refshim``.  Every case records
@@ -256,6 +257,48 @@ def diagnostics_main(ref_root: str) -> None:
     print(f"diagnostics: {len(out)} entries")
 
 
+SPEC_KEYS = ("k_bins", "E_bt", "E_bc", "E_tot", "q", "w", "th")
+
+
+def spectra_main(ref_root: str) -> None:
+    """Reference ``energy_spectrum`` of psi at the CGL nodes
+    (nhqg/diagnostics.py:80-101, called as compute_diagnostics' budget path
+    does, with grid.L) and ``vertical_mode_energy`` (:583-585) of q, w, theta
+    at the ``r`` and ``s0`` states of every case -> ``spectra.npz``
+    (``<case>.<state>.<key>``, keys SPEC_KEYS)."""
+    sys.path.insert(0, str(HERE / "refshim"))
+    sys.path.insert(0, ref_root)
+    from nhqg import diagnostics, solver  # noqa: E402
+    from nhqg.config import NHQGConfig  # noqa: E402
+    from nhqg.grid import make_grid  # noqa: E402
+    import jax.numpy as jnp  # the stand-in  # noqa: E402
+
+    global jnp_asarray
+    jnp_asarray = jnp.asarray
+    out = {}
+    for name, over in CASES.items():
+        cfgd = dict(BASE)
+        cfgd.update(over)
+        override = cfgd.pop("_override_eta_sponge", False)
+        grid = make_grid(NHQGConfig(**cfgd))
+        if override:
+            eta_hat, sponge_phys = smooth_eta_sponge(grid)
+            grid = grid._replace(eta_hat=jnp.asarray(eta_hat), sponge_phys=jnp.asarray(sponge_phys))
+        for label, st in (("r", rich_state(grid, solver, seed=0)),
+                          ("s0", theta_init(grid, solver, seed=0))):
+            psi_nodal = solver._to_nodal(solver.invert_psi(st.q_hat, grid.inv_denom), grid.V)
+            k_bins, E_bt, E_bc, E_tot = diagnostics.energy_spectrum(psi_nodal, grid.ksq, grid.cc_weights,
+                                                                    float(grid.L))
+            vals = dict(k_bins=k_bins, E_bt=E_bt, E_bc=E_bc, E_tot=E_tot,
+                        q=diagnostics.vertical_mode_energy(st.q_hat),
+                        w=diagnostics.vertical_mode_energy(st.w_hat),
+                        th=diagnostics.vertical_mode_energy(st.th_hat))
+            for k in SPEC_KEYS:
+                out[f"{name}.{label}.{k}"] = np.asarray(vals[k], dtype=np.float64)
+    np.savez_compressed(HERE / "spectra.npz", **out)
+    print(f"spectra: {len(out)} arrays, {(HERE / 'spectra.npz').stat().st_size / 1024:.0f} KiB")
+
+
 # the reference's own bitwise regression (tests/test_mixed_bc_plumbing.py:99-117):
 # make_initial_state(seed=0, amplitude=1e-3) with JAX's PRNG, then 20 steps
 JAXPRNG_CFG = dict(Nx=32, Nz=16, L=20.0, Ra_tilde=100.0, sigma=1.0, beta=0.0, Ld=float("inf"),
@@ -287,6 +330,8 @@ if __name__ == "__main__":
     root = args[0] if args else "/root/reference"
     if "--diagnostics" in sys.argv:
         diagnostics_main(root)
+    elif "--spectra" in sys.argv:
+        spectra_main(root)
     elif "--jaxprng" in sys.argv:
         jaxprng_main(root)
     else:

@@ -108,3 +108,21 @@ def test_oracle_diagnostics_golden(case):
         ref = gd[f"{case}.{label}"]
         for i, key in enumerate(oracle.DIAG_KEYS):
             assert abs(got[key] - ref[i]) <= 1e-12 * max(abs(ref[i]), 1e-300) + 1e-300, (case, label, key)
+
+
+@pytest.mark.parametrize("case", fixtures.CASES)
+def test_oracle_spectra_golden(case):
+    """Shell and vertical spectra against the reference's energy_spectrum and
+    vertical_mode_energy (tests/golden/spectra.npz, nhqg/diagnostics.py:80-101,
+    583-585): 1e-12 relative to each spectrum's largest entry."""
+    meta, arrays = fixtures.load_case(case)
+    grid = _grid(meta, arrays)
+    gs = fixtures.load_spectra()
+    for label in ("r", "s0"):
+        got = oracle.spectra(oracle.OracleState(*_state(arrays, label)), grid)
+        for key in fixtures.SPEC_KEYS:
+            ref = gs[f"{case}.{label}.{key}"]
+            assert got[key].shape == ref.shape, (case, label, key)
+            scale = max(float(np.max(np.abs(ref))), 1e-300)
+            assert float(np.max(np.abs(got[key] - ref))) <= 1e-12 * scale, (case, label, key)
+        assert 0.0 <= oracle.high_mode_fraction(got["q"]) <= 1.0
