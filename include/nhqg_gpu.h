@@ -45,6 +45,12 @@ enum { NHQG_EXCHANGE_LEGACY = 0, NHQG_EXCHANGE_BALANCED_SBP2 = 1,
        NHQG_EXCHANGE_BALANCED_SBP2_PC = 2 };
 enum { NHQG_WBC_DIRICHLET = 0, NHQG_WBC_NEUMANN = 1 };
 enum { NHQG_PRECISION_FP64 = 0, NHQG_PRECISION_MIXED = 1 };
+/* imex_scheme (nhqg/config.py:45).  As in the reference's dispatch
+ * (nhqg/solver.py:1228-1242) the scheme selects the stepper only with the
+ * legacy exchange; the balanced SBP2 exchanges run their own stage-wise
+ * stepper with the grid's gamma.  RK443 runs in FP64 (NHQG_PRECISION_MIXED
+ * steps return NHQG_ERR_UNSUPPORTED). */
+enum { NHQG_SCHEME_ARS222 = 0, NHQG_SCHEME_RK443 = 1 };
 
 /*
  * Host-side description of a Grid (nhqg/grid.py:29-141 Grid fields, built by
@@ -88,6 +94,10 @@ typedef struct nhqg_grid_desc {
   const double *cc_weights;                    /* (P,) Clenshaw-Curtis weights on
                                                   [0,1]; NULL disables
                                                   nhqg_diagnostics */
+  int imex_scheme;                             /* NHQG_SCHEME_*; gamma_imex and the
+                                                  shell tables must be the
+                                                  scheme's (1 - 1/sqrt 2 for
+                                                  ARS222, 1/2 for RK443) */
 } nhqg_grid_desc;
 
 typedef struct nhqg_ctx nhqg_ctx;

@@ -39,6 +39,7 @@ CLOSURE = {"fixed_conduction": 0, "evolve_mean": 1}
 EXCHANGE = {"legacy": 0, "balanced_sbp2": 1, "balanced_sbp2_pc": 2}
 WBC = {"dirichlet": 0, "neumann": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
+SCHEME = {"ars222": 0, "rk443": 1}
 DIAG_KEYS = ("KE_bt", "KE_bc", "KE_tot", "enstrophy", "Nusselt", "Nusselt_dealiased",
              "vol_avg_tw", "vol_avg_tw_dealiased", "q_rms", "w_rms", "th_rms", "th_bar_max")
 
@@ -113,6 +114,7 @@ class GridDesc(ctypes.Structure):
         ("proj_dirichlet", c_double_p), ("sbp_D1", c_double_p), ("sbp_L", c_double_p),
         ("cgl_to_sbp", c_double_p), ("sbp_to_cgl", c_double_p), ("mean_solve", c_double_p),
         ("shell_coef", c_double_p), ("cc_weights", c_double_p),
+        ("imex_scheme", ctypes.c_int),
     ]
 
 

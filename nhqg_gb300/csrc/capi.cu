@@ -28,6 +28,12 @@ struct nhqg_ctx {
   double *tb0, *tb1p, *tb1, *tb2p, *tb2, *E1tb, *E2tb, *Itb, *flux, *dtb;
   double* diag_part = nullptr;  // diagnostics block partials
   double* spec_mode = nullptr;  // spectra: per-mode energies [2*M], allocated on first use
+  // ARS(4,4,3) (scheme RK443, legacy exchange): explicit E_0..E_3 and implicit
+  // K_1..K_4 derivatives of (q, w, theta) [P*M] and of th_bar [P]
+  double2* rkE[4][3] = {};
+  double2* rkK[4][3] = {};
+  double* rkEtb[4] = {};
+  double* rkKtb[4] = {};
   // mixed-precision path: FP32 nodal inputs and outputs of the horizontal
   // products, allocated by the first nhqg_set_precision(NHQG_PRECISION_MIXED)
   int precision = NHQG_PRECISION_FP64;
@@ -148,6 +154,8 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
       !g->cgl_to_sbp || !g->sbp_to_cgl)
     return NHQG_ERR_BAD_ARG;
   if (g->eta_hat && !g->eta_phys) return NHQG_ERR_BAD_ARG;
+  if (g->imex_scheme != NHQG_SCHEME_ARS222 && g->imex_scheme != NHQG_SCHEME_RK443)
+    return NHQG_ERR_BAD_ARG;
 
   nhqg_ctx* c = new (std::nothrow) nhqg_ctx();
   if (!c) return NHQG_ERR_BAD_ARG;
@@ -165,6 +173,7 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   p.beta = g->beta; p.eps_sq = g->eps_sq;
   p.has_eta = g->eta_hat != nullptr;
   p.has_sponge = g->sponge_phys != nullptr;
+  p.scheme = g->imex_scheme;
   const Dims& d = p.d;
   const int P = d.P, G = d.G, N = d.Nz, M = d.M;
   int rc = NHQG_OK;
@@ -454,6 +463,21 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     if (dalloc(c, f, fe) != cudaSuccess) return fail(NHQG_ERR_CUDA);
     if (cudaMemset(*f, 0, fe * sizeof(double2)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
   }
+  if (p.scheme == NHQG_SCHEME_RK443 && p.exchange == NHQG_EXCHANGE_LEGACY) {
+    for (int s = 0; s < 4; ++s) {
+      for (int f = 0; f < 3; ++f) {
+        if (dalloc(c, &c->rkE[s][f], fe) != cudaSuccess || dalloc(c, &c->rkK[s][f], fe) != cudaSuccess)
+          return fail(NHQG_ERR_CUDA);
+      }
+      if (dalloc(c, &c->rkEtb[s], (size_t)P) != cudaSuccess ||
+          dalloc(c, &c->rkKtb[s], (size_t)P) != cudaSuccess)
+        return fail(NHQG_ERR_CUDA);
+      // th_bar derivatives stay zero unless the legacy mean closure writes them
+      if (cudaMemset(c->rkEtb[s], 0, P * sizeof(double)) != cudaSuccess ||
+          cudaMemset(c->rkKtb[s], 0, P * sizeof(double)) != cudaSuccess)
+        return fail(NHQG_ERR_CUDA);
+    }
+  }
   double** vecs[] = {&c->tb0, &c->tb1p, &c->tb1, &c->tb2p, &c->tb2, &c->E1tb, &c->E2tb, &c->Itb,
                      &c->flux, &c->dtb};
   for (double** v : vecs) {
@@ -740,9 +764,114 @@ int solve_back(nhqg_ctx* c, double2* qo, double2* wo, double2* to, bool zero_mea
   return NHQG_OK;
 }
 
-// one ARS(2,2,2) step from (q0,w0,t0,tb0); result left in (q0,w0,t0,tb0)
+// ---- ARS(4,4,3) (nhqg/solver.py:1056-1122), gamma = 1/2 in the tables
+// Tableau rows: (coefficient, term) with term 0..3 = K_1..K_4, 4..7 = E_0..E_3;
+// stage i solves y_n + dt * sum(c X) of row i, the last row is y_{n+1}.
+struct RkRow {
+  int n;
+  double c[8];
+  int x[8];
+};
+const RkRow kRk443[5] = {
+    {1, {0.5}, {4}},
+    {3, {1.0 / 6.0, 11.0 / 18.0, 1.0 / 18.0}, {0, 4, 5}},
+    {5, {-0.5, 0.5, 5.0 / 6.0, -5.0 / 6.0, 0.5}, {0, 1, 4, 5, 6}},
+    {7, {1.5, -1.5, 0.5, 0.25, 1.75, 0.75, -1.75}, {0, 1, 2, 4, 5, 6, 7}},
+    {8, {1.5, -1.5, 0.5, 0.5, 0.25, 1.75, 0.75, -1.75}, {0, 1, 2, 3, 4, 5, 6, 7}},
+};
+
+// y_n + dt * (row terms) -> (Q2, W2, T2p, tb2p)
+int rk_combine(nhqg_ctx* c, const RkRow& row, cudaStream_t st) {
+  const Params& p = c->p;
+  const double2* base[3] = {c->q0, c->w0, c->t0};
+  double2* out[3] = {c->Q2, c->W2, c->T2p};
+  const int levels[3] = {p.d.P, p.d.G, p.d.G};
+  for (int f = 0; f < 3; ++f) {
+    LinCombT<double2> a{};
+    a.base = base[f];
+    a.out = out[f];
+    a.n = row.n;
+    a.dt = p.dt;
+    a.count = (size_t)levels[f] * p.d.M;
+    for (int k = 0; k < row.n; ++k) {
+      a.c[k] = row.c[k];
+      a.x[k] = row.x[k] < 4 ? c->rkK[row.x[k]][f] : c->rkE[row.x[k] - 4][f];
+    }
+    PCK("rk_combine", launch_lincomb(a, st));
+  }
+  LinCombT<double> b{};
+  b.base = c->tb0;
+  b.out = c->tb2p;
+  b.n = row.n;
+  b.dt = p.dt;
+  b.count = (size_t)p.d.P;
+  for (int k = 0; k < row.n; ++k) {
+    b.c[k] = row.c[k];
+    b.x[k] = row.x[k] < 4 ? c->rkKtb[row.x[k]] : c->rkEtb[row.x[k] - 4];
+  }
+  PCK("rk_combine", launch_lincomb(b, st));
+  c->launches += 4;
+  return NHQG_OK;
+}
+
+// E_s = explicit_rhs_dispatch(Y) into the RK buffers (legacy exchange)
+int rk_explicit(nhqg_ctx* c, int s, const double2* q, const double2* w, const double2* t,
+                const double* tb, cudaStream_t st) {
+  const bool legacy_mean = c->p.closure == NHQG_CLOSURE_EVOLVE_MEAN;
+  int rc = explicit_front(c, q, w, t, tb, legacy_mean, c->rkEtb[s], nullptr, true, st);
+  if (rc) return rc;
+  if ((rc = closure_front(c, q, st))) return rc;
+  VArgs a = base_vargs(c);
+  a.q0 = q; a.w0 = w; a.t0 = t;
+  a.dtb_nodal = legacy_mean ? c->dtb : nullptr;
+  a.Eq = c->rkE[s][0]; a.Ew = c->rkE[s][1]; a.Et = c->rkE[s][2];
+  PCK("vback_rhs", launch_vback(c->p, c->t, VB_RHS, a, st));
+  c->launches += 1;
+  return NHQG_OK;
+}
+
+int one_step_rk443(nhqg_ctx* c, cudaStream_t st) {
+  const Params& p = c->p;
+  if (mixed(c) || !c->rkE[0][0]) return NHQG_ERR_UNSUPPORTED;
+  const bool evolve = p.closure == NHQG_CLOSURE_EVOLVE_MEAN;
+  int rc = rk_explicit(c, 0, c->q0, c->w0, c->t0, c->tb0, st);
+  if (rc) return rc;
+  for (int i = 1; i <= 4; ++i) {
+    if ((rc = rk_combine(c, kRk443[i - 1], st))) return rc;
+    // Y_i = implicit solve of the combination (imex_implicit_solve, imex_mean_temp_solve)
+    VArgs a = base_vargs(c);
+    a.q0 = c->Q2; a.w0 = c->W2; a.t0 = c->T2p;
+    PCK("vback_solve", launch_vback(p, c->t, VB_SOLVE, a, st));
+    MeanArgs m{};
+    m.tb0 = c->tb2p; m.out = c->tb1; m.stage = 1; m.closure = p.closure;
+    PCK("mean_1d", launch_mean_stage(p, c->t, m, st));
+    c->launches += 2;
+    if ((rc = solve_back(c, c->Q1, c->W1, c->T1, false, st))) return rc;
+    // K_i = implicit_tendency(Y_i) - dissipation (nhqg/solver.py:1002-1009)
+    double2* const* K = c->rkK[i - 1];
+    PCK("itend", launch_itend(p, c->t, c->Q1, c->W1, c->T1, K[0], K[1], K[2], st));
+    PCK("itend", launch_sub_diss(p, K[0], c->Q1, c->t.drq, p.d.P, st));
+    PCK("itend", launch_sub_diss(p, K[1], c->W1, c->t.drw, p.d.G, st));
+    PCK("itend", launch_sub_diss(p, K[2], c->T1, c->t.drt, p.d.G, st));
+    c->launches += 4;
+    if (evolve) {
+      PCK("mean_1d", launch_mean_legacy_rhs(p, c->t, c->tb1, nullptr, nullptr, nullptr, c->rkKtb[i - 1], st));
+      c->launches += 1;
+    }
+    if (i < 4 && (rc = rk_explicit(c, i, c->Q1, c->W1, c->T1, c->tb1, st))) return rc;
+  }
+  if ((rc = rk_combine(c, kRk443[4], st))) return rc;
+  PCK("finalize", launch_finalize(p, c->Q2, c->W2, c->T2p, c->q0, c->w0, c->t0, st));
+  CK(cudaMemcpyAsync(c->tb0, c->tb2p, p.d.P * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  c->launches += 1;
+  return NHQG_OK;
+}
+
+// one step from (q0,w0,t0,tb0); result left in (q0,w0,t0,tb0).  ARS(2,2,2)
+// unless the scheme is RK443 with the legacy exchange (nhqg/solver.py:1228-1242)
 int one_step(nhqg_ctx* c, cudaStream_t st) {
   const Params& p = c->p;
+  if (p.scheme == NHQG_SCHEME_RK443 && p.exchange == NHQG_EXCHANGE_LEGACY) return one_step_rk443(c, st);
   const double dt = p.dt, g = p.gamma_imex;
   const double alpha = g * dt;
   const double delta = -std::sqrt(2.0) / 2.0;

@@ -103,6 +103,7 @@ struct Params {
   int h_col_kib[2], h_row_kib[2];
   // mixed-precision vertical transforms on the tensor cores (else FP32 DCT)
   bool tc_vertical;
+  int scheme;  // NHQG_SCHEME_*
 };
 
 }  // namespace nhqg
@@ -254,6 +255,23 @@ cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, cons
 cudaError_t launch_vfwd_f32(const Params& p, const Tables& t, const double2* q, const double2* w,
                             const double2* th, float2* qn, float2* wn, float2* tn, cudaStream_t st);
 cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs& a, cudaStream_t st);
+// stage combination out = base + dt * sum_k c_k x_k over count elements
+constexpr int kLinCombMax = 8;
+template <typename T>
+struct LinCombT {
+  const T* base;
+  T* out;
+  const T* x[kLinCombMax];
+  double c[kLinCombMax];
+  int n;
+  double dt;
+  size_t count;
+};
+template <typename T>
+cudaError_t launch_lincomb(const LinCombT<T>& a, cudaStream_t st);
+// K -= rate[m] * Y over levels x M compact elements
+cudaError_t launch_sub_diss(const Params& p, double2* K, const double2* Y, const double* rate,
+                            int levels, cudaStream_t st);
 // tensor-core vertical transforms (csrc/tc_vertical.cu).  Host images: false
 // when Nz is odd or above 256, or a matrix lacks the mirror parity.
 bool tc_vertical_images(const nhqg_grid_desc* g, TcHostImage img[4]);

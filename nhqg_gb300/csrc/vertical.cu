@@ -709,6 +709,55 @@ cudaError_t launch_vback(const Params& p, const Tables& t, int mode, const VArgs
 
 namespace {
 
+__device__ __forceinline__ double2 operator*(double a, double2 b) { return make_double2(a * b.x, a * b.y); }
+__device__ __forceinline__ double2 operator+(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+// out = base + dt * (sum_k c_k x_k), the sum taken left to right (the stage
+// combinations of nhqg/solver.py:1066-1119)
+template <typename T>
+__global__ void k_lincomb(LinCombT<T> a) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += stride) {
+    T s = a.c[0] * a.x[0][i];
+    for (int k = 1; k < a.n; ++k) s = s + a.c[k] * a.x[k][i];
+    a.out[i] = a.base[i] + a.dt * s;
+  }
+}
+
+// K -= rate * Y per compact mode (nhqg/solver.py:1002-1009)
+__global__ void k_sub_diss(double2* __restrict__ K, const double2* __restrict__ Y,
+                           const double* __restrict__ rate, int levels, int M) {
+  const size_t n = (size_t)levels * M;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double r = rate[i % M];
+    K[i] = make_double2(K[i].x - r * Y[i].x, K[i].y - r * Y[i].y);
+  }
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_lincomb(const LinCombT<T>& a, cudaStream_t st) {
+  if (a.n < 1 || a.n > kLinCombMax) return cudaErrorInvalidValue;
+  if (a.count == 0) return cudaSuccess;
+  const int blocks = (int)std::min<size_t>((a.count + 255) / 256, 152 * 8);
+  k_lincomb<T><<<blocks, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+template cudaError_t launch_lincomb<double>(const LinCombT<double>&, cudaStream_t);
+template cudaError_t launch_lincomb<double2>(const LinCombT<double2>&, cudaStream_t);
+
+cudaError_t launch_sub_diss(const Params& p, double2* K, const double2* Y, const double* rate,
+                            int levels, cudaStream_t st) {
+  const size_t n = (size_t)levels * p.d.M;
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+  k_sub_diss<<<blocks, 256, 0, st>>>(K, Y, rate, levels, p.d.M);
+  return cudaGetLastError();
+}
+
+namespace {
+
 __global__ void k_to_f32(const double2* __restrict__ a, const double2* __restrict__ b,
                          float2* __restrict__ fa, float2* __restrict__ fb, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;

@@ -87,6 +87,7 @@ class Engine:
         if getattr(g, "imex_shell_coef", None) is not None:
             d.shell_coef = arr("shell_coef", np.ravel(g.imex_shell_coef))
         d.cc_weights = arr("cc_weights", g.cc_weights)
+        d.imex_scheme = nat.SCHEME[g.imex_scheme]
         self._desc = d
         handle = ctypes.c_void_p()
         nat.check(self.lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(handle)), "nhqg_ctx_create")

@@ -212,8 +212,8 @@ def make_grid(cfg: NHQGConfig) -> Grid:
         raise ValueError(f"Unsupported vertical_dealiasing={cfg.vertical_dealiasing!r}")
     if cfg.vertical_cutoff_n is not None:
         raise ValueError("vertical_cutoff_n is not implemented by the GPU time step")
-    if cfg.imex_scheme != "ars222":
-        raise ValueError(f"Unsupported imex_scheme={cfg.imex_scheme!r} (GPU path: 'ars222')")
+    if cfg.imex_scheme not in ("ars222", "rk443"):
+        raise ValueError(f"Unsupported imex_scheme={cfg.imex_scheme!r} (GPU path: 'ars222', 'rk443')")
     if cfg.thermal_closure not in _CLOSURES:
         raise ValueError(f"Unsupported thermal_closure={cfg.thermal_closure!r}")
     if cfg.mean_exchange_discretization not in _EXCHANGES:
@@ -336,7 +336,8 @@ def make_grid(cfg: NHQGConfig) -> Grid:
                 f"energy lies outside the 2/3 band (tolerance 1e-10)")
         sponge_phys = np.fft.irfft2(sig_hat * mask, s=(Nx, Nx))
 
-    gamma_imex = 1.0 - 1.0 / np.sqrt(2.0)
+    # implicit coefficient of the scheme (nhqg/grid.py:671-676)
+    gamma_imex = 1.0 - 1.0 / np.sqrt(2.0) if cfg.imex_scheme == "ars222" else 0.5
     p = cfg.hyper_order
     drq = cfg.nu_q * ksq ** p + cfg.drag
     drw = cfg.nu_w * ksq ** p

@@ -9,7 +9,7 @@ horizontal products under the 2/3 rule in flux or Jacobian form, polar trap
 eta, Rayleigh sponge, Dirichlet or open-top (Neumann) w basis,
 ``q_boundary='none'``, thermal closures ``fixed_conduction`` and
 ``evolve_mean`` with ``legacy`` / ``balanced_sbp2`` / ``balanced_sbp2_pc``
-exchange, ``imex_scheme='ars222'``.
+exchange, ``imex_scheme='ars222'`` and (legacy exchange) ``'rk443'``.
 """
 
 from __future__ import annotations
@@ -282,6 +282,7 @@ class OracleGrid:
     sigma: float
     dt: float
     gamma_imex: float
+    imex_scheme: str
     mean_temp_eps_sq: float
     thermal_closure: str
     mean_exchange_discretization: str
@@ -410,9 +411,12 @@ def make_grid(cfg: OracleConfig, with_shell_inverses: bool = True) -> OracleGrid
             sig_hat = sig_hat * mask
         sponge_phys = np.fft.irfft2(sig_hat, s=(Nx, Nx))
 
-    if cfg.imex_scheme != "ars222":
-        raise NotImplementedError("oracle covers imex_scheme='ars222'")
-    gamma_imex = 1.0 - 1.0 / np.sqrt(2.0)
+    if cfg.imex_scheme == "ars222":  # nhqg/grid.py:671-676
+        gamma_imex = 1.0 - 1.0 / np.sqrt(2.0)
+    elif cfg.imex_scheme == "rk443":
+        gamma_imex = 0.5
+    else:
+        raise NotImplementedError(f"oracle covers imex_scheme 'ars222' and 'rk443', not {cfg.imex_scheme!r}")
     p = cfg.hyper_order
     drq = cfg.nu_q * ksq ** p + cfg.drag
     drw = cfg.nu_w * ksq ** p
@@ -441,7 +445,7 @@ def make_grid(cfg: OracleConfig, with_shell_inverses: bool = True) -> OracleGrid
         inv_alpha_th=inv_at, imex_inv=imex_inv,
         ksq_idx=np.asarray(inv_idx, dtype=np.int32).reshape(Nx, Nk),
         beta=cfg.beta, Ra_sigma=cfg.Ra_tilde / cfg.sigma, sigma=cfg.sigma, dt=dt,
-        gamma_imex=gamma_imex, mean_temp_eps_sq=cfg.mean_temp_eps_sq,
+        gamma_imex=gamma_imex, imex_scheme=cfg.imex_scheme, mean_temp_eps_sq=cfg.mean_temp_eps_sq,
         thermal_closure=cfg.thermal_closure,
         mean_exchange_discretization=cfg.mean_exchange_discretization,
         horizontal_dealiasing=cfg.horizontal_dealiasing,
@@ -827,6 +831,44 @@ def imex_step_ars222(state: OracleState, grid: OracleGrid) -> OracleState:
     return _finalize(OracleState(q2, w2, th2, tb2))
 
 
+def _implicit_with_diss(state: OracleState, impl: OracleState, grid: OracleGrid) -> OracleState:
+    """Implicit derivative including horizontal dissipation (nhqg/solver.py:1002-1009)."""
+    return OracleState(impl.q_hat - grid.diss_rate_q[None] * state.q_hat,
+                       impl.w_hat - grid.diss_rate_w[None] * state.w_hat,
+                       impl.th_hat - grid.diss_rate_th[None] * state.th_hat, impl.th_bar)
+
+
+# ARS(4,4,3) tableau rows as (coefficient, K_j or E_j) pairs, K_j the implicit
+# derivative at stage j (1-based), E_j the explicit one at stage j (0 = y_n)
+RK443_ROWS = (
+    ((0.5, "E0"),),
+    ((1.0 / 6.0, "K1"), (11.0 / 18.0, "E0"), (1.0 / 18.0, "E1")),
+    ((-0.5, "K1"), (0.5, "K2"), (5.0 / 6.0, "E0"), (-5.0 / 6.0, "E1"), (0.5, "E2")),
+    ((1.5, "K1"), (-1.5, "K2"), (0.5, "K3"), (0.25, "E0"), (1.75, "E1"), (0.75, "E2"), (-1.75, "E3")),
+)
+RK443_FINAL = ((1.5, "K1"), (-1.5, "K2"), (0.5, "K3"), (0.5, "K4"), (0.25, "E0"), (1.75, "E1"),
+               (0.75, "E2"), (-1.75, "E3"))
+
+
+def imex_step_rk443(state: OracleState, grid: OracleGrid) -> OracleState:
+    """ARS(4,4,3) IMEX-RK step, gamma = 1/2 in every implicit stage
+    (nhqg/solver.py:1056-1122): y0 + dt * sum(c X) per row, left to right."""
+    dt = grid.dt
+    d = {"E0": explicit_rhs_dispatch(state, grid)}
+
+    def comb(row):
+        return OracleState(*(state[f] + dt * sum(c * d[name][f] for c, name in row) for f in range(4)))
+
+    for i, row in enumerate(RK443_ROWS, start=1):
+        rhs = comb(row)
+        q, w, th = imex_implicit_solve(rhs.q_hat, rhs.w_hat, rhs.th_hat, grid)
+        Y = OracleState(q, w, th, imex_mean_temp_solve(rhs.th_bar, grid))
+        d[f"K{i}"] = _implicit_with_diss(Y, implicit_tendency(Y, grid), grid)
+        if i < 4:
+            d[f"E{i}"] = explicit_rhs_dispatch(Y, grid)
+    return _finalize(comb(RK443_FINAL))
+
+
 def imex_step_balanced_sbp2_pc(state: OracleState, grid: OracleGrid) -> OracleState:
     """Stage-wise predictor/corrector (nhqg/solver.py:1167-1225)."""
     base = _base_grid(grid)
@@ -869,7 +911,7 @@ def imex_step(state: OracleState, grid: OracleGrid) -> OracleState:
         new = _finalize(apply_balanced_sbp2_corrector(
             imex_step_ars222(state, _base_grid(grid)), grid, grid.dt))
     elif m == "legacy":
-        new = imex_step_ars222(state, grid)
+        new = imex_step_rk443(state, grid) if grid.imex_scheme == "rk443" else imex_step_ars222(state, grid)
     else:
         raise NotImplementedError(f"oracle does not cover {m!r}")
     return sanitize_state(new, grid)

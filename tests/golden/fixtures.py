@@ -67,6 +67,8 @@ def state_from(arrays: dict, prefix: str):
 
 
 CASES = ("prod16", "fixed16", "jac16", "polar16", "radix24", "legacy16")
+# ARS(4,4,3) with the legacy exchange (fixed conduction; legacy evolve_mean)
+RK_CASES = ("rk443f16", "rk443l16")
 
 
 def load_diagnostics() -> dict:

@@ -6,6 +6,7 @@ tests)::
     python tests/golden/make_golden.py /path/to/NHQG
     python tests/golden/make_golden.py /path/to/NHQG --diagnostics
     python tests/golden/make_golden.py /path/to/NHQG --spectra
+    python tests/golden/make_golden.py /path/to/NHQG --rk443
 
 The reference (``nhqg/*.py``, unmodified, read-only) is imported under the
 NumPy stand-in for ``jax`` in ``tests/golden/refshim``.  Every case records
@@ -72,6 +73,15 @@ CASES = {
                      mean_exchange_discretization="legacy", mean_temp_eps_sq=0.7),
 }
 
+# ARS(4,4,3) ("rk443", nhqg/solver.py:1056-1122): the reference runs it with
+# the legacy exchange only (nhqg/solver.py:1228-1242), gamma = 1/2 in the
+# shell tables (nhqg/grid.py:671-676)
+RK_CASES = {
+    "rk443f16": dict(Nx=16, Nz=10, imex_scheme="rk443", thermal_closure="fixed_conduction"),
+    "rk443l16": dict(Nx=16, Nz=8, imex_scheme="rk443", thermal_closure="evolve_mean",
+                     mean_exchange_discretization="legacy", mean_temp_eps_sq=0.7),
+}
+
 # grid-only fixture: the polar trap / sponge / open-top tables at a size whose
 # resolution guards pass (production flavour scaled down from 256^2 x 32)
 GRID_CASE = dict(Nx=96, Nz=8, L=40.0, gamma=2.2e-3, trap_r_star=8.0,
@@ -130,7 +140,7 @@ def smooth_eta_sponge(grid):
     return np.fft.rfft2(eta), sigma
 
 
-def main(ref_root: str) -> None:
+def main(ref_root: str, cases: dict | None = None, grid_fixture: bool = True) -> None:
     sys.path.insert(0, str(HERE / "refshim"))
     sys.path.insert(0, ref_root)
     from nhqg import solver  # noqa: E402
@@ -141,7 +151,7 @@ def main(ref_root: str) -> None:
     global jnp_asarray
     jnp_asarray = jnp.asarray
 
-    for name, over in CASES.items():
+    for name, over in (CASES if cases is None else cases).items():
         cfgd = dict(BASE)
         cfgd.update(over)
         override = cfgd.pop("_override_eta_sponge", False)
@@ -201,6 +211,8 @@ def main(ref_root: str) -> None:
         size = (HERE / f"{name}.npz").stat().st_size
         print(f"{name}: {len(out)} arrays, {size / 1024:.0f} KiB")
 
+    if not grid_fixture:
+        return
     cfgd = dict(BASE)
     cfgd.update(GRID_CASE)
     grid = make_grid(NHQGConfig(**cfgd))
@@ -332,6 +344,8 @@ if __name__ == "__main__":
         diagnostics_main(root)
     elif "--spectra" in sys.argv:
         spectra_main(root)
+    elif "--rk443" in sys.argv:
+        main(root, RK_CASES, grid_fixture=False)
     elif "--jaxprng" in sys.argv:
         jaxprng_main(root)
     else:

@@ -30,7 +30,7 @@ def _state(arrays, prefix):
     return OracleState(*fixtures.state_from(arrays, prefix))
 
 
-@pytest.fixture(scope="module", params=fixtures.CASES)
+@pytest.fixture(scope="module", params=fixtures.CASES + fixtures.RK_CASES)
 def case(request):
     meta, arrays = fixtures.load_case(request.param)
     return request.param, meta, arrays, _grid(meta, arrays)
