@@ -435,9 +435,9 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
 
   // ---- tensor-core vertical transforms of the mixed-precision path ----
   if (g->shell_coef) {
-    TcHostImage img[4];
+    TcHostImage img[TC_IMAGES];
     if (tc_vertical_images(g, img)) {
-      for (int i = 0; i < 4; ++i) {
+      for (int i = 0; i < TC_IMAGES; ++i) {
         uint8_t* b = nullptr;
         float* x = nullptr;
         UP(b, img[i].bytes.data(), img[i].bytes.size());
@@ -445,6 +445,7 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
         t.tc.img[i] = b;
         t.tc.xrow[i] = x;
         t.tc.K[i] = img[i].K;
+        t.tc.rows[i] = img[i].rows;
         t.tc.nch[i] = img[i].nch;
       }
       const char* e = getenv("NHQG_TC_VERTICAL");
@@ -614,7 +615,7 @@ int nhqg_tc_to_nodal(nhqg_ctx* c, int field, const void* coef, void* nodal, void
 int nhqg_tc_to_coef(nhqg_ctx* c, void* nodal_inout, void* stream) {
   if (!c || !nodal_inout) return NHQG_ERR_BAD_ARG;
   if (!c->t.tc.img[0]) return NHQG_ERR_UNSUPPORTED;
-  CK(launch_tc_to_coef(c->p, c->t, c->w, static_cast<float2*>(nodal_inout), nullptr, nullptr,
+  CK(launch_tc_to_coef(c->p, c->t, c->w, static_cast<float2*>(nodal_inout), nullptr, nullptr, false,
                        static_cast<cudaStream_t>(stream)));
   return NHQG_OK;
 }
@@ -671,7 +672,7 @@ int horizontal_step_f32(nhqg_ctx* c, const float2* qn, const float2* wn, const f
   a.Aq = c->Aqf; a.Aw = c->Awf; a.Ath = c->Atf;
   CK(launch_horizontal_f32(p, c->t, c->w, a, st, &c->launches));
   if (p.tc_vertical) {  // nodal A -> Chebyshev coefficients on the tensor cores
-    PCK("tc_to_coef", launch_tc_to_coef(p, c->t, c->w, c->Aqf, c->Awf, c->Atf, st));
+    PCK("tc_to_coef", launch_tc_to_coef(p, c->t, c->w, c->Aqf, c->Awf, c->Atf, true, st));
     c->launches += 1;
   }
   return NHQG_OK;

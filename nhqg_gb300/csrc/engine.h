@@ -14,19 +14,27 @@ namespace nhqg {
 constexpr int NHQG_STATUS_BIT_OOB = 0;      // input content outside the 2/3 band
 constexpr int NHQG_STATUS_BIT_TIMEOUT = 1;  // a bounded device wait ran out
 
-// Tensor-core vertical transforms (csrc/tc_vertical.cu): per transform
-// (0 forward q: V, 1 forward w: V S_w, 2 forward theta: V S, 3 inverse V^-1)
-// the parity-folded TF32 hi/lo matrix image in shared-memory order, the
-// CUDA-core row, the input rows K and the number of k-chunks.
+// Tensor-core vertical transforms (csrc/tc_vertical.cu): per transform the
+// parity-folded TF32 hi/lo matrix image in shared-memory order, the CUDA-core
+// row, the input rows K, the output rows and the number of k-chunks.
+enum TcImage {
+  TC_FWD_Q = 0,  // V: Chebyshev q -> nodal
+  TC_FWD_W = 1,  // V S_w: Galerkin w -> nodal
+  TC_FWD_T = 2,  // V S: Galerkin theta -> nodal
+  TC_INV = 3,    // V^-1: nodal -> Chebyshev
+  TC_E_Q = 4,    // -V^-1: nodal A_q -> E_q (Chebyshev)
+  TC_E_G = 5,    // -pinv V^-1: nodal A_w, A_theta -> E_w, E_theta (Galerkin, Dirichlet basis)
+  TC_IMAGES = 6
+};
 struct TcHostImage {
   std::vector<uint8_t> bytes;
   std::vector<float> xrow;
-  int K = 0, nch = 0;
+  int K = 0, rows = 0, nch = 0;
 };
 struct TcTables {
-  const uint8_t* img[4] = {};
-  const float* xrow[4] = {};
-  int K[4] = {}, nch[4] = {};
+  const uint8_t* img[TC_IMAGES] = {};
+  const float* xrow[TC_IMAGES] = {};
+  int K[TC_IMAGES] = {}, rows[TC_IMAGES] = {}, nch[TC_IMAGES] = {};
 };
 
 // Device-resident tables, uploaded once by nhqg_ctx_create.
@@ -274,14 +282,16 @@ cudaError_t launch_sub_diss(const Params& p, double2* K, const double2* Y, const
                             int levels, cudaStream_t st);
 // tensor-core vertical transforms (csrc/tc_vertical.cu).  Host images: false
 // when Nz is odd or above 256, or a matrix lacks the mirror parity.
-bool tc_vertical_images(const nhqg_grid_desc* g, TcHostImage img[4]);
+bool tc_vertical_images(const nhqg_grid_desc* g, TcHostImage img[TC_IMAGES]);
 // FP64 Chebyshev (q) / Galerkin (w, theta) coefficients -> FP32 nodal values
 cudaError_t launch_tc_to_nodal(const Params& p, const Tables& t, const Work& w, const double2* q,
                                const double2* wf, const double2* th, float2* qn, float2* wn,
                                float2* tn, cudaStream_t st);
-// FP32 nodal values -> FP32 Chebyshev coefficients, in place
+// FP32 nodal values -> FP32 Chebyshev coefficients, in place (TC_INV), or
+// with explicit = true the explicit tendencies E_q (Chebyshev, P rows) and
+// E_w, E_theta (Galerkin, G rows) of nodal A_q, A_w, A_theta (TC_E_Q, TC_E_G)
 cudaError_t launch_tc_to_coef(const Params& p, const Tables& t, const Work& w, float2* aq,
-                              float2* aw, float2* at, cudaStream_t st);
+                              float2* aw, float2* at, bool explicit_form, cudaStream_t st);
 // FP64 nodal fields (the corrector's w and theta) -> FP32, P*M elements each
 cudaError_t launch_to_f32(const Params& p, const double2* a, const double2* b, float2* fa,
                           float2* fb, cudaStream_t st);  // a/fa may be null

@@ -219,7 +219,7 @@ struct TcField {
   float* out;          // FP32 [P][ncols] (the inverse writes over its input)
   const uint8_t* img;  // nch * kAB bytes
   const float* xrow;   // CUDA-core row: forward A[N/2][0:K], inverse A[N][0:P]
-  int K, nch;
+  int K, rows, nch;    // input rows, output rows (inverse: P or G), k-chunks
 };
 struct TcArgs {
   TcField f[3];
@@ -413,12 +413,13 @@ __global__ void __launch_bounds__(kThreads + 64, 1) k_tc_vertical(const __grid_c
         for (int r = 0; r < nrow; ++r) {
           const int i = lq * 32 + r;
           const int row = INV ? 2 * i + pass : (pass ? N - i : i);
+          if (INV && row >= F.rows) break;
           F.out[(size_t)row * ld + cg] = tt[r * 33 + lane];
         }
       }
       __syncwarp();
     }
-    if (grp == 0 && cval) {
+    if (grp == 0 && cval && (!INV || F.rows > N)) {
       const float x = ((red[t] + red[kCols + t]) + red[2 * kCols + t]) + red[3 * kCols + t];
       F.out[(size_t)(INV ? N : H) * ld + col] = x;
     }
@@ -486,8 +487,8 @@ void fold_image(const Dense& A, int N, bool inverse, TcHostImage& out) {
         if (2 * f < A.cols) e = A.at(i, 2 * f);
         if (2 * f + 1 < A.cols) o = A.at(i, 2 * f + 1);
       } else {
-        if (f <= H) e = A.at(2 * i, f);
-        if (f < H) o = A.at(2 * i + 1, f);
+        if (f <= H && 2 * i < A.rows) e = A.at(2 * i, f);
+        if (f < H && 2 * i + 1 < A.rows) o = A.at(2 * i + 1, f);
       }
       float hi, lo;
       const int chunk = f / kKc, kk = f % kKc;
@@ -498,14 +499,16 @@ void fold_image(const Dense& A, int N, bool inverse, TcHostImage& out) {
       put(chunk, 2, i, kk, hi);
       put(chunk, 3, i, kk, lo);
     }
-  const int xr = inverse ? N : H;
+  const int xr = inverse ? N : H;  // no CUDA-core row for G-row inverse matrices
+  out.rows = inverse ? A.rows : N + 1;
   out.xrow.assign(kXrow, 0.f);
-  for (int k = 0; k < A.cols; ++k) out.xrow[k] = (float)A.at(xr, k);
+  if (xr < A.rows)
+    for (int k = 0; k < A.cols; ++k) out.xrow[k] = (float)A.at(xr, k);
 }
 
 }  // namespace
 
-bool tc_vertical_images(const nhqg_grid_desc* g, TcHostImage img[4]) {
+bool tc_vertical_images(const nhqg_grid_desc* g, TcHostImage img[TC_IMAGES]) {
   const int N = g->Nz, P = N + 1, G = N - 1;
   // N >= 16 keeps every fold index of the last chunk (< N/2 + 8) inside [0, N]
   if (N % 2 != 0 || N / 2 > kFold || N < 16) return false;
@@ -526,10 +529,19 @@ bool tc_vertical_images(const nhqg_grid_desc* g, TcHostImage img[4]) {
     Sd[(size_t)k * G + k] = -1.0;
     Sd[(size_t)(k + 2) * G + k] = 1.0;
   }
-  const Dense mats[4] = {V, times(std::vector<double>(g->w_stencil, g->w_stencil + (size_t)P * G)),
-                         times(Sd), Vi};
-  for (int i = 0; i < 4; ++i) {
-    const bool inv = i == 3;
+  // explicit-tendency forms: E_q = -V^-1 A_q; E_g = pinv_dir(-V^-1 A_g) with
+  // pinv_dir[g][n] = -1 for n <= g, n = g mod 2 (x_n = x_{n-2} - c_n), so
+  // -pinv_dir V^-1 sums the rows of V^-1 of g's parity up to g
+  Dense Eq{P, P, std::vector<double>((size_t)P * P)};
+  for (size_t i = 0; i < Eq.a.size(); ++i) Eq.a[i] = -Vi.a[i];
+  Dense Eg{G, P, std::vector<double>((size_t)G * P, 0.0)};
+  for (int gg = 0; gg < G; ++gg)
+    for (int n = gg & 1; n <= gg; n += 2)
+      for (int j = 0; j < P; ++j) Eg.a[(size_t)gg * P + j] += Vi.at(n, j);
+  const Dense mats[TC_IMAGES] = {
+      V, times(std::vector<double>(g->w_stencil, g->w_stencil + (size_t)P * G)), times(Sd), Vi, Eq, Eg};
+  for (int i = 0; i < TC_IMAGES; ++i) {
+    const bool inv = i >= TC_INV;
     if (!mirror_ok(mats[i], N, inv)) return false;
     fold_image(mats[i], N, inv, img[i]);
   }
@@ -571,6 +583,7 @@ cudaError_t launch_tc_to_nodal(const Params& p, const Tables& t, const Work& w, 
     f.img = t.tc.img[i];
     f.xrow = t.tc.xrow[i];
     f.K = t.tc.K[i];
+    f.rows = t.tc.rows[i];
     f.nch = t.tc.nch[i];
   }
   if (nf == 0) return cudaSuccess;
@@ -578,8 +591,8 @@ cudaError_t launch_tc_to_nodal(const Params& p, const Tables& t, const Work& w, 
 }
 
 cudaError_t launch_tc_to_coef(const Params& p, const Tables& t, const Work& w, float2* aq,
-                              float2* aw, float2* at, cudaStream_t st) {
-  if (!t.tc.img[3]) return cudaErrorInvalidValue;
+                              float2* aw, float2* at, bool explicit_form, cudaStream_t st) {
+  if (!t.tc.img[TC_INV]) return cudaErrorInvalidValue;
   TcArgs a{};
   a.ncols = 2 * p.d.M;
   a.N = p.d.Nz;
@@ -592,10 +605,12 @@ cudaError_t launch_tc_to_coef(const Params& p, const Tables& t, const Work& w, f
     TcField& f = a.f[nf++];
     f.in = io[i];
     f.out = reinterpret_cast<float*>(io[i]);
-    f.img = t.tc.img[3];
-    f.xrow = t.tc.xrow[3];
-    f.K = t.tc.K[3];
-    f.nch = t.tc.nch[3];
+    const int im = !explicit_form ? TC_INV : (i == 0 ? TC_E_Q : TC_E_G);
+    f.img = t.tc.img[im];
+    f.xrow = t.tc.xrow[im];
+    f.K = t.tc.K[im];
+    f.rows = t.tc.rows[im];
+    f.nch = t.tc.nch[im];
   }
   if (nf == 0) return cudaSuccess;
   return tc_launch<true>(a, nf, st);

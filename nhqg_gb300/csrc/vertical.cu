@@ -29,6 +29,7 @@ using col::NT;
 using col::tload;
 using col::tstore;
 using col::tcvt;
+using col::tload_f2d;
 using col::tmat;
 using col::tstencil_dir;
 using col::tpinv_dir;
@@ -126,7 +127,8 @@ __global__ void __launch_bounds__(NT) k_vfwd(VK k, const double2* q, const doubl
 enum AKind {
   AK_F64 = 0,       // FP64 nodal values (plain path)
   AK_F32_NODAL = 1, // FP32 nodal values, inverse DCT in FP32
-  AK_F32_COEF = 2,  // FP32 Chebyshev coefficients (tensor-core inverse ran before)
+  AK_F32_COEF = 2,  // FP32 explicit tendencies from the tensor-core inverse:
+                    // E_q (Chebyshev), E_w and E_theta (Galerkin, pinv applied)
 };
 
 // Chebyshev coefficients (FP64 tile out) of the explicit operand A, read in
@@ -139,10 +141,7 @@ __device__ __forceinline__ void a_to_coef(const VK& k, const DS& ds, const doubl
     __syncthreads();
     tdct(out, tmp, k.dct, ds, true, k.P);
   } else if constexpr (AK == AK_F32_COEF) {
-    float2* fi = reinterpret_cast<float2*>(tmp);
-    tload(fi, Af, k.P, m0, k.M);
-    __syncthreads();
-    tcvt(out, fi, k.P);
+    tload_f2d(out, Af, k.P, m0, k.M);
   } else {
     float2* fi = reinterpret_cast<float2*>(tmp);
     float2* fo = fi + k.P * TM;
@@ -176,7 +175,7 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
     for (int i = threadIdx.x; i < PT; i += blockDim.x) {
       const int l = i / TM, m = mode_of(i, m0);
       if (m >= M) continue;
-      double2 e = cneg(b1[i]);
+      double2 e = (AK == AK_F32_COEF) ? b1[i] : cneg(b1[i]);
       if (k.beta != 0.0) {
         const double s = k.beta * k.kx[m] * k.inv_denom[m];
         const double2 qv = qs[(size_t)l * Ms + m];
@@ -239,11 +238,15 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
 
   // ------------------------------------------------------------- w
   if (MODE != VB_SOLVE) {
-    a_to_coef<AK>(k, ds, a.Aw, a.Awf, b0, b1, m0);
-    __syncthreads();
-    for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
-    __syncthreads();
-    tpinv_w(k, b2, b1);
+    if constexpr (AK == AK_F32_COEF) {  // E_w in the Galerkin basis
+      tload_f2d(b2, a.Awf, G, m0, M);
+    } else {
+      a_to_coef<AK>(k, ds, a.Aw, a.Awf, b0, b1, m0);
+      __syncthreads();
+      for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
+      __syncthreads();
+      tpinv_w(k, b2, b1);
+    }
     __syncthreads();
     if (MODE == VB_RHS) {
       tstore(b2, a.Ew, G, m0, M);
@@ -304,13 +307,17 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
         __syncthreads();
       }
       tdct(b1, b0, k.dct, ds, true, P);
-    } else {  // the mixed path has no legacy evolve_mean term
+    } else if constexpr (AK == AK_F32_NODAL) {  // the mixed path has no legacy evolve_mean term
       a_to_coef<AK>(k, ds, nullptr, a.Atf, b0, b1, m0);
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
-    __syncthreads();
-    tpinv_dir(b2, b1, G);
+    if constexpr (AK == AK_F32_COEF) {  // E_theta in the Galerkin basis
+      tload_f2d(b2, a.Atf, G, m0, M);
+    } else {
+      __syncthreads();
+      for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
+      __syncthreads();
+      tpinv_dir(b2, b1, G);
+    }
     __syncthreads();
     if (MODE == VB_RHS) {
       tstore(b2, a.Et, G, m0, M);
