@@ -133,7 +133,7 @@ int nhqg_step(nhqg_ctx *ctx, nhqg_state *state, int n_steps, void *stream);
  *     solve stay FP64, the last as an O(Nz) Chebyshev-tau solve per mode
  *     instead of the dense shell inverse.  Not supported
  *     (NHQG_ERR_UNSUPPORTED): legacy evolve_mean (its nodal exchange
- *     product), Nz whose 2*Nz is not 2^a 3^b, Nz > 886, and a descriptor
+ *     product), Nz whose 2*Nz is not 2^a 3^b, and a descriptor
  *     without shell_coef.
  * The first switch to MIXED allocates 6 FP32 fields of (Nz+1) x (2/3-band
  * modes) each. */

@@ -756,7 +756,8 @@ VArgs base_vargs(nhqg_ctx* c) {
 int solve_back(nhqg_ctx* c, double2* qo, double2* wo, double2* to, bool zero_mean, cudaStream_t st) {
   const Params& p = c->p;
   if (mixed(c)) {
-    PCK("tau_solve", launch_tau_solve(p, c->t, c->rhs, wo, st));
+    // scratch: the FP64 explicit operand of the plain path, idle in the mixed step
+    PCK("tau_solve", launch_tau_solve(p, c->t, c->rhs, wo, c->Aq, st));
   } else {
     PCK("shell_solve", launch_shell(p, c->t, c->rhs, wo, st));
   }

@@ -298,7 +298,7 @@ cudaError_t launch_to_f32(const Params& p, const double2* a, const double2* b, f
 // O(N) tau solve of the per-shell w system (the mixed-precision path's
 // replacement for the dense shell inverses)
 cudaError_t launch_tau_solve(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
-                             cudaStream_t st);
+                             double2* scratch, cudaStream_t st);  // scratch: P*M
 // host factorisation of the per-shell tau systems; coef = [n_shells][2] (a, s)
 void build_tau_tables(int Nz, bool open_top, int n_shells, const double* coef,
                       std::vector<double>& tab, std::vector<double>& par, std::vector<double>& uni);

@@ -121,10 +121,11 @@ void build_tau_tables(int N, bool open_top, int n_shells, const double* coef,
 
 namespace {
 
-constexpr int kMB = 16;  // modes per CTA; 4 chains (re/im x parity) per mode
+constexpr int kTauThreads = 256;  // 64 modes per CTA, 4 chains (re/im x parity) per mode
+constexpr int kPF = 8;            // rows per operand prefetch block
 
 struct TK {
-  int N, G, M, LD;
+  int N, G, M;
   bool open_top;
   double g1_0, g1_1;  // first boundary functional at n = 0, 1
   const int* mode_shell;
@@ -132,52 +133,40 @@ struct TK {
   const double *wa, *wb;
 };
 
-// One CTA: kMB modes, 4 kMB threads.  Columns live in shared memory as
-// y[(mode*2 + re/im) * LD + n]; thread t owns chain (mode t/4, re/im, parity).
-__global__ void __launch_bounds__(4 * kMB) k_tau_solve(TK k, const double2* __restrict__ rhs,
-                                                       double2* __restrict__ wout) {
-  extern __shared__ double ybuf[];
-  const int N = k.N, G = k.G, M = k.M, LD = k.LD, P = N + 1;
-  const int m0 = blockIdx.x * kMB;
-  // f = S_w r for n <= N-2 (parallel over levels and modes)
-  for (int idx = threadIdx.x; idx < (N - 1) * kMB; idx += blockDim.x) {
-    const int n = idx / kMB, mm = idx - n * kMB, m = m0 + mm;
-    double fr = 0.0, fi = 0.0;
-    if (m < M) {
-      const double2 r0 = rhs[(size_t)n * M + m];
-      if (!k.open_top) {
-        fr = -r0.x; fi = -r0.y;
-        if (n >= 2) { const double2 r2 = rhs[(size_t)(n - 2) * M + m]; fr += r2.x; fi += r2.y; }
-      } else {
-        fr = r0.x; fi = r0.y;
-        if (n >= 1) {
-          const double2 r1 = rhs[(size_t)(n - 1) * M + m];
-          fr = fma(k.wa[n - 1], r1.x, fr); fi = fma(k.wa[n - 1], r1.y, fi);
-        }
-        if (n >= 2) {
-          const double2 r2 = rhs[(size_t)(n - 2) * M + m];
-          fr = fma(k.wb[n - 2], r2.x, fr); fi = fma(k.wb[n - 2], r2.y, fi);
-        }
-      }
+// Thread t owns chain (compact mode t/4, re/im, parity).  The columns stay in
+// global memory (the per-launch working set, a few tens of MB, lives in L2):
+// element n of a [level][M] complex field viewed as doubles is
+// (n M + m) 2 + re/im.  Without shared-memory columns the occupancy is set by
+// registers, and many chains in flight hide the 64-cycle FP64 latency of the
+// serial recurrences.  y is scratch for the particular solution and then c.
+__global__ void __launch_bounds__(kTauThreads) k_tau_solve(TK k, const double* __restrict__ r,
+                                                           double* __restrict__ y,
+                                                           double* __restrict__ wout) {
+  const int N = k.N, G = k.G, M = k.M, P = N + 1;
+  const int t = blockIdx.x * kTauThreads + threadIdx.x;
+  const int m = t >> 2, ri = (t >> 1) & 1, p = t & 1;
+  // lanes past M run the same warp collectives on zeros and store nothing
+  const bool live = m < M;
+  const int mc = live ? m : 0;
+  auto at = [&](int n) { return ((size_t)n * M + mc) * 2 + ri; };
+  auto rv = [&](int n) { return live ? r[at(n)] : 0.0; };
+  auto f = [&](int n) {  // (S_w r)_n
+    if (!k.open_top) {
+      double v = -rv(n);
+      if (n >= 2) v += rv(n - 2);
+      return v;
     }
-    ybuf[(mm * 2) * LD + n] = fr;
-    ybuf[(mm * 2 + 1) * LD + n] = fi;
-  }
-  __syncthreads();
-
-  // Every lane runs the same sequence of warp collectives (the shuffles and
-  // __syncwarp below); lanes of modes past M compute on their own unused
-  // columns with shell 0 and are never stored.
-  const int t = threadIdx.x;
-  const int mm = t >> 2, ri = (t >> 1) & 1, p = t & 1;
-  const int m = m0 + mm;
-  double* y = ybuf + (mm * 2 + ri) * LD;
+    double v = rv(n);
+    if (n >= 1) v = fma(k.wa[n - 1], rv(n - 1), v);
+    if (n >= 2) v = fma(k.wb[n - 2], rv(n - 2), v);
+    return v;
+  };
   const double* uA = k.uni;
   const double* uB = uA + P;
   const double* uC = uB + P;
   const double* uW1 = uC + P;
   const double* uW2 = uW1 + P;
-  const int sh = (m < M) ? k.mode_shell[m] : 0;
+  const int sh = live ? k.mode_shell[m] : 0;
   const double* rm = k.tab + (size_t)sh * 4 * P;
   const double* Lrm = rm + P;
   const double* cp = Lrm + P;
@@ -185,35 +174,30 @@ __global__ void __launch_bounds__(4 * kMB) k_tau_solve(TK k, const double2* __re
   const double* pr = k.par + (size_t)sh * 8;
   const double ra = pr[0], s4ra = pr[1];
   const bool s_zero = pr[6] != 0.0;
-  const double f0 = y[0], f1 = y[1];
+  const double f0 = f(0), f1 = f(1);
   const double fp = p ? f1 : f0;
-  __syncwarp();
   // Thomas forward and back substitution in the class, then the boundary-row
-  // dot products of the particular solution y
-  // The per-shell tables are scattered L2 reads; each block of kPF rows is
-  // loaded into registers before its dependent chain runs, so the loads of a
-  // block overlap one another instead of each one stalling the chain.
+  // dot products of the particular solution.  Each block of kPF rows loads
+  // its operands before its dependent chain runs.
   double b0 = 0.0, b1 = 0.0;
   if (!s_zero) {
-    constexpr int kPF = 8;
     const int cnt = (N - 2 - p) / 2;  // rows n = p+2, p+4, .., last
     const int last = p + 2 * cnt;
     double d = 0.0;
     for (int r0 = 0; r0 < cnt; r0 += kPF) {
-      double lr[kPF], rr[kPF], yy[kPF];
+      double lr[kPF], ty[kPF];
 #pragma unroll
       for (int q = 0; q < kPF; ++q) {
         const int n = p + 2 + 2 * (r0 + q);
         const bool in = r0 + q < cnt;
         lr[q] = in ? __ldg(Lrm + n) : 0.0;
-        rr[q] = in ? __ldg(rm + n) : 0.0;
-        yy[q] = in ? y[n] : 0.0;
+        ty[q] = in ? f(n) * __ldg(rm + n) : 0.0;
       }
 #pragma unroll
       for (int q = 0; q < kPF; ++q) {
         if (r0 + q < cnt) {
-          d = fma(-lr[q], d, yy[q] * rr[q]);
-          y[p + 2 + 2 * (r0 + q)] = d;
+          d = fma(-lr[q], d, ty[q]);
+          if (live) y[at(p + 2 + 2 * (r0 + q))] = d;
         }
       }
     }
@@ -225,7 +209,7 @@ __global__ void __launch_bounds__(4 * kMB) k_tau_solve(TK k, const double2* __re
         const int n = p + 2 + 2 * (r0 - q);
         const bool in = r0 - q >= 0;
         cc[q] = in ? __ldg(cp + n) : 0.0;
-        yy[q] = in ? y[n] : 0.0;
+        yy[q] = (in && live) ? y[at(n)] : 0.0;
         w1[q] = in ? __ldg(uW1 + n) : 0.0;
         w2[q] = in ? __ldg(uW2 + n) : 0.0;
       }
@@ -234,7 +218,7 @@ __global__ void __launch_bounds__(4 * kMB) k_tau_solve(TK k, const double2* __re
         if (r0 - q >= 0) {
           const int n = p + 2 + 2 * (r0 - q);
           const double v = (n == last) ? yy[q] : fma(-cc[q], nxt, yy[q]);
-          y[n] = v;
+          if (live) y[at(n)] = v;
           nxt = v;
           b0 = fma(w1[q], v, b0);
           b1 = fma(w2[q], v, b1);
@@ -246,67 +230,82 @@ __global__ void __launch_bounds__(4 * kMB) k_tau_solve(TK k, const double2* __re
   b1 += __shfl_xor_sync(0xffffffffu, b1, 1);
   if (s_zero) {
     // A' = a I: c_n = f_n / a for n <= N-2 (the rows the pseudo-inverse reads)
-    for (int n = p; n <= N - 2; n += 2) y[n] *= ra;
+    for (int n = p; n <= N - 2; n += 2)
+      if (live) y[at(n)] = f(n) * ra;
   } else {
     b0 = fma(ra, fma(k.g1_0, f0, k.g1_1 * f1), b0);
     b1 = fma(ra, f0 - f1, b1);
     const double x = -fma(pr[2 + 2 * p], b0, pr[3 + 2 * p] * b1);
-    // e = y + x z on the class (y_p = 0, z_p = 1), then c in place with a
-    // sliding window over e_{n-2}, e_n, e_{n+2}
-    y[p] = x;
-    for (int n = p + 2; n <= N - 2; n += 2) y[n] = fma(x, __ldg(z + n), y[n]);
-    double em2 = 0.0, e0 = y[p];
+    // e = v + x z on the class (e_p = x, z_p = 1), then c in place with a
+    // sliding window over e_{n-2}, e_n, e_{n+2}; e_{n+2} is formed from v_{n+2}
+    // before row n+2 is overwritten
+    double em2 = 0.0, e0 = x;
+#pragma unroll 4
     for (int n = p; n <= N - 2; n += 2) {
-      const double ep2 = (n + 2 <= N - 2) ? y[n + 2] : 0.0;
+      double ep2 = 0.0;
+      if (n + 2 <= N - 2) ep2 = fma(x, __ldg(z + n + 2), live ? y[at(n + 2)] : 0.0);
       double c;
       if (n < 2) c = fma(s4ra, e0, fp * ra);
-      else c = fma(uA[n], em2, fma(uB[n], e0, uC[n] * ep2));
-      y[n] = c;
+      else c = fma(__ldg(uA + n), em2, fma(__ldg(uB + n), e0, __ldg(uC + n) * ep2));
+      if (live) y[at(n)] = c;
       em2 = e0;
       e0 = ep2;
     }
   }
   __syncwarp();
   // w = pinv_w c over n < G (the pseudo-inverse reads c_0 .. c_{N-2})
+  if (!live) return;
   if (!k.open_top) {
-    double w = 0.0;
-    for (int n = p; n < G; n += 2) { w -= y[n]; y[n] = w; }
+    double acc = 0.0;
+    for (int r0 = p; r0 < G; r0 += 2 * kPF) {
+      double cv[kPF];
+#pragma unroll
+      for (int q = 0; q < kPF; ++q) {
+        const int n = r0 + 2 * q;
+        cv[q] = n < G ? y[at(n)] : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < kPF; ++q) {
+        const int n = r0 + 2 * q;
+        if (n < G) {
+          acc -= cv[q];
+          wout[at(n)] = acc;
+        }
+      }
+    }
   } else if (p == 0) {
     double w1 = 0.0, w2 = 0.0;
     for (int n = 0; n < G; ++n) {
-      double w = y[n];
+      double w = y[at(n)];
       if (n >= 1) w = fma(-k.wa[n - 1], w1, w);
       if (n >= 2) w = fma(-k.wb[n - 2], w2, w);
-      y[n] = w;
+      wout[at(n)] = w;
       w2 = w1;
       w1 = w;
     }
-  }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < G * kMB; idx += blockDim.x) {
-    const int n = idx / kMB, j = idx - n * kMB, mj = m0 + j;
-    if (mj < M) wout[(size_t)n * M + mj] = make_double2(ybuf[(j * 2) * LD + n], ybuf[(j * 2 + 1) * LD + n]);
   }
 }
 
 }  // namespace
 
-size_t tau_smem_bytes(int Nz) { return (size_t)kMB * 2 * (Nz + 1) * sizeof(double); }
+size_t tau_smem_bytes(int) { return 0; }
 
 cudaError_t launch_tau_solve(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
-                             cudaStream_t st) {
-  if (!t.tau_tab) return cudaErrorInvalidValue;
+                             double2* scratch, cudaStream_t st) {
+  if (!t.tau_tab || !scratch) return cudaErrorInvalidValue;
   TK k;
-  k.N = p.d.Nz; k.G = p.d.G; k.M = p.d.M; k.LD = p.d.Nz + 1;
+  k.N = p.d.Nz; k.G = p.d.G; k.M = p.d.M;
   k.open_top = t.wst_a != nullptr;
   k.g1_0 = k.open_top ? 0.0 : 1.0;
   k.g1_1 = 1.0;
   k.mode_shell = t.mode_shell;
   k.tab = t.tau_tab; k.par = t.tau_par; k.uni = t.tau_uni;
   k.wa = t.wst_a; k.wb = t.wst_b;
-  const size_t sm = tau_smem_bytes(p.d.Nz);
-  cudaFuncSetAttribute(k_tau_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_tau_solve<<<(k.M + kMB - 1) / kMB, 4 * kMB, sm, st>>>(k, rhs_w, w_out);
+  const size_t threads = 4 * (size_t)k.M;
+  const int blocks = (int)((threads + kTauThreads - 1) / kTauThreads);
+  k_tau_solve<<<blocks, kTauThreads, 0, st>>>(k, reinterpret_cast<const double*>(rhs_w),
+                                               reinterpret_cast<double*>(scratch),
+                                               reinterpret_cast<double*>(w_out));
   return cudaGetLastError();
 }
 
