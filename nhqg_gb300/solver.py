@@ -102,6 +102,60 @@ def imex_step(state, grid: Grid, precision: str = "fp64") -> State:
     return step_inplace(s, grid, 1, check=True, precision=precision)
 
 
+def imex_step_many(states, grid: Grid, precision: str = "fp64", out=None) -> list:
+    """``imex_step`` of each of a sequence of independent states held in host
+    memory, with the host<->device copies overlapped with the steps: step k
+    computes on the current stream while the input of step k+1 is uploaded
+    and the result of step k-1 downloaded on two copy streams (double-buffered
+    device states, ordered by CUDA events).  Inputs in pinned memory let the
+    copies run asynchronously.  Results go to ``out`` (a list of host State
+    tuples of pinned tensors, reused cyclically if shorter than ``states``) or
+    to new pinned tensors; returns the list of results, complete on return.
+    The band-limit status is checked once, after the last step."""
+    states = list(states)
+    if not states:
+        return []
+    eng = engine_for(grid)
+    eng.set_precision(precision)
+    compute = torch.cuda.current_stream()
+    up, down = torch.cuda.Stream(), torch.cuda.Stream()
+    dtypes = (torch.complex128, torch.complex128, torch.complex128, torch.float64)
+    first = [torch.as_tensor(np.asarray(x)) if not isinstance(x, torch.Tensor) else x for x in states[0]]
+    bufs = [State(*(torch.empty(t.shape, dtype=d, device="cuda") for t, d in zip(first, dtypes)))
+            for _ in range(2)]
+    if out is None:
+        out = [tuple(torch.empty(t.shape, dtype=d, pin_memory=True) for t, d in zip(first, dtypes))
+               for _ in range(len(states))]
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_done = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
+    results = []
+    for k, st in enumerate(states):
+        b = k % 2
+        if k >= 2:
+            up.wait_event(ev_out[b])  # buffer b's previous result has left the device
+        with torch.cuda.stream(up):
+            for dst, src, d in zip(bufs[b], st, dtypes):
+                src = src if isinstance(src, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(src))
+                dst.copy_(src.to(dtype=d), non_blocking=True)
+            ev_in[b].record(up)
+        compute.wait_event(ev_in[b])
+        eng.step(*bufs[b], n_steps=1, precision=precision)
+        ev_done[b].record(compute)
+        res = out[k % len(out)]
+        down.wait_event(ev_done[b])
+        with torch.cuda.stream(down):
+            for dst, src in zip(res, bufs[b]):
+                dst.copy_(src, non_blocking=True)
+            ev_out[b].record(down)
+        results.append(res)
+    compute.wait_stream(down)
+    compute.wait_stream(up)
+    torch.cuda.synchronize()
+    _check_band(eng, "imex_step_many")
+    return results
+
+
 def _split(grid: Grid) -> bool:
     return grid.mean_exchange_discretization in ("balanced_sbp2", "balanced_sbp2_pc")
 

@@ -200,3 +200,21 @@ def test_make_initial_state_reference_regression():
     s = S.make_initial_state(g, seed=meta["seed"], amplitude=meta["amplitude"])
     S.step_inplace(s, g, meta["n_steps"], check=True)
     assert_state_close(_host(s), fixtures.state_from(arrays, "sN"), 1e-12, th_bar_abs=1e-18)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_imex_step_many_matches_imex_step(precision):
+    """The pipelined host-state stepping (copies on two streams overlapped with
+    the steps) returns exactly what imex_step returns for each input."""
+    meta, arrays = fixtures.load_case("prod16")
+    g = make_grid(NHQGConfig(**dict(meta["cfg"])))
+    ins = []
+    for label in ("r", "s0", "r1", "r5"):
+        st = fixtures.state_from(arrays, label)
+        ins.append(tuple(torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in st))
+    got = S.imex_step_many(ins, g, precision=precision)
+    assert len(got) == len(ins)
+    for inp, res in zip(ins, got):
+        ref = _host(S.imex_step(inp, g, precision=precision))
+        for a, b in zip(res, ref):
+            np.testing.assert_array_equal(a.numpy(), b)
