@@ -615,12 +615,16 @@ __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const
   const double2* bl = b + (size_t)l * d.M;
   const int chunk = (d.M + kParSeg - 1) / kParSeg;
   const int m0 = seg * chunk, m1 = min(d.M, m0 + chunk);
-  double acc = 0.0;
+  // two FMAs per element on two accumulators (the FP64 pipe, not HBM, bounds
+  // this reduction on GB300); the half-plane weight 2 is applied once
+  double accr = 0.0, acci = 0.0;
 #pragma unroll 4
   for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
     const double2 x = al[m], y = bl[m];
-    acc += 2.0 * fma(x.x, y.x, x.y * y.y);
+    accr = fma(x.x, y.x, accr);
+    acci = fma(x.y, y.y, acci);
   }
+  double acc = 2.0 * (accr + acci);
   // the ky = 0 column: replace the doubled term by the Hermitian projection
   for (int r = threadIdx.x; r < d.Mr; r += blockDim.x) {
     const int m = r * d.Mc;
