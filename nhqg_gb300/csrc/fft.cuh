@@ -92,8 +92,14 @@ struct FftIndex {
   }
 };
 
+// Element i of a sequence sits at i + (i >> PS) when PS > 0: one padding
+// element every 2^PS breaks the power-of-two strides of the late passes
+// across shared-memory banks.
+template <int PS>
+__device__ __forceinline__ int fft_pad(int i) { return PS > 0 ? i + (i >> PS) : i; }
+
 // Forward DFT (sign -1), natural -> reversed.  tw[k] = exp(-2 pi i k / n).
-template <typename C>
+template <typename C, int PS = 0>
 __device__ __forceinline__ void fft_dif_fwd(C* __restrict__ data, int nseq, int stride,
                                             const FftPlan& pl, const C* __restrict__ tw) {
   using T = decltype(C().x);
@@ -107,42 +113,44 @@ __device__ __forceinline__ void fft_dif_fwd(C* __restrict__ data, int nseq, int 
     for (int idx = threadIdx.x; idx < nseq * nb; idx += blockDim.x) {
       int s, blk, j;
       ix.split(idx, s, blk, j);
-      C* a = data + s * stride + blk * L + j;
+      C* const a0 = data + s * stride;
+      const int e = blk * L + j;
+      auto A = [&](int r) -> C& { return a0[fft_pad<PS>(e + r * Ls)]; };
       if (R == 4) {
-        const C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
+        const C x0 = A(0), x1 = A(1), x2 = A(2), x3 = A(3);
         const C t0 = gadd(x0, x2), t1 = gsub(x0, x2), t2 = gadd(x1, x3), t3 = gsub(x1, x3);
         C y1 = gmk<C>(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
         C y2 = gsub(t0, t2);
         C y3 = gmk<C>(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
-        a[0] = gadd(t0, t2);
+        A(0) = gadd(t0, t2);
         if (j != 0) {
           y1 = gmul(y1, tw[j * tws]);
           y2 = gmul(y2, tw[2 * j * tws]);
           y3 = gmul(y3, tw[3 * j * tws]);
         }
-        a[Ls] = y1;
-        a[2 * Ls] = y2;
-        a[3 * Ls] = y3;
+        A(1) = y1;
+        A(2) = y2;
+        A(3) = y3;
       } else if (R == 2) {
-        const C x0 = a[0], x1 = a[Ls];
+        const C x0 = A(0), x1 = A(1);
         C y1 = gsub(x0, x1);
-        a[0] = gadd(x0, x1);
+        A(0) = gadd(x0, x1);
         if (j != 0) y1 = gmul(y1, tw[j * tws]);
-        a[Ls] = y1;
+        A(1) = y1;
       } else {  // R == 3
-        const C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls];
+        const C x0 = A(0), x1 = A(1), x2 = A(2);
         const C sp = gadd(x1, x2);
         const C d = gscale(gsub(x1, x2), (T)kSqrt3Half);
         const C m = gmk<C>(fma((T)-0.5, sp.x, x0.x), fma((T)-0.5, sp.y, x0.y));
         C y1 = gmk<C>(m.x + d.y, m.y - d.x);  // m - i d
         C y2 = gmk<C>(m.x - d.y, m.y + d.x);  // m + i d
-        a[0] = gadd(x0, sp);
+        A(0) = gadd(x0, sp);
         if (j != 0) {
           y1 = gmul(y1, tw[j * tws]);
           y2 = gmul(y2, tw[2 * j * tws]);
         }
-        a[Ls] = y1;
-        a[2 * Ls] = y2;
+        A(1) = y1;
+        A(2) = y2;
       }
     }
     __syncthreads();
@@ -151,7 +159,7 @@ __device__ __forceinline__ void fft_dif_fwd(C* __restrict__ data, int nseq, int 
 }
 
 // Inverse DFT (sign +1, unscaled), reversed -> natural.
-template <typename C>
+template <typename C, int PS = 0>
 __device__ __forceinline__ void fft_dit_inv(C* __restrict__ data, int nseq, int stride,
                                             const FftPlan& pl, const C* __restrict__ tw) {
   using T = decltype(C().x);
@@ -170,26 +178,28 @@ __device__ __forceinline__ void fft_dit_inv(C* __restrict__ data, int nseq, int 
     for (int idx = threadIdx.x; idx < nseq * nb; idx += blockDim.x) {
       int s, blk, j;
       ix.split(idx, s, blk, j);
-      C* a = data + s * stride + blk * L + j;
+      C* const a0 = data + s * stride;
+      const int e = blk * L + j;
+      auto A = [&](int r) -> C& { return a0[fft_pad<PS>(e + r * Ls)]; };
       if (R == 4) {
-        C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls], x3 = a[3 * Ls];
+        C x0 = A(0), x1 = A(1), x2 = A(2), x3 = A(3);
         if (j != 0) {
           x1 = gmulc(x1, tw[j * tws]);
           x2 = gmulc(x2, tw[2 * j * tws]);
           x3 = gmulc(x3, tw[3 * j * tws]);
         }
         const C t0 = gadd(x0, x2), t1 = gsub(x0, x2), t2 = gadd(x1, x3), t3 = gsub(x1, x3);
-        a[0] = gadd(t0, t2);
-        a[Ls] = gmk<C>(t1.x - t3.y, t1.y + t3.x);      // t1 + i t3
-        a[2 * Ls] = gsub(t0, t2);
-        a[3 * Ls] = gmk<C>(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+        A(0) = gadd(t0, t2);
+        A(1) = gmk<C>(t1.x - t3.y, t1.y + t3.x);      // t1 + i t3
+        A(2) = gsub(t0, t2);
+        A(3) = gmk<C>(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
       } else if (R == 2) {
-        C x0 = a[0], x1 = a[Ls];
+        C x0 = A(0), x1 = A(1);
         if (j != 0) x1 = gmulc(x1, tw[j * tws]);
-        a[0] = gadd(x0, x1);
-        a[Ls] = gsub(x0, x1);
+        A(0) = gadd(x0, x1);
+        A(1) = gsub(x0, x1);
       } else {
-        C x0 = a[0], x1 = a[Ls], x2 = a[2 * Ls];
+        C x0 = A(0), x1 = A(1), x2 = A(2);
         if (j != 0) {
           x1 = gmulc(x1, tw[j * tws]);
           x2 = gmulc(x2, tw[2 * j * tws]);
@@ -197,9 +207,9 @@ __device__ __forceinline__ void fft_dit_inv(C* __restrict__ data, int nseq, int 
         const C sp = gadd(x1, x2);
         const C d = gscale(gsub(x1, x2), (T)kSqrt3Half);
         const C m = gmk<C>(fma((T)-0.5, sp.x, x0.x), fma((T)-0.5, sp.y, x0.y));
-        a[0] = gadd(x0, sp);
-        a[Ls] = gmk<C>(m.x - d.y, m.y + d.x);      // m + i d
-        a[2 * Ls] = gmk<C>(m.x + d.y, m.y - d.x);  // m - i d
+        A(0) = gadd(x0, sp);
+        A(1) = gmk<C>(m.x - d.y, m.y + d.x);      // m + i d
+        A(2) = gmk<C>(m.x + d.y, m.y - d.x);  // m - i d
       }
     }
     __syncthreads();

@@ -28,6 +28,7 @@ struct HK {
   using T = decltype(C().x);
   // geometry
   int Nx, Nk, K, Mr, Mc, M;
+  int sx;  // shared-memory stride of one FFT sequence (Nx plus FP32 padding)
   int levels;
   int rows_in, cols_in;  // input plane extent (compact Mr x Mc or full Nx x Nk)
   bool full_in, full_out;
@@ -48,6 +49,12 @@ struct HK {
 
 template <typename C, typename CI>
 __device__ __forceinline__ C to_c(CI v) { C r; r.x = v.x; r.y = v.y; return r; }
+
+// FP32 FFT sequences carry one padding element every 8 (fft_pad) so that the
+// strided late passes spread over the shared-memory banks; the FP64 kernels,
+// bound by the FP64 pipe, keep the dense layout
+template <typename C>
+__host__ __device__ constexpr int pad_shift() { return sizeof(C) == sizeof(float2) ? 3 : 0; }
 
 // H1 -> H2 -> H3 intermediates, pair-major: [field][level][x/2][column][x%2]
 template <typename K>
@@ -81,7 +88,8 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
   const int ncb = min(CB, k.cols_in - c0);
   const int nseq = k.nf1 * CB;
   load_tables(k, tw_s, perm_s);
-  for (int i = threadIdx.x; i < nseq * k.Nx; i += blockDim.x) seq[i] = gmk<C>(T(0), T(0));
+  constexpr int PS = pad_shift<C>();
+  for (int i = threadIdx.x; i < nseq * k.sx; i += blockDim.x) seq[i] = gmk<C>(T(0), T(0));
   __syncthreads();
 
   const size_t plane = (size_t)k.rows_in * k.cols_in;
@@ -92,8 +100,8 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
     const T kxs = k.kx_full[kf] * k.scale;
     const T kys = k.ky_full[c] * k.scale;
     const int pos = perm_s[kf];
-    C* s0 = seq + (size_t)cc * k.Nx + pos;
-    const size_t fs = (size_t)CB * k.Nx;  // stride between fields
+    C* s0 = seq + (size_t)cc * k.sx + fft_pad<PS>(pos);
+    const size_t fs = (size_t)CB * k.sx;  // stride between fields
     if (k.form == HF_SPONGE) {
       s0[0] = gscale(to_c<C>(k.q[off]), k.scale);
       continue;
@@ -132,7 +140,7 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
     }
   }
   __syncthreads();
-  fft_dit_inv(seq, nseq, k.Nx, k.plan, tw_s);
+  fft_dit_inv<C, PS>(seq, nseq, k.sx, k.plan, tw_s);
   // pair-major output: consecutive threads take (x parity, column), so the
   // row pairs H2 reads are contiguous
   const int half = k.Nx / 2;
@@ -141,7 +149,7 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
     const int cc = r2 % ncb, r3 = r2 / ncb;
     const int pp = r3 % half, f = r3 / half;
     const int x = 2 * pp + par;
-    k.x1[xidx(k, f, lev, pp, c0 + cc, k.cols_in) + par] = seq[((size_t)f * CB + cc) * k.Nx + x];
+    k.x1[xidx(k, f, lev, pp, c0 + cc, k.cols_in) + par] = seq[((size_t)f * CB + cc) * k.sx + fft_pad<PS>(x)];
   }
 }
 
@@ -153,12 +161,13 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
   C* tw_s = reinterpret_cast<C*>(smem_raw);
   int* perm_s = reinterpret_cast<int*>(tw_s + k.Nx);
   C* in = reinterpret_cast<C*>(perm_s + ((k.Nx + 3) / 4) * 4);
+  constexpr int PS = pad_shift<C>();
   const int NPR = RB / 2;
-  C* pr = in + (size_t)k.nf1 * NPR * k.Nx;
+  C* pr = in + (size_t)k.nf1 * NPR * k.sx;
   const int lev = blockIdx.y;
   const int x0 = blockIdx.x * RB;
   load_tables(k, tw_s, perm_s);
-  for (int i = threadIdx.x; i < k.nf1 * NPR * k.Nx; i += blockDim.x) in[i] = gmk<C>(T(0), T(0));
+  for (int i = threadIdx.x; i < k.nf1 * NPR * k.sx; i += blockDim.x) in[i] = gmk<C>(T(0), T(0));
   __syncthreads();
   const int half = k.Nx / 2;
   // Hermitian-extended spectra of row pairs (a, b): Z = Xa + i Xb
@@ -169,23 +178,23 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
     const int xa = x0 + 2 * p;
     const size_t base = xidx(k, f, lev, xa >> 1, c, k.cols_in);
     const C A = k.x1[base], B = k.x1[base + 1];
-    C* s = in + ((size_t)f * NPR + p) * k.Nx;
+    C* s = in + ((size_t)f * NPR + p) * k.sx;
     if (c == 0 || c == half) {
-      s[perm_s[c]] = gmk<C>(A.x, B.x);
+      s[fft_pad<PS>(perm_s[c])] = gmk<C>(A.x, B.x);
     } else {
-      s[perm_s[c]] = gmk<C>(A.x - B.y, A.y + B.x);
-      s[perm_s[k.Nx - c]] = gmk<C>(A.x + B.y, B.x - A.y);
+      s[fft_pad<PS>(perm_s[c])] = gmk<C>(A.x - B.y, A.y + B.x);
+      s[fft_pad<PS>(perm_s[k.Nx - c])] = gmk<C>(A.x + B.y, B.x - A.y);
     }
   }
   __syncthreads();
-  fft_dit_inv(in, k.nf1 * NPR, k.Nx, k.plan, tw_s);
+  fft_dit_inv<C, PS>(in, k.nf1 * NPR, k.sx, k.plan, tw_s);
   // pointwise products, two rows per complex lane
-  const size_t fs = (size_t)NPR * k.Nx;
+  const size_t fs = (size_t)NPR * k.sx;
   for (int i = threadIdx.x; i < NPR * k.Nx; i += blockDim.x) {
     const int y = i % k.Nx, p = i / k.Nx;
     const int xa = x0 + 2 * p;
-    const C* s = in + (size_t)p * k.Nx + y;
-    C* o = pr + (size_t)p * k.Nx + y;
+    const C* s = in + (size_t)p * k.sx + fft_pad<PS>(y);
+    C* o = pr + (size_t)p * k.sx + fft_pad<PS>(y);
     T sa = 0, sb = 0, ea = 0, eb = 0;
     if (k.sponge) {
       sa = k.sponge_phys[(size_t)xa * k.Nx + y];
@@ -229,16 +238,16 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
     }
   }
   __syncthreads();
-  fft_dif_fwd(pr, k.nprod * NPR, k.Nx, k.plan, tw_s);
+  fft_dif_fwd<C, PS>(pr, k.nprod * NPR, k.sx, k.plan, tw_s);
   // split the paired spectra, apply i*ky / sponge, write ky <= K
   for (int i = threadIdx.x; i < k.ng * NPR * k.Mc; i += blockDim.x) {
     const int c = i % k.Mc;
     const int rest = i / k.Mc;
     const int p = rest % NPR, g = rest / NPR;
     const int xa = x0 + 2 * p;
-    const int pa = perm_s[c], pb = perm_s[c == 0 ? 0 : k.Nx - c];
+    const int pa = fft_pad<PS>(perm_s[c]), pb = fft_pad<PS>(perm_s[c == 0 ? 0 : k.Nx - c]);
     auto split = [&](int prod, C& Xa, C& Xb) {
-      const C* s = pr + ((size_t)prod * NPR + p) * k.Nx;
+      const C* s = pr + ((size_t)prod * NPR + p) * k.sx;
       const C A = s[pa], B = s[pb];
       Xa = gmk<C>(T(0.5) * (A.x + B.x), T(0.5) * (A.y - B.y));
       Xb = gmk<C>(T(0.5) * (A.y + B.y), T(0.5) * (B.x - A.x));
@@ -281,32 +290,33 @@ __global__ void __launch_bounds__(256) k_h3(HK<C, CI> k, int CB) {
   const int lev = blockIdx.y;
   const int c0 = blockIdx.x * CB;
   const int ncb = min(CB, k.Mc - c0);
+  constexpr int PS = pad_shift<C>();
   load_tables(k, tw_s, perm_s);
   const int half = k.Nx / 2;
   for (int i = threadIdx.x; i < k.ng * ncb * k.Nx; i += blockDim.x) {
     const int par = i & 1, r2 = i >> 1;
     const int cc = r2 % ncb, r3 = r2 / ncb;
     const int pp = r3 % half, g = r3 / half;
-    seq[((size_t)g * CB + cc) * k.Nx + 2 * pp + par] = k.x2[xidx(k, g, lev, pp, c0 + cc, k.Mc) + par];
+    seq[((size_t)g * CB + cc) * k.sx + fft_pad<PS>(2 * pp + par)] = k.x2[xidx(k, g, lev, pp, c0 + cc, k.Mc) + par];
   }
   __syncthreads();
-  fft_dif_fwd(seq, k.ng * CB, k.Nx, k.plan, tw_s);
+  fft_dif_fwd<C, PS>(seq, k.ng * CB, k.sx, k.plan, tw_s);
   const int nout = (k.form == HF_SPONGE) ? 1 : 3;
   for (int i = threadIdx.x; i < k.Mr * ncb; i += blockDim.x) {
     const int r = i / ncb, cc = i - r * ncb, c = c0 + cc;
     const int kf = full_row(r, k.K, k.Nx);
-    const int pos = perm_s[kf];
+    const int pos = fft_pad<PS>(perm_s[kf]);
     const size_t oidx = k.full_out ? ((size_t)lev * k.Nx + kf) * k.Nk + c
                                    : (size_t)lev * k.M + (size_t)r * k.Mc + c;
     for (int f = 0; f < nout; ++f) {
       C val;
       if (k.form == HF_FLUX) {
-        const C G = seq[((size_t)(2 * f) * CB + cc) * k.Nx + pos];
-        const C H = seq[((size_t)(2 * f + 1) * CB + cc) * k.Nx + pos];
+        const C G = seq[((size_t)(2 * f) * CB + cc) * k.sx + pos];
+        const C H = seq[((size_t)(2 * f + 1) * CB + cc) * k.sx + pos];
         const T kx = k.kx_full[kf];
         val = gmk<C>(fma(-kx, G.y, H.x), fma(kx, G.x, H.y));
       } else {
-        val = seq[((size_t)f * CB + cc) * k.Nx + pos];
+        val = seq[((size_t)f * CB + cc) * k.sx + pos];
       }
       C* out = (f == 0) ? k.Aq : (f == 1 ? k.Aw : k.Ath);
       out[oidx] = val;
@@ -324,6 +334,7 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
   HK<C, CI> k;
   const Dims& d = p.d;
   k.Nx = d.Nx; k.Nk = d.Nk; k.K = d.K; k.Mr = d.Mr; k.Mc = d.Mc; k.M = d.M;
+  k.sx = pad_shift<C>() > 0 ? d.Nx + (d.Nx + 7) / 8 : d.Nx;
   k.levels = a.levels;
   k.full_in = a.full_in;
   k.full_out = a.full_out;
@@ -358,19 +369,20 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
   const int pi = sizeof(T) == 8 ? 0 : 1;
   const size_t tile = (size_t)1024 * (p.h_col_kib[pi] > 0 ? p.h_col_kib[pi] : (pi == 0 ? 96 : 44));
   const size_t budget2 = (size_t)1024 * (p.h_row_kib[pi] > 0 ? p.h_row_kib[pi] : (pi == 0 ? 200 : 52));
-  int CB1 = (int)(tile / ((size_t)k.nf1 * d.Nx * sizeof(C)));
+  const size_t seqb = (size_t)k.sx * sizeof(C);  // bytes of one FFT sequence
+  int CB1 = (int)(tile / ((size_t)k.nf1 * seqb));
   CB1 = max(1, min(CB1, k.cols_in));
-  size_t sm1 = tb + (size_t)k.nf1 * CB1 * d.Nx * sizeof(C);
+  size_t sm1 = tb + (size_t)k.nf1 * CB1 * seqb;
   if (sm1 > budget) return cudaErrorInvalidConfiguration;
   int RB = 2;
   while (RB * 2 <= 16 && d.Nx % (RB * 2) == 0 &&
-         tb + (size_t)(k.nf1 + k.nprod) * RB * d.Nx * sizeof(C) <= budget2)
+         tb + (size_t)(k.nf1 + k.nprod) * RB * seqb <= budget2)
     RB *= 2;
-  size_t sm2 = tb + (size_t)(k.nf1 + k.nprod) * (RB / 2) * d.Nx * sizeof(C);
+  size_t sm2 = tb + (size_t)(k.nf1 + k.nprod) * (RB / 2) * seqb;
   if (sm2 > budget) return cudaErrorInvalidConfiguration;
-  int CB3 = (int)(tile / ((size_t)k.ng * d.Nx * sizeof(C)));
+  int CB3 = (int)(tile / ((size_t)k.ng * seqb));
   CB3 = max(1, min(CB3, d.Mc));
-  size_t sm3 = tb + (size_t)k.ng * CB3 * d.Nx * sizeof(C);
+  size_t sm3 = tb + (size_t)k.ng * CB3 * seqb;
   if (sm3 > budget) return cudaErrorInvalidConfiguration;
 
   cudaFuncSetAttribute(k_h1<C, CI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
