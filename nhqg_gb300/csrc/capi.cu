@@ -416,7 +416,7 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.shell_start, start.data(), start.size());
     UP(t.shell_modes, modes.data(), modes.size());
     // per-shell tau factors of the mixed-precision w solve
-    if (g->shell_coef && tau_smem_bytes(N) <= 227 * 1024) {
+    if (g->shell_coef) {
       std::vector<int> mshell(M);
       std::vector<double> coef(2 * (size_t)t.n_shells);
       for (int sidx = 0; sidx < t.n_shells; ++sidx) {

@@ -302,7 +302,6 @@ cudaError_t launch_tau_solve(const Params& p, const Tables& t, const double2* rh
 // host factorisation of the per-shell tau systems; coef = [n_shells][2] (a, s)
 void build_tau_tables(int Nz, bool open_top, int n_shells, const double* coef,
                       std::vector<double>& tab, std::vector<double>& par, std::vector<double>& uni);
-size_t tau_smem_bytes(int Nz);
 cudaError_t launch_shell(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
                          cudaStream_t st);
 cudaError_t launch_vpost(const Params& p, const Tables& t, const double2* Rq, const double2* Rt,

@@ -288,8 +288,6 @@ __global__ void __launch_bounds__(kTauThreads) k_tau_solve(TK k, const double* _
 
 }  // namespace
 
-size_t tau_smem_bytes(int) { return 0; }
-
 cudaError_t launch_tau_solve(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
                              double2* scratch, cudaStream_t st) {
   if (!t.tau_tab || !scratch) return cudaErrorInvalidValue;
