@@ -21,7 +21,10 @@
 namespace nhqg {
 namespace col {
 
-constexpr int TM = 4;    // modes per CTA
+// modes per CTA: 2 keeps five FP64 tiles of a 257-level column at 41 KB, so
+// five CTAs share an SM (4 modes: 82 KB, 2 CTAs, 3% slower mixed step;
+// 1 mode: 2% slower)
+constexpr int TM = 2;
 constexpr int NT = 256;  // threads per CTA
 
 struct Dct {
