@@ -5,7 +5,8 @@ the reference layout: spectral ``(levels, Nx, Nx//2+1)`` complex128 with ky
 contiguous and kx in fftfreq order; ``th_bar`` is ``(Nz+1,)`` float64.
 
 Covered branches (the time-step hot path and its documented variants):
-horizontal products under the 2/3 rule in flux or Jacobian form, polar trap
+horizontal products under the 2/3 rule or the 3/2 rule (zero-padded) in flux
+or Jacobian form, polar trap
 eta, Rayleigh sponge, Dirichlet or open-top (Neumann) w basis,
 ``q_boundary='none'``, thermal closures ``fixed_conduction`` and
 ``evolve_mean`` with ``legacy`` / ``balanced_sbp2`` / ``balanced_sbp2_pc``
@@ -270,6 +271,7 @@ class OracleGrid:
     mask_23: np.ndarray
     eta_hat: np.ndarray | None
     sponge_phys: np.ndarray | None
+    sponge_phys_pad: np.ndarray | None
     diss_rate_q: np.ndarray
     diss_rate_w: np.ndarray
     diss_rate_th: np.ndarray
@@ -391,7 +393,7 @@ def make_grid(cfg: OracleConfig, with_shell_inverses: bool = True) -> OracleGrid
             raise ValueError(f"Trap background PV is under-resolved: {e_out / e_tot:.2e}")
         if cfg.horizontal_dealiasing == "23_rule":
             eta_hat = eta_hat * mask
-    sponge_phys = None
+    sponge_phys = sponge_phys_pad = None
     if cfg.sponge_rate < 0.0:
         raise ValueError("sponge_rate must be >= 0")
     if cfg.sponge_rate > 0.0:
@@ -410,6 +412,9 @@ def make_grid(cfg: OracleConfig, with_shell_inverses: bool = True) -> OracleGrid
         if cfg.horizontal_dealiasing == "23_rule":
             sig_hat = sig_hat * mask
         sponge_phys = np.fft.irfft2(sig_hat, s=(Nx, Nx))
+        # the padded-grid sigma of the 3/2 rule, without the (Npad/Nx)^2
+        # rescale (nhqg/grid.py:663-667)
+        sponge_phys_pad = np.fft.irfft2(_zero_pad(sig_hat, Nx, cfg.Npad), s=(cfg.Npad, cfg.Npad))
 
     if cfg.imex_scheme == "ars222":  # nhqg/grid.py:671-676
         gamma_imex = 1.0 - 1.0 / np.sqrt(2.0)
@@ -440,7 +445,7 @@ def make_grid(cfg: OracleConfig, with_shell_inverses: bool = True) -> OracleGrid
         map_w_to_th=map_w_to_th, map_th_to_w=map_th_to_w, proj_dirichlet=proj_dir,
         proj_neumann=proj_neu, proj_w=proj_w, sbp_D1=D1, sbp_L=Lap,
         cgl_to_sbp=c2s, sbp_to_cgl=s2c, kx=kx, ky=ky, ksq=ksq, inv_denom=inv_denom,
-        mask_23=mask, eta_hat=eta_hat, sponge_phys=sponge_phys,
+        mask_23=mask, eta_hat=eta_hat, sponge_phys=sponge_phys, sponge_phys_pad=sponge_phys_pad,
         diss_rate_q=drq, diss_rate_w=drw, diss_rate_th=drt, inv_alpha_q=inv_aq,
         inv_alpha_th=inv_at, imex_inv=imex_inv,
         ksq_idx=np.asarray(inv_idx, dtype=np.int32).reshape(Nx, Nk),
@@ -559,6 +564,67 @@ def _zero_pad(f_hat, Nx, Npad):
     return out
 
 
+def _truncate(f_pad, Nx, Npad):
+    """Keep the Nx-grid modes of a padded spectrum and rescale by (Npad/Nx)^2
+    (nhqg/spectral.py:37-50)."""
+    out = np.concatenate([f_pad[..., :Nx // 2, :Nx // 2 + 1], f_pad[..., Npad - Nx // 2:, :Nx // 2 + 1]],
+                         axis=-2)
+    return out * (Npad / Nx) ** 2
+
+
+def _pad_wavenumbers(ky, Npad):
+    """kx, ky of the padded grid from the base grid's ky spacing
+    (nhqg/spectral.py:79-87)."""
+    k0 = ky[0, 1] if ky.shape[1] >= 2 else 0.0
+    kxp = k0 * np.fft.fftfreq(Npad, d=1.0 / Npad)
+    kyp = k0 * np.arange(Npad // 2 + 1)
+    return kxp[:, None], kyp[None, :]
+
+
+def _pad_irfft2(f_hat, Nx, Npad):
+    return _irfft2(_zero_pad(f_hat, Nx, Npad), Npad)
+
+
+def triple_conservative_flux_divergence_32(psi, q, w, th, kx, ky, Nx, Npad):
+    """div(u f, v f) under the 3/2 rule: zero-pad, products on the Npad grid,
+    padded-grid derivatives, truncate (nhqg/spectral.py:190-216, 237-253)."""
+    kx3, ky3 = kx[None], ky[None]
+    u = _pad_irfft2(-1j * ky3 * psi, Nx, Npad)
+    v = _pad_irfft2(1j * kx3 * psi, Nx, Npad)
+    kxp, kyp = _pad_wavenumbers(ky, Npad)
+    outs = []
+    for f_hat in (q, w, th):
+        f = _pad_irfft2(f_hat, Nx, Npad)
+        div = 1j * kxp[None] * _rfft2(u * f) + 1j * kyp[None] * _rfft2(v * f)
+        outs.append(_truncate(div, Nx, Npad))
+    return tuple(outs)
+
+
+def triple_jacobian_32(psi, q, w, th, kx, ky, Nx, Npad):
+    """J[psi, f] under the 3/2 rule (nhqg/spectral.py:147-180, 219-234)."""
+    kx3, ky3 = kx[None], ky[None]
+    psi_x = _pad_irfft2(1j * kx3 * psi, Nx, Npad)
+    psi_y = _pad_irfft2(1j * ky3 * psi, Nx, Npad)
+    outs = []
+    for f_hat in (q, w, th):
+        fx = _pad_irfft2(1j * kx3 * f_hat, Nx, Npad)
+        fy = _pad_irfft2(1j * ky3 * f_hat, Nx, Npad)
+        outs.append(_truncate(_rfft2(psi_x * fy - psi_y * fx), Nx, Npad))
+    return tuple(outs)
+
+
+def sponge_product_32(f_hat, sponge_phys_pad, Nx, Npad):
+    """sigma * f under the 3/2 rule with the pre-attenuated padded sigma
+    (nhqg/spectral.py:63-75)."""
+    return _truncate(_rfft2(sponge_phys_pad[None] * _pad_irfft2(f_hat, Nx, Npad)), Nx, Npad)
+
+
+def _mean_npad(grid):
+    """Grid of the SBP2 corrector's horizontal means: Nx under the 2/3 rule,
+    the padded grid under the 3/2 rule (nhqg/solver.py:836, 931)."""
+    return None if grid.horizontal_dealiasing == "23_rule" else grid.Npad
+
+
 def horizontal_mean(a_nodal, b_nodal, Nx, Npad=None):
     """<a b>_xy per level from spectral fields (nhqg/solver.py:204-245)."""
     if Npad is None or Npad == Nx:
@@ -596,16 +662,19 @@ def explicit_rhs(state: OracleState, grid: OracleGrid) -> OracleState:
     th_n = vmat(grid.V, th_cheb)
     if grid.eta_hat is not None:  # nhqg/solver.py:534-535
         q_n = q_n + grid.eta_hat[None]
-    if grid.horizontal_dealiasing != "23_rule":
-        raise NotImplementedError("oracle covers the 2/3 rule")
-    if grid.nonlinear_advection == "flux":
-        Aq_n, Aw_n, Ath_n = triple_conservative_flux_divergence_23(
-            psi_n, q_n, w_n, th_n, grid.kx, grid.ky, grid.mask_23, grid.Nx)
-    elif grid.nonlinear_advection == "jacobian":
-        Aq_n, Aw_n, Ath_n = triple_jacobian_23(
-            psi_n, q_n, w_n, th_n, grid.kx, grid.ky, grid.mask_23, grid.Nx)
-    else:
+    # nhqg/solver.py:389-418
+    if grid.nonlinear_advection not in ("flux", "jacobian"):
         raise ValueError(f"Unsupported nonlinear_advection={grid.nonlinear_advection!r}")
+    if grid.horizontal_dealiasing == "23_rule":
+        prod = (triple_conservative_flux_divergence_23 if grid.nonlinear_advection == "flux"
+                else triple_jacobian_23)
+        Aq_n, Aw_n, Ath_n = prod(psi_n, q_n, w_n, th_n, grid.kx, grid.ky, grid.mask_23, grid.Nx)
+    elif grid.horizontal_dealiasing == "32_rule":
+        prod = (triple_conservative_flux_divergence_32 if grid.nonlinear_advection == "flux"
+                else triple_jacobian_32)
+        Aq_n, Aw_n, Ath_n = prod(psi_n, q_n, w_n, th_n, grid.kx, grid.ky, grid.Nx, grid.Npad)
+    else:
+        raise ValueError(f"Unsupported horizontal_dealiasing={grid.horizontal_dealiasing!r}")
     Aq = vmat(grid.V_inv, Aq_n)
     Aw = vmat(grid.V_inv, Aw_n)
     Ath = vmat(grid.V_inv, Ath_n)
@@ -624,10 +693,14 @@ def explicit_rhs(state: OracleState, grid: OracleGrid) -> OracleState:
     else:
         E_th = vmat(grid.dirichlet_pinv, vmat(grid.proj_dirichlet, -Ath))
         E_th_bar = np.zeros_like(th_bar)
-    if grid.sponge_phys is not None:  # nhqg/solver.py:591-597
-        E_q = E_q - sponge_product_23(q_hat, grid.sponge_phys, grid.mask_23, grid.Nx)
-        E_w = E_w - sponge_product_23(w_hat, grid.sponge_phys, grid.mask_23, grid.Nx)
-        E_th = E_th - sponge_product_23(th_hat, grid.sponge_phys, grid.mask_23, grid.Nx)
+    if grid.sponge_phys is not None:  # nhqg/solver.py:421-424, 591-597
+        if grid.horizontal_dealiasing == "23_rule":
+            sp = lambda f: sponge_product_23(f, grid.sponge_phys, grid.mask_23, grid.Nx)  # noqa: E731
+        else:
+            sp = lambda f: sponge_product_32(f, grid.sponge_phys_pad, grid.Nx, grid.Npad)  # noqa: E731
+        E_q = E_q - sp(q_hat)
+        E_w = E_w - sp(w_hat)
+        E_th = E_th - sp(th_hat)
     return OracleState(E_q, E_w, E_th, E_th_bar)
 
 
@@ -763,7 +836,7 @@ def apply_balanced_sbp2_corrector(state: OracleState, grid: OracleGrid, total_dt
     D1, Lap = grid.sbp_D1, grid.sbp_L
     c2s, s2c = grid.cgl_to_sbp, grid.sbp_to_cgl
     w_sbp = vmat(c2s, vmat(grid.V, vmat(grid.w_stencil, state.w_hat)))
-    w2 = horizontal_mean(w_sbp, w_sbp, grid.Nx, None)  # 2/3 rule: Nx grid
+    w2 = horizontal_mean(w_sbp, w_sbp, grid.Nx, _mean_npad(grid))
     I = np.eye(grid.Nz + 1)
     half = 0.5 * mu * kappa * sub_dt * Lap + 0.25 * mu * sub_dt ** 2 * (D1 @ np.diag(w2) @ D1)
     A = I - half
@@ -776,7 +849,7 @@ def apply_balanced_sbp2_corrector(state: OracleState, grid: OracleGrid, total_dt
     for _ in range(n_sub):
         th_sbp = vmat(c2s, vmat(grid.V, vmat(grid.dirichlet_stencil, th_hat)))
         tb_sbp = c2s @ (grid.V @ th_bar)
-        flux = horizontal_mean(w_sbp, th_sbp, grid.Nx, None)
+        flux = horizontal_mean(w_sbp, th_sbp, grid.Nx, _mean_npad(grid))
         rhs = B @ tb_sbp - mu * sub_dt * (D1 @ flux)
         rhs[0] = rhs[-1] = 0.0
         tb_new = sla.lu_solve(lu, rhs)

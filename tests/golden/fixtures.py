@@ -4,7 +4,8 @@ Spectral fields in NHQG's rfft2 layout ``(levels, Nx, Nx//2+1)`` are stored
 packed to the 2/3-rule band: rows ``kx in [0..K] + [Nx-K..Nx-1]`` (fftfreq
 order) and columns ``ky in [0..K]`` with ``K = Nx//3``.  Every state the
 reference produces from a band-limited input is exactly zero outside that
-rectangle, and ``make_golden.py`` asserts it before packing.
+rectangle, and ``make_golden.py`` asserts it before packing.  The 3/2-rule
+cases (``PAD_CASES``) are full band and stored unpacked.
 """
 
 from __future__ import annotations
@@ -69,6 +70,8 @@ def state_from(arrays: dict, prefix: str):
 CASES = ("prod16", "fixed16", "jac16", "polar16", "radix24", "legacy16")
 # ARS(4,4,3) with the legacy exchange (fixed conduction; legacy evolve_mean)
 RK_CASES = ("rk443f16", "rk443l16")
+# 3/2-rule padded products: full-band states, stored unpacked
+PAD_CASES = ("pad32p16", "pad32j16", "pad32o16", "pad32s16", "pad32l24")
 
 
 def load_diagnostics() -> dict:

@@ -7,6 +7,7 @@ tests)::
     python tests/golden/make_golden.py /path/to/NHQG --diagnostics
     python tests/golden/make_golden.py /path/to/NHQG --spectra
     python tests/golden/make_golden.py /path/to/NHQG --rk443
+    python tests/golden/make_golden.py /path/to/NHQG --pad32
 
 The reference (``nhqg/*.py``, unmodified, read-only) is imported under the
 NumPy stand-in for ``jax`` in ``tests/golden/refshim``.  Every case records
@@ -24,7 +25,8 @@ the reference's own outputs for:
               ``imex_step`` applied 1/5 times.
 
 Spectral arrays are stored packed to the 2/3 band (see ``fixtures.py``); the
-script asserts the out-of-band content is exactly zero first.
+script asserts the out-of-band content is exactly zero first.  The 3/2-rule
+cases (``--pad32``) carry full-band states and store them unpacked.
 """
 
 from __future__ import annotations
@@ -79,6 +81,29 @@ CASES = {
 RK_CASES = {
     "rk443f16": dict(Nx=16, Nz=10, imex_scheme="rk443", thermal_closure="fixed_conduction"),
     "rk443l16": dict(Nx=16, Nz=8, imex_scheme="rk443", thermal_closure="evolve_mean",
+                     mean_exchange_discretization="legacy", mean_temp_eps_sq=0.7),
+}
+
+# 3/2-rule padded products (horizontal_dealiasing='32_rule', the reference's
+# config default; nhqg/spectral.py:147-253): states are full band, so these
+# fixtures store spectral fields unpacked (Nx x Nk)
+PAD_CASES = {
+    # production recipe: padded <w theta> means in the SBP2 corrector
+    "pad32p16": dict(Nx=16, Nz=8, horizontal_dealiasing="32_rule", thermal_closure="evolve_mean",
+                     mean_exchange_discretization="balanced_sbp2_pc", sbp_corrector_substeps=4),
+    # Jacobian form, beta plane, finite deformation radius, hyperviscosity, drag
+    "pad32j16": dict(Nx=16, Nz=8, horizontal_dealiasing="32_rule", thermal_closure="fixed_conduction",
+                     nonlinear_advection="jacobian", beta=0.7, Ld=3.0, hyper_order=2, nu_q=1e-3,
+                     nu_w=2e-3, nu_theta=3e-3, drag=0.05),
+    # open top, trap eta and padded sponge (band-limited stand-ins), flux form
+    "pad32o16": dict(Nx=16, Nz=8, horizontal_dealiasing="32_rule", w_bc_top="neumann",
+                     thermal_closure="evolve_mean", mean_exchange_discretization="balanced_sbp2_pc",
+                     sbp_corrector_substeps=4, _override_eta_sponge=True),
+    # Jacobian form with eta and the padded sponge
+    "pad32s16": dict(Nx=16, Nz=6, horizontal_dealiasing="32_rule", thermal_closure="fixed_conduction",
+                     nonlinear_advection="jacobian", _override_eta_sponge=True),
+    # radix-3 sizes (Nx = 24, Npad = 36), legacy explicit exchange
+    "pad32l24": dict(Nx=24, Nz=6, horizontal_dealiasing="32_rule", thermal_closure="evolve_mean",
                      mean_exchange_discretization="legacy", mean_temp_eps_sq=0.7),
 }
 
@@ -140,6 +165,17 @@ def smooth_eta_sponge(grid):
     return np.fft.rfft2(eta), sigma
 
 
+def padded_sponge(sponge_phys, Nx, Npad):
+    """The pre-attenuated padded sponge of a sponge field, built as
+    nhqg/grid.py:663-667 builds grid.sponge_phys_pad."""
+    s_hat = np.fft.rfft2(sponge_phys)
+    Nk = Nx // 2 + 1
+    pad = np.zeros((Npad, Npad // 2 + 1), dtype=np.complex128)
+    pad[:Nx // 2, :Nk] = s_hat[:Nx // 2, :]
+    pad[Npad - Nx // 2:, :Nk] = s_hat[Nx // 2:, :]
+    return np.fft.irfft2(pad, s=(Npad, Npad))
+
+
 def main(ref_root: str, cases: dict | None = None, grid_fixture: bool = True) -> None:
     sys.path.insert(0, str(HERE / "refshim"))
     sys.path.insert(0, ref_root)
@@ -159,12 +195,17 @@ def main(ref_root: str, cases: dict | None = None, grid_fixture: bool = True) ->
         grid = make_grid(cfg)
         Nx = grid.Nx
         extra = {}
+        full = grid.horizontal_dealiasing == "32_rule"
         if override:
             eta_hat, sponge_phys = smooth_eta_sponge(grid)
             grid = grid._replace(eta_hat=jnp.asarray(eta_hat),
                                  sponge_phys=jnp.asarray(sponge_phys))
             extra = {"grid.eta_hat__packed": pack(eta_hat[None], Nx),
                      "grid.sponge_phys": sponge_phys}
+            if full:
+                pad_sponge = padded_sponge(sponge_phys, Nx, int(grid.Npad))
+                grid = grid._replace(sponge_phys_pad=jnp.asarray(pad_sponge))
+                extra["grid.sponge_phys_pad"] = pad_sponge
         split = solver.uses_split_thermal_exchange(grid)
         base = (grid._replace(thermal_closure="fixed_conduction",
                               mean_exchange_discretization="legacy") if split else grid)
@@ -173,7 +214,9 @@ def main(ref_root: str, cases: dict | None = None, grid_fixture: bool = True) ->
         def put_state(prefix, s):
             for fname, arr in zip(("q_hat", "w_hat", "th_hat", "th_bar"), s):
                 arr = np.asarray(arr)
-                if arr.ndim == 3:
+                if arr.ndim == 3 and full:
+                    out[f"{prefix}.{fname}"] = arr
+                elif arr.ndim == 3:
                     oob = out_of_band_max(arr, Nx)
                     assert oob == 0.0, (name, prefix, fname, oob)
                     out[f"{prefix}.{fname}__packed"] = pack(arr, Nx)
@@ -346,6 +389,8 @@ if __name__ == "__main__":
         spectra_main(root)
     elif "--rk443" in sys.argv:
         main(root, RK_CASES, grid_fixture=False)
+    elif "--pad32" in sys.argv:
+        main(root, PAD_CASES, grid_fixture=False)
     elif "--jaxprng" in sys.argv:
         jaxprng_main(root)
     else:

@@ -22,7 +22,8 @@ def _grid(meta, arrays):
     cfg.pop("_override_eta_sponge", None)
     grid = oracle.make_grid(OracleConfig(**cfg))
     if meta.get("override_eta_sponge"):
-        grid = grid.replace(eta_hat=arrays["grid.eta_hat"][0], sponge_phys=arrays["grid.sponge_phys"])
+        grid = grid.replace(eta_hat=arrays["grid.eta_hat"][0], sponge_phys=arrays["grid.sponge_phys"],
+                            sponge_phys_pad=arrays.get("grid.sponge_phys_pad"))
     return grid
 
 
@@ -30,7 +31,7 @@ def _state(arrays, prefix):
     return OracleState(*fixtures.state_from(arrays, prefix))
 
 
-@pytest.fixture(scope="module", params=fixtures.CASES + fixtures.RK_CASES)
+@pytest.fixture(scope="module", params=fixtures.CASES + fixtures.RK_CASES + fixtures.PAD_CASES)
 def case(request):
     meta, arrays = fixtures.load_case(request.param)
     return request.param, meta, arrays, _grid(meta, arrays)
