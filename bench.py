@@ -43,10 +43,10 @@ L_C = 2.0 * math.pi / 1.3048
 METRIC = "NHQG steps/s at 256^2x256: mixed-precision vs plain FP64 on GB300, rel err <=1e-6"
 
 
-def workload(nx: int, nz: int) -> dict:
+def workload(nx: int, nz: int, rule: str = "23_rule") -> dict:
     return dict(Nx=nx, Nz=nz, L=10 * L_C, Ra_tilde=100.0, sigma=1.0, nu_q=1.0, nu_w=1.0,
                 nu_theta=1.0, hyper_order=1, dt=2e-5, nonlinear_advection="flux",
-                horizontal_dealiasing="23_rule", float_dtype="float64",
+                horizontal_dealiasing=rule, float_dtype="float64",
                 thermal_closure="evolve_mean", mean_exchange_discretization="balanced_sbp2_pc",
                 sbp_corrector_substeps=4)
 
@@ -136,14 +136,17 @@ def kernel_work(name: str, g, launches_per_step: int, tc: bool = False) -> tuple
     of FP32, so every FP64 kernel is arithmetic-bound -- or 'hbm'."""
     Nx, Nz = g.Nx, g.Nz
     P, G = Nz + 1, Nz - 1
-    K = Nx // 3
-    Mc, Mr = K + 1, 2 * K + 1
+    if g.horizontal_dealiasing == "32_rule":  # full band, products on the padded grid
+        Mr, Mc, N = Nx, Nx // 2 + 1, 3 * Nx // 2
+    else:
+        K = Nx // 3
+        Mr, Mc, N = 2 * K + 1, K + 1, Nx
     M = Mr * Mc
     f32 = name.endswith("_f32")
     base = name[:-4] if f32 else name
     cplx = 8.0 if f32 else 16.0
     pipe = "fp32" if f32 else "fp64"
-    fft = 5.0 * Nx * math.log2(Nx)
+    fft = 5.0 * N * math.log2(N)
     L = 2 * Nz
     smooth = L
     for f in (2, 3):
@@ -153,11 +156,11 @@ def kernel_work(name: str, g, launches_per_step: int, tc: bool = False) -> tuple
     field = P * M * cplx
     field64 = P * M * 16.0
     if base == "h1_col_ifft":
-        return 5 * Mc * P * fft, 3 * field + 5 * P * Mc * Nx * cplx, pipe
+        return 5 * Mc * P * fft, 3 * field + 5 * P * Mc * N * cplx, pipe
     if base == "h2_row_products":
-        return (5 + 6) * (Nx / 2) * P * fft + 6 * Nx * Nx * P, (5 + 6) * P * Mc * Nx * cplx, pipe
+        return (5 + 6) * (N / 2) * P * fft + 6 * N * N * P, (5 + 6) * P * Mc * N * cplx, pipe
     if base == "h3_col_fft":
-        return 6 * Mc * P * fft, 6 * P * Mc * Nx * cplx + 3 * field, pipe
+        return 6 * Mc * P * fft, 6 * P * Mc * N * cplx + 3 * field, pipe
     if base == "vfwd":
         nf = 3 if launches_per_step <= 1 else 2  # 3 fields at stage 1, 1 at stage 2
         return nf * dct * M, nf * (field64 + field), pipe
@@ -252,8 +255,9 @@ def measured_hbm_gbs() -> float | None:
 
 
 # ------------------------------------------------------------------ CPU (oracle) arm
-def workload_name(nx: int, nz: int) -> str:
-    return (f"{nx}^2x{nz} ARS222, evolve_mean balanced_sbp2_pc sub4, flux, 2/3 rule, "
+def workload_name(nx: int, nz: int, rule: str = "23_rule") -> str:
+    r = "2/3 rule" if rule == "23_rule" else f"3/2 rule (padded {3 * nx // 2}^2 products)"
+    return (f"{nx}^2x{nz} ARS222, evolve_mean balanced_sbp2_pc sub4, flux, {r}, "
             "L=10Lc, Ra=100, Pr=1, dt=2e-5")
 
 
@@ -375,7 +379,7 @@ def run_ours(args, ws, rank, local):
     from nhqg_gb300 import solver as S
     from nhqg_gb300.engine import engine_for
 
-    cfgd = workload(args.nx, args.nz)
+    cfgd = workload(args.nx, args.nz, args.rule)
     t0 = time.perf_counter()
     grid = make_grid(NHQGConfig(**cfgd))
     t_grid = time.perf_counter() - t0
@@ -489,7 +493,7 @@ def run_ours(args, ws, rank, local):
         "dtype": "f32 products + tf32x3 tensor-core vertical transforms + f64 solves/exchange",
         "data": (f"synthetic: seeded theta' 1e-3 N(0,1) sin(pi Z) (PCG64 seed 0), spun up by "
                  f"{args.spinup} plain FP64 steps"),
-        "config": {"workload": workload_name(args.nx, args.nz), "path": "mixed", "Nx": args.nx, "Nz": args.nz,
+        "config": {"workload": workload_name(args.nx, args.nz, args.rule), "path": "mixed", "Nx": args.nx, "Nz": args.nz,
                    "timed": "one step_inplace call of `steps` steps on a device-resident state",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "state and per-step traffic >> 129 MB L2; no flush needed"},
@@ -706,14 +710,14 @@ def run_reference(args, ws, rank):
     this arm's workload, metric and units; rank 0 only."""
     if rank != 0:
         return None
-    cfgd = workload(args.nx, args.nz)
+    cfgd = workload(args.nx, args.nz, args.rule)
     cb = cpu_reference(cfgd, samples=args.steps, warmup=max(0, min(args.warmup, 1)))
     return {
         "metric": METRIC, "value": round(cb["value"], 6), "unit": "steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / cb["value"], 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded theta' start)", "impl": "reference",
-        "config": {"workload": workload_name(args.nx, args.nz), "path": "cpu_port",
+        "config": {"workload": workload_name(args.nx, args.nz, args.rule), "path": "cpu_port",
                    "Nx": args.nx, "Nz": args.nz, "parallelism": "host cores"},
         "cpu_baseline": cb,
         "e2e": {"value": round(cb["value"], 6), "unit": "steps/s", "h2d_bytes_per_step": 0,
@@ -729,6 +733,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--nz", type=int, default=256)
+    ap.add_argument("--rule", default="23_rule", choices=["23_rule", "32_rule"],
+                    help="horizontal dealiasing of the workload (the headline uses the 2/3 rule)")
     ap.add_argument("--spinup", type=int, default=1000,
                     help="plain FP64 steps from the seeded start before measuring "
                          "(the precision study's configuration uses 5000)")

@@ -51,6 +51,14 @@ enum { NHQG_PRECISION_FP64 = 0, NHQG_PRECISION_MIXED = 1 };
  * stepper with the grid's gamma.  RK443 runs in FP64 (NHQG_PRECISION_MIXED
  * steps return NHQG_ERR_UNSUPPORTED). */
 enum { NHQG_SCHEME_ARS222 = 0, NHQG_SCHEME_RK443 = 1 };
+/* horizontal_dealiasing (nhqg/config.py:62).  NHQG_DEALIAS_23 ("23_rule"):
+ * products on the Nx grid masked to |kx|, ky <= Nx/3, states band-limited to
+ * that rectangle.  NHQG_DEALIAS_32 ("32_rule", the reference's default):
+ * products on the zero-padded 3Nx/2 grid and truncated back
+ * (nhqg/spectral.py:18-50, 147-253); states are full band and the horizontal
+ * means <a b> are those of the padded fields (nhqg/solver.py:204-245).
+ * 3Nx/2 must factor as 2^a 3^b. */
+enum { NHQG_DEALIAS_23 = 0, NHQG_DEALIAS_32 = 1 };
 
 /*
  * Host-side description of a Grid (nhqg/grid.py:29-141 Grid fields, built by
@@ -74,8 +82,16 @@ typedef struct nhqg_grid_desc {
   const int *shell_of_mode;                    /* (Nx,Nk) row of shell_inv, or -1 */
   const double *shell_inv;                     /* (n_shells,G,G) imex_inv rows */
   const double *eta_hat;                       /* (Nx,Nk) complex or NULL */
-  const double *eta_phys;                      /* (Nx,Nx) irfft2(eta_hat), or NULL */
-  const double *sponge_phys;                   /* (Nx,Nx) or NULL */
+  const double *eta_phys;                      /* (Nh,Nh) physical eta, or NULL:
+                                                  irfft2(eta_hat) on the Nx grid
+                                                  (2/3 rule); irfft2 of the
+                                                  zero-padded eta_hat on the
+                                                  Npad grid, no rescale (3/2
+                                                  rule) */
+  const double *sponge_phys;                   /* (Nh,Nh) or NULL: the Grid's
+                                                  sponge_phys (2/3 rule) or
+                                                  sponge_phys_pad (3/2 rule,
+                                                  nhqg/grid.py:663-667) */
   const double *V, *V_inv;                     /* (P,P) */
   const double *w_stencil;                     /* (P,G) */
   const double *G_Z;                           /* (P,P) */
@@ -98,6 +114,9 @@ typedef struct nhqg_grid_desc {
                                                   shell tables must be the
                                                   scheme's (1 - 1/sqrt 2 for
                                                   ARS222, 1/2 for RK443) */
+  int horizontal_dealiasing;                   /* NHQG_DEALIAS_*; Nh = Nx for the
+                                                  2/3 rule, Npad = 3Nx/2 for the
+                                                  3/2 rule */
 } nhqg_grid_desc;
 
 typedef struct nhqg_ctx nhqg_ctx;
@@ -117,8 +136,9 @@ int nhqg_ctx_create(const nhqg_grid_desc *desc, nhqg_ctx **out);
 int nhqg_ctx_destroy(nhqg_ctx *ctx);
 
 /* n_steps applications of imex_step (nhqg/solver.py:1228-1242, including
- * sanitize_state), in place.  The input must be band-limited (every state
- * that sanitize_state, make_initial_state, run or imex_step produced is). */
+ * sanitize_state), in place.  Under the 2/3 rule the input must be
+ * band-limited (every state that sanitize_state, make_initial_state, run or
+ * imex_step produced is); under the 3/2 rule every mode is stored. */
 int nhqg_step(nhqg_ctx *ctx, nhqg_state *state, int n_steps, void *stream);
 
 /* Arithmetic of the following nhqg_step / nhqg_explicit_rhs /
@@ -213,8 +233,23 @@ int nhqg_triple_advection_23_noalloc(int advection, int Nx, int levels,
 int nhqg_sponge_product_23(nhqg_ctx *ctx, int levels, const void *f, void *out,
                            void *stream);
 
+/* 3/2-rule planes, on a context built with NHQG_DEALIAS_32 (a 2/3-rule
+ * context returns NHQG_ERR_UNSUPPORTED, and the _23 calls refuse a 3/2-rule
+ * context): triple_jacobian / triple_conservative_flux_divergence
+ * (nhqg/spectral.py:147-253) on `levels` planes (Nx, Nk) complex128 each,
+ * zero-padded to the context's Npad = 3Nx/2 grid and truncated back; and
+ * sponge_product_32 (nhqg/spectral.py:63-75) with the context's padded
+ * sponge. */
+int nhqg_triple_advection_32(nhqg_ctx *ctx, int advection, int levels,
+                             const void *psi, const void *q, const void *w,
+                             const void *th, void *Aq, void *Aw, void *Ath,
+                             void *stream);
+int nhqg_sponge_product_32(nhqg_ctx *ctx, int levels, const void *f, void *out,
+                           void *stream);
+
 /* sanitize_state (nhqg/solver.py:128-146), in place: Hermitian projection
- * of the ky=0 column and the 2/3 band limit. */
+ * of the ky=0 column and the 2/3 band limit (2/3 rule), or of the ky=0 and
+ * ky=Nx/2 columns (3/2 rule, no band limit). */
 int nhqg_sanitize(nhqg_ctx *ctx, nhqg_state *state, void *stream);
 
 /* imex_mean_temp_solve (nhqg/solver.py:741-758) of R_th_bar (Nz+1 doubles,

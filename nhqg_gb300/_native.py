@@ -40,6 +40,7 @@ EXCHANGE = {"legacy": 0, "balanced_sbp2": 1, "balanced_sbp2_pc": 2}
 WBC = {"dirichlet": 0, "neumann": 1}
 PRECISION = {"fp64": 0, "mixed": 1}
 SCHEME = {"ars222": 0, "rk443": 1}
+DEALIAS = {"23_rule": 0, "32_rule": 1}
 DIAG_KEYS = ("KE_bt", "KE_bc", "KE_tot", "enstrophy", "Nusselt", "Nusselt_dealiased",
              "vol_avg_tw", "vol_avg_tw_dealiased", "q_rms", "w_rms", "th_rms", "th_bar_max")
 
@@ -115,6 +116,7 @@ class GridDesc(ctypes.Structure):
         ("cgl_to_sbp", c_double_p), ("sbp_to_cgl", c_double_p), ("mean_solve", c_double_p),
         ("shell_coef", c_double_p), ("cc_weights", c_double_p),
         ("imex_scheme", ctypes.c_int),
+        ("horizontal_dealiasing", ctypes.c_int),
     ]
 
 
@@ -142,6 +144,10 @@ SIGNATURES = {
     "nhqg_triple_advection_23_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int] +
                                          [ctypes.c_void_p] * 9 + [ctypes.c_void_p]),
     "nhqg_sponge_product_23": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p]),
+    "nhqg_triple_advection_32": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] +
+                                 [ctypes.c_void_p] * 7 + [ctypes.c_void_p]),
+    "nhqg_sponge_product_32": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_void_p]),
     "nhqg_sanitize": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(StateDesc), ctypes.c_void_p]),
     "nhqg_mean_temp_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -25,7 +25,7 @@ import torch
 
 from . import _native as nat
 from .engine import Engine, _stream_handle
-from .grid import Grid
+from .grid import Grid, compact_layout
 from .solver import State, explicit_rhs, to_device
 
 N_IN, N_H1, N_H2, N_OUT = 66, 256, 128, 64
@@ -195,12 +195,11 @@ def mode_geometry(engine: Engine) -> tuple[np.ndarray, np.ndarray]:
     """|k|^2 and inv_denom of the in-band modes in the engine's compact order
     (r = kx row in fftfreq order of the band, c = ky column)."""
     g = engine.grid
-    K = g.Nx // 3
-    rows = np.concatenate([np.arange(0, K + 1), np.arange(g.Nx - K, g.Nx)])
+    rows, ncol = compact_layout(g)
     kx = np.asarray(g.kx).reshape(g.Nx, -1)[:, 0][rows]
-    ky = np.asarray(g.ky).reshape(-1)[: K + 1]
+    ky = np.asarray(g.ky).reshape(-1)[:ncol]
     KX, KY = np.meshgrid(kx, ky, indexing="ij")
-    inv = np.asarray(g.inv_denom)[np.ix_(rows, np.arange(K + 1))]
+    inv = np.asarray(g.inv_denom)[np.ix_(rows, np.arange(ncol))]
     return (KX ** 2 + KY ** 2).ravel(), inv.ravel()
 
 

@@ -102,7 +102,7 @@ CSR to_csr(const double* A, int n) {
   return s;
 }
 
-int full_index(const Dims& d, int r, int c) { return full_row(r, d.K, d.Nx) * d.Nk + c; }
+int full_index(const Dims& d, int r, int c) { return full_row(r, d.K, d.Mr, d.Nx) * d.Nk + c; }
 
 // exp(-2 pi i k / n) with the angle reduced to [0, pi/4] so that each
 // component comes from one correctly-rounded-in-practice libm call
@@ -140,7 +140,12 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   if (!g || !out) return NHQG_ERR_BAD_ARG;
   *out = nullptr;
   if (g->Nx < 8 || g->Nx % 2 != 0 || g->Nz < 4 || g->Nz + 1 > 1024) return NHQG_ERR_UNSUPPORTED;
-  FftPlan plan = make_fft_plan(g->Nx);
+  if (g->horizontal_dealiasing != NHQG_DEALIAS_23 && g->horizontal_dealiasing != NHQG_DEALIAS_32)
+    return NHQG_ERR_BAD_ARG;
+  const bool pad32 = g->horizontal_dealiasing == NHQG_DEALIAS_32;
+  // the horizontal transforms run on the Nx grid (2/3 rule) or the padded
+  // 3Nx/2 grid (3/2 rule): that length must be 2^a 3^b
+  FftPlan plan = make_fft_plan(pad32 ? 3 * g->Nx / 2 : g->Nx);
   if (plan.npass <= 0) return NHQG_ERR_UNSUPPORTED;
   if (g->advection != NHQG_ADV_FLUX && g->advection != NHQG_ADV_JACOBIAN) return NHQG_ERR_UNSUPPORTED;
   if (g->exchange < NHQG_EXCHANGE_LEGACY || g->exchange > NHQG_EXCHANGE_BALANCED_SBP2_PC)
@@ -160,7 +165,7 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   nhqg_ctx* c = new (std::nothrow) nhqg_ctx();
   if (!c) return NHQG_ERR_BAD_ARG;
   Params& p = c->p;
-  p.d = make_dims(g->Nx, g->Nz);
+  p.d = make_dims(g->Nx, g->Nz, pad32);
   p.plan = plan;
   p.plan_v = make_fft_plan(g->Nz);
   p.fast_dct = g->Nz % 2 == 0 && p.plan_v.npass > 0 && getenv("NHQG_DENSE_VERTICAL") == nullptr;
@@ -209,7 +214,7 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     for (int cc = 0; cc < d.Mc; ++cc) {
       const int m = r * d.Mc + cc;
       const int f = full_index(d, r, cc);
-      kx[m] = g->kx[full_row(r, d.K, d.Nx)];
+      kx[m] = g->kx[full_row(r, d.K, d.Mr, d.Nx)];
       ky[m] = g->ky[cc];
       idn[m] = g->inv_denom[f];
       iaq[m] = g->inv_alpha_q[f];
@@ -226,11 +231,25 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   UP(t.kx, kx.data(), M); UP(t.ky, ky.data(), M); UP(t.inv_denom, idn.data(), M);
   UP(t.inv_aq, iaq.data(), M); UP(t.inv_at, iat.data(), M);
   UP(t.drq, drq.data(), M); UP(t.drw, drw.data(), M); UP(t.drt, drt.data(), M);
+  // physical-space eta and sigma on the Nh grid, in the products' scaling:
+  // the horizontal kernels carry each field as (Nh/Nx) irfft2 of its padded
+  // spectrum (1 under the 2/3 rule)
+  const size_t nh2 = (size_t)d.Nh * d.Nh;
+  const double hscale = (double)d.Nh / (double)d.Nx;
+  std::vector<double> eta_ph, sponge_ph;
+  if (p.has_eta) {
+    eta_ph.assign(g->eta_phys, g->eta_phys + nh2);
+    for (double& v : eta_ph) v *= hscale;
+  }
+  if (p.has_sponge) {
+    sponge_ph.assign(g->sponge_phys, g->sponge_phys + nh2);
+    for (double& v : sponge_ph) v *= hscale;
+  }
   if (p.has_eta) {
     UP(t.eta, eta.data(), M);
-    UP(t.eta_phys, g->eta_phys, (size_t)d.Nx * d.Nx);
+    UP(t.eta_phys, eta_ph.data(), nh2);
   }
-  if (p.has_sponge) UP(t.sponge, g->sponge_phys, (size_t)d.Nx * d.Nx);
+  if (p.has_sponge) UP(t.sponge, sponge_ph.data(), nh2);
   UP(t.kx_full, g->kx, d.Nx);
   UP(t.ky_full, g->ky, d.Nk);
   UP(t.inv_denom_full, g->inv_denom, (size_t)d.Nx * d.Nk);
@@ -238,12 +257,12 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
 
   // ---- FFT tables ----
   {
-    std::vector<double2> tw(d.Nx);
-    for (int k = 0; k < d.Nx; ++k) tw[k] = twiddle(k, d.Nx);
-    std::vector<int> perm(d.Nx);
+    std::vector<double2> tw(d.Nh);
+    for (int k = 0; k < d.Nh; ++k) tw[k] = twiddle(k, d.Nh);
+    std::vector<int> perm(d.Nh);
     make_fft_perm(plan, perm.data());
-    UP(t.tw, tw.data(), d.Nx);
-    UP(t.perm, perm.data(), d.Nx);
+    UP(t.tw, tw.data(), d.Nh);
+    UP(t.perm, perm.data(), d.Nh);
   }
   if (p.fast_dct) {
     const int L = d.Nz;
@@ -272,8 +291,8 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     std::vector<float> kxf = f32(g->kx, d.Nx), kyf = f32(g->ky, d.Nk);
     UP(t.kx_f, kxf.data(), kxf.size());
     UP(t.ky_f, kyf.data(), kyf.size());
-    std::vector<double2> tw(d.Nx);
-    for (int k = 0; k < d.Nx; ++k) tw[k] = twiddle(k, d.Nx);
+    std::vector<double2> tw(d.Nh);
+    for (int k = 0; k < d.Nh; ++k) tw[k] = twiddle(k, d.Nh);
     std::vector<float2> twf = c32(tw);
     UP(t.tw_f, twf.data(), twf.size());
     if (p.fast_dct) {
@@ -285,11 +304,11 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
       UP(t.cs_v_f, csvf.data(), csvf.size());
     }
     if (p.has_sponge) {
-      std::vector<float> v = f32(g->sponge_phys, (size_t)d.Nx * d.Nx);
+      std::vector<float> v = f32(sponge_ph.data(), nh2);
       UP(t.sponge_f, v.data(), v.size());
     }
     if (p.has_eta) {
-      std::vector<float> v = f32(g->eta_phys, (size_t)d.Nx * d.Nx);
+      std::vector<float> v = f32(eta_ph.data(), nh2);
       UP(t.eta_phys_f, v.data(), v.size());
       std::vector<float2> e = c32(eta);
       UP(t.eta_f, e.data(), e.size());
@@ -495,12 +514,12 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   {
     const int nf1 = (p.advection == NHQG_ADV_JACOBIAN) ? 11 : 5;
     const int ng = (p.advection == NHQG_ADV_JACOBIAN) ? 3 : 6;
-    w.x1_elems = (size_t)nf1 * P * d.Mc * d.Nx;
-    w.x2_elems = (size_t)ng * P * d.Mc * d.Nx;
+    w.x1_elems = (size_t)nf1 * P * d.Mc * d.Nh;
+    w.x2_elems = (size_t)ng * P * d.Mc * d.Nh;
     // the plane API (full Nk columns, up to 11 fields) reuses these in level chunks
-    const size_t plane_min = (size_t)11 * d.Nk * d.Nx;
+    const size_t plane_min = (size_t)11 * d.Nk * d.Nh;
     if (w.x1_elems < plane_min) w.x1_elems = plane_min;
-    const size_t plane2_min = (size_t)6 * d.Mc * d.Nx;
+    const size_t plane2_min = (size_t)6 * d.Mc * d.Nh;
     if (w.x2_elems < plane2_min) w.x2_elems = plane2_min;
     if (dalloc(c, &w.x1, w.x1_elems) != cudaSuccess) return fail(NHQG_ERR_CUDA);
     if (dalloc(c, &w.x2, w.x2_elems) != cudaSuccess) return fail(NHQG_ERR_CUDA);
@@ -1131,19 +1150,27 @@ int nhqg_mean_temp_solve(nhqg_ctx* c, const double* R, double* out, int closure,
   return NHQG_OK;
 }
 
-int nhqg_triple_advection_23(nhqg_ctx* c, int advection, int levels, const void* psi,
-                             const void* q, const void* w, const void* th, void* Aq, void* Aw,
-                             void* Ath, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// Plane APIs: products of caller-supplied nodal planes in the full rfft2
+// layout, in level chunks that fit the step's workspace.  The context's
+// dealiasing rule (pad32) selects the 2/3 or the 3/2 products.
+int plane_advection(nhqg_ctx* c, bool pad32, int advection, int levels, const void* psi,
+                    const void* q, const void* w, const void* th, void* Aq, void* Aw, void* Ath,
+                    void* stream) {
   if (!c || levels <= 0 || !psi || !q || !w || !th || !Aq || !Aw || !Ath) return NHQG_ERR_BAD_ARG;
   if (advection != NHQG_ADV_FLUX && advection != NHQG_ADV_JACOBIAN) return NHQG_ERR_UNSUPPORTED;
+  if (c->p.d.pad != pad32) return NHQG_ERR_UNSUPPORTED;
   cudaStream_t st = S(stream);
   c->launches = 0;
   const Dims& d = c->p.d;
   const size_t plane = (size_t)d.Nx * d.Nk;
   const int nf1 = advection == NHQG_ADV_JACOBIAN ? 8 : 5;
   const int ng = advection == NHQG_ADV_JACOBIAN ? 3 : 6;
-  int chunk = (int)std::min(c->w.x1_elems / ((size_t)nf1 * d.Nk * d.Nx),
-                            c->w.x2_elems / ((size_t)ng * d.Mc * d.Nx));
+  int chunk = (int)std::min(c->w.x1_elems / ((size_t)nf1 * d.Nk * d.Nh),
+                            c->w.x2_elems / ((size_t)ng * d.Mc * d.Nh));
   if (chunk < 1) return NHQG_ERR_UNSUPPORTED;
   CK(cudaMemsetAsync(Aq, 0, (size_t)levels * plane * sizeof(double2), st));
   CK(cudaMemsetAsync(Aw, 0, (size_t)levels * plane * sizeof(double2), st));
@@ -1163,14 +1190,15 @@ int nhqg_triple_advection_23(nhqg_ctx* c, int advection, int levels, const void*
   return NHQG_OK;
 }
 
-int nhqg_sponge_product_23(nhqg_ctx* c, int levels, const void* f, void* out, void* stream) {
+int plane_sponge(nhqg_ctx* c, bool pad32, int levels, const void* f, void* out, void* stream) {
   if (!c || levels <= 0 || !f || !out) return NHQG_ERR_BAD_ARG;
-  if (!c->p.has_sponge) return NHQG_ERR_UNSUPPORTED;
+  if (!c->p.has_sponge || c->p.d.pad != pad32) return NHQG_ERR_UNSUPPORTED;
   cudaStream_t st = S(stream);
   c->launches = 0;
   const Dims& d = c->p.d;
   const size_t plane = (size_t)d.Nx * d.Nk;
-  int chunk = (int)std::min(c->w.x1_elems / ((size_t)d.Nk * d.Nx), c->w.x2_elems / ((size_t)d.Mc * d.Nx));
+  int chunk = (int)std::min(c->w.x1_elems / ((size_t)d.Nk * d.Nh), c->w.x2_elems / ((size_t)d.Mc * d.Nh));
+  if (chunk < 1) return NHQG_ERR_UNSUPPORTED;
   CK(cudaMemsetAsync(out, 0, (size_t)levels * plane * sizeof(double2), st));
   for (int l0 = 0; l0 < levels; l0 += chunk) {
     const int nl = std::min(chunk, levels - l0);
@@ -1184,6 +1212,30 @@ int nhqg_sponge_product_23(nhqg_ctx* c, int levels, const void* f, void* out, vo
     CK(launch_horizontal(c->p, c->t, c->w, a, st, &c->launches));
   }
   return NHQG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nhqg_triple_advection_23(nhqg_ctx* c, int advection, int levels, const void* psi,
+                             const void* q, const void* w, const void* th, void* Aq, void* Aw,
+                             void* Ath, void* stream) {
+  return plane_advection(c, false, advection, levels, psi, q, w, th, Aq, Aw, Ath, stream);
+}
+
+int nhqg_triple_advection_32(nhqg_ctx* c, int advection, int levels, const void* psi,
+                             const void* q, const void* w, const void* th, void* Aq, void* Aw,
+                             void* Ath, void* stream) {
+  return plane_advection(c, true, advection, levels, psi, q, w, th, Aq, Aw, Ath, stream);
+}
+
+int nhqg_sponge_product_23(nhqg_ctx* c, int levels, const void* f, void* out, void* stream) {
+  return plane_sponge(c, false, levels, f, out, stream);
+}
+
+int nhqg_sponge_product_32(nhqg_ctx* c, int levels, const void* f, void* out, void* stream) {
+  return plane_sponge(c, true, levels, f, out, stream);
 }
 
 }  // extern "C"

@@ -1,8 +1,8 @@
 // Diagnostics of a state.  Scalars (nhqg/diagnostics.py:597-690, the subset
 // without the budgets): Clenshaw-Curtis depth integrals of
 // |psi|^2, |q|^2, |w|^2, |theta|^2, Re(w theta*) and of the barotropic psi
-// per mode, weighted by the half-plane Parseval weights (1 at ky = 0, 2
-// elsewhere in the 2/3 band) and normalised by Nx^4.  Spectra: the shell
+// per mode, weighted by the half-plane Parseval weights (1 at ky = 0 and, in
+// the full-band layout of the 3/2 rule, at ky = Nx/2; 2 elsewhere) and normalised by Nx^4.  Spectra: the shell
 // energy spectrum and the vertical mode energies (k_spec_*, k_vspec).
 #include "engine.h"
 
@@ -11,6 +11,12 @@ namespace nhqg {
 namespace {
 
 constexpr int kDiagThreads = 256;
+
+// rfft2 half-plane weight of compact mode m (nhqg/diagnostics.py:48-54)
+__device__ __forceinline__ double hweight(const Dims& d, int m) {
+  const int c = m % d.Mc;
+  return (c == 0 || (d.pad && c == d.Nk - 1)) ? 1.0 : 2.0;
+}
 
 // one thread per compact mode, levels looped (level-major fields: coalesced)
 __global__ void __launch_bounds__(kDiagThreads) k_diag_modes(Dims d, const double* __restrict__ cc,
@@ -40,8 +46,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_modes(Dims d, const doubl
       st = fma(c, fma(t.x, t.x, t.y * t.y), st);
       swt = fma(c, fma(w.x, t.x, w.y * t.y), swt);
     }
-    const int col = m % d.Mc;
-    const double wt = (col == 0) ? 1.0 : 2.0;
+    const double wt = hweight(d, m);
     const double ksq = fma(kx[m], kx[m], ky[m] * ky[m]);
     v[0] = 0.5 * wt * ksq * fma(pbt.x, pbt.x, pbt.y * pbt.y);  // KE_bt
     v[1] = 0.5 * wt * ksq * spsi;                              // KE_tot
@@ -134,7 +139,7 @@ __global__ void __launch_bounds__(kDiagThreads) k_spec_modes(Dims d, const doubl
     pbt = caxpy(cc[j], psi, pbt);
     spsi = fma(cc[j], fma(psi.x, psi.x, psi.y * psi.y), spsi);
   }
-  const double wt = (m % d.Mc == 0) ? 1.0 : 2.0;
+  const double wt = hweight(d, m);
   const double ksq = fma(kx[m], kx[m], ky[m] * ky[m]);
   per_mode[m] = 0.5 * wt * ksq * fma(pbt.x, pbt.x, pbt.y * pbt.y);
   per_mode[d.M + m] = 0.5 * wt * ksq * spsi;
@@ -178,7 +183,7 @@ __global__ void k_vspec(Dims d, const double2* __restrict__ q, const double2* __
     const double2 x = src[(size_t)n * d.M + m];
     double a2 = fma(x.x, x.x, x.y * x.y);
     if (f == 3) {
-      const double wt = (m % d.Mc == 0) ? 1.0 : 2.0;
+      const double wt = hweight(d, m);
       const double ksq = fma(kx[m], kx[m], ky[m] * ky[m]);
       a2 *= wt * ksq * inv_denom[m] * inv_denom[m];
     }

@@ -1,14 +1,18 @@
-// 2/3-rule dealiased horizontal products (FP64), three kernels per call.
+// Dealiased horizontal products (FP64 or FP32), three kernels per call.
 //
-// Reference semantics: nhqg/spectral.py:307-328 (flux form: D = i kx F(u f) +
-// i ky F(v f) with u = -psi_y, v = psi_x), :281-304 (Jacobian form
-// J = psi_x f_y - psi_y f_x), :53-60 (sponge mask * rfft2(sigma * irfft2 f)),
-// each masked to |kx|, ky <= Nx/3, batched over levels (:331-358).
+// Reference semantics, 2/3 rule: nhqg/spectral.py:307-328 (flux form: D =
+// i kx F(u f) + i ky F(v f) with u = -psi_y, v = psi_x), :281-304 (Jacobian
+// form J = psi_x f_y - psi_y f_x), :53-60 (sponge mask * rfft2(sigma *
+// irfft2 f)), each masked to |kx|, ky <= Nx/3, batched over levels
+// (:331-358).  3/2 rule: the same products on the zero-padded N = 3Nx/2 grid
+// (:18-50 pad / truncate, :63-75 sponge, :147-253 products): the transforms
+// below run at length N, the input spectra enter at their padded rows, the
+// outputs are read back at the kept rows, and the (N/Nx)^2 of the truncation
+// is folded into the input scale (1/(N Nx) per factor).
 //
 //   H1  per (level, ky column): inverse complex FFT over kx of the derived
 //       spectra (u, v, q+eta, w, theta, or the Jacobian's derivatives) -- only
-//       the in-band ky columns exist, so only Mc of the Nk columns are
-//       transformed.
+//       the stored ky columns exist, so only Mc columns are transformed.
 //   H2  per (level, pair of x rows): two real rows share one complex FFT
 //       (c2r via the Hermitian extension, numpy irfft semantics: the imaginary
 //       parts of the ky=0 / Nyquist bins are ignored), pointwise products,
@@ -16,7 +20,8 @@
 //       sponge term are applied to the ky <= K outputs.
 //   H3  per (level, ky column): forward complex FFT over x, combine
 //       i kx G + H, keep the in-band kx rows.
-// Scaling: numpy's irfft2 carries 1/Nx^2, folded into H1's input spectra.
+// Scaling: numpy's irfft2 carries 1/N^2, folded into H1's input spectra
+// together with the truncation's (N/Nx)^2.
 #include "engine.h"
 
 namespace nhqg {
@@ -28,13 +33,14 @@ struct HK {
   using T = decltype(C().x);
   // geometry
   int Nx, Nk, K, Mr, Mc, M;
-  int sx;  // shared-memory stride of one FFT sequence (Nx plus FP32 padding)
+  int N;   // transform length: Nx (2/3 rule) or the padded 3Nx/2 (3/2 rule)
+  int sx;  // shared-memory stride of one FFT sequence (N plus FP32 padding)
   int levels;
   int rows_in, cols_in;  // input plane extent (compact Mr x Mc or full Nx x Nk)
   bool full_in, full_out;
   int form, nf1, nprod, ng;
   bool sponge, eta, psi_derived;
-  T scale;  // 1/Nx^2
+  T scale;  // 1/(N Nx)
   FftPlan plan;
   const CI *psi, *q, *w, *th;
   const T *kx_full, *ky_full;
@@ -59,7 +65,7 @@ __host__ __device__ constexpr int pad_shift() { return sizeof(C) == sizeof(float
 // H1 -> H2 -> H3 intermediates, pair-major: [field][level][x/2][column][x%2]
 template <typename K>
 __device__ __forceinline__ size_t xidx(const K& k, int f, int lev, int pair, int c, int cols) {
-  return ((((size_t)f * k.levels + lev) * (k.Nx / 2) + pair) * cols + c) * 2;
+  return ((((size_t)f * k.levels + lev) * (k.N / 2) + pair) * cols + c) * 2;
 }
 
 template <typename K>
@@ -69,7 +75,7 @@ __device__ __forceinline__ int plane_index(const K& k, int r, int c) {
 
 template <typename K, typename C>
 __device__ __forceinline__ void load_tables(const K& k, C* tw_s, int* perm_s) {
-  for (int i = threadIdx.x; i < k.Nx; i += blockDim.x) {
+  for (int i = threadIdx.x; i < k.N; i += blockDim.x) {
     tw_s[i] = k.tw[i];
     perm_s[i] = k.perm[i];
   }
@@ -81,8 +87,8 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
   using T = decltype(C().x);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw_s = reinterpret_cast<C*>(smem_raw);
-  int* perm_s = reinterpret_cast<int*>(tw_s + k.Nx);
-  C* seq = reinterpret_cast<C*>(perm_s + ((k.Nx + 3) / 4) * 4);
+  int* perm_s = reinterpret_cast<int*>(tw_s + k.N);
+  C* seq = reinterpret_cast<C*>(perm_s + ((k.N + 3) / 4) * 4);
   const int lev = blockIdx.y;
   const int c0 = blockIdx.x * CB;
   const int ncb = min(CB, k.cols_in - c0);
@@ -95,11 +101,11 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
   const size_t plane = (size_t)k.rows_in * k.cols_in;
   for (int i = threadIdx.x; i < k.rows_in * ncb; i += blockDim.x) {
     const int r = i / ncb, cc = i - r * ncb, c = c0 + cc;
-    const int kf = k.full_in ? r : full_row(r, k.K, k.Nx);
+    const int kf = k.full_in ? r : full_row(r, k.K, k.Mr, k.Nx);
     const size_t off = (size_t)lev * plane + plane_index(k, r, c);
     const T kxs = k.kx_full[kf] * k.scale;
     const T kys = k.ky_full[c] * k.scale;
-    const int pos = perm_s[kf];
+    const int pos = perm_s[padded_row(kf, k.Nx, k.N)];
     C* s0 = seq + (size_t)cc * k.sx + fft_pad<PS>(pos);
     const size_t fs = (size_t)CB * k.sx;  // stride between fields
     if (k.form == HF_SPONGE) {
@@ -143,8 +149,8 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
   fft_dit_inv<C, PS>(seq, nseq, k.sx, k.plan, tw_s);
   // pair-major output: consecutive threads take (x parity, column), so the
   // row pairs H2 reads are contiguous
-  const int half = k.Nx / 2;
-  for (int i = threadIdx.x; i < k.nf1 * ncb * k.Nx; i += blockDim.x) {
+  const int half = k.N / 2;
+  for (int i = threadIdx.x; i < k.nf1 * ncb * k.N; i += blockDim.x) {
     const int par = i & 1, r2 = i >> 1;
     const int cc = r2 % ncb, r3 = r2 / ncb;
     const int pp = r3 % half, f = r3 / half;
@@ -159,8 +165,8 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
   using T = decltype(C().x);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw_s = reinterpret_cast<C*>(smem_raw);
-  int* perm_s = reinterpret_cast<int*>(tw_s + k.Nx);
-  C* in = reinterpret_cast<C*>(perm_s + ((k.Nx + 3) / 4) * 4);
+  int* perm_s = reinterpret_cast<int*>(tw_s + k.N);
+  C* in = reinterpret_cast<C*>(perm_s + ((k.N + 3) / 4) * 4);
   constexpr int PS = pad_shift<C>();
   const int NPR = RB / 2;
   C* pr = in + (size_t)k.nf1 * NPR * k.sx;
@@ -169,7 +175,7 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
   load_tables(k, tw_s, perm_s);
   for (int i = threadIdx.x; i < k.nf1 * NPR * k.sx; i += blockDim.x) in[i] = gmk<C>(T(0), T(0));
   __syncthreads();
-  const int half = k.Nx / 2;
+  const int half = k.N / 2;
   // Hermitian-extended spectra of row pairs (a, b): Z = Xa + i Xb
   for (int i = threadIdx.x; i < k.nf1 * NPR * k.cols_in; i += blockDim.x) {
     const int c = i % k.cols_in;
@@ -183,25 +189,25 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
       s[fft_pad<PS>(perm_s[c])] = gmk<C>(A.x, B.x);
     } else {
       s[fft_pad<PS>(perm_s[c])] = gmk<C>(A.x - B.y, A.y + B.x);
-      s[fft_pad<PS>(perm_s[k.Nx - c])] = gmk<C>(A.x + B.y, B.x - A.y);
+      s[fft_pad<PS>(perm_s[k.N - c])] = gmk<C>(A.x + B.y, B.x - A.y);
     }
   }
   __syncthreads();
   fft_dit_inv<C, PS>(in, k.nf1 * NPR, k.sx, k.plan, tw_s);
   // pointwise products, two rows per complex lane
   const size_t fs = (size_t)NPR * k.sx;
-  for (int i = threadIdx.x; i < NPR * k.Nx; i += blockDim.x) {
-    const int y = i % k.Nx, p = i / k.Nx;
+  for (int i = threadIdx.x; i < NPR * k.N; i += blockDim.x) {
+    const int y = i % k.N, p = i / k.N;
     const int xa = x0 + 2 * p;
     const C* s = in + (size_t)p * k.sx + fft_pad<PS>(y);
     C* o = pr + (size_t)p * k.sx + fft_pad<PS>(y);
     T sa = 0, sb = 0, ea = 0, eb = 0;
     if (k.sponge) {
-      sa = k.sponge_phys[(size_t)xa * k.Nx + y];
-      sb = k.sponge_phys[(size_t)(xa + 1) * k.Nx + y];
+      sa = k.sponge_phys[(size_t)xa * k.N + y];
+      sb = k.sponge_phys[(size_t)(xa + 1) * k.N + y];
       if (k.eta) {
-        ea = k.eta_phys[(size_t)xa * k.Nx + y];
-        eb = k.eta_phys[(size_t)(xa + 1) * k.Nx + y];
+        ea = k.eta_phys[(size_t)xa * k.N + y];
+        eb = k.eta_phys[(size_t)(xa + 1) * k.N + y];
       }
     }
     if (k.form == HF_FLUX) {
@@ -245,7 +251,7 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
     const int rest = i / k.Mc;
     const int p = rest % NPR, g = rest / NPR;
     const int xa = x0 + 2 * p;
-    const int pa = fft_pad<PS>(perm_s[c]), pb = fft_pad<PS>(perm_s[c == 0 ? 0 : k.Nx - c]);
+    const int pa = fft_pad<PS>(perm_s[c]), pb = fft_pad<PS>(perm_s[c == 0 ? 0 : k.N - c]);
     auto split = [&](int prod, C& Xa, C& Xb) {
       const C* s = pr + ((size_t)prod * NPR + p) * k.sx;
       const C A = s[pa], B = s[pb];
@@ -285,15 +291,15 @@ __global__ void __launch_bounds__(256) k_h3(HK<C, CI> k, int CB) {
   using T = decltype(C().x);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tw_s = reinterpret_cast<C*>(smem_raw);
-  int* perm_s = reinterpret_cast<int*>(tw_s + k.Nx);
-  C* seq = reinterpret_cast<C*>(perm_s + ((k.Nx + 3) / 4) * 4);
+  int* perm_s = reinterpret_cast<int*>(tw_s + k.N);
+  C* seq = reinterpret_cast<C*>(perm_s + ((k.N + 3) / 4) * 4);
   const int lev = blockIdx.y;
   const int c0 = blockIdx.x * CB;
   const int ncb = min(CB, k.Mc - c0);
   constexpr int PS = pad_shift<C>();
   load_tables(k, tw_s, perm_s);
-  const int half = k.Nx / 2;
-  for (int i = threadIdx.x; i < k.ng * ncb * k.Nx; i += blockDim.x) {
+  const int half = k.N / 2;
+  for (int i = threadIdx.x; i < k.ng * ncb * k.N; i += blockDim.x) {
     const int par = i & 1, r2 = i >> 1;
     const int cc = r2 % ncb, r3 = r2 / ncb;
     const int pp = r3 % half, g = r3 / half;
@@ -304,8 +310,8 @@ __global__ void __launch_bounds__(256) k_h3(HK<C, CI> k, int CB) {
   const int nout = (k.form == HF_SPONGE) ? 1 : 3;
   for (int i = threadIdx.x; i < k.Mr * ncb; i += blockDim.x) {
     const int r = i / ncb, cc = i - r * ncb, c = c0 + cc;
-    const int kf = full_row(r, k.K, k.Nx);
-    const int pos = fft_pad<PS>(perm_s[kf]);
+    const int kf = full_row(r, k.K, k.Mr, k.Nx);
+    const int pos = fft_pad<PS>(perm_s[padded_row(kf, k.Nx, k.N)]);
     const size_t oidx = k.full_out ? ((size_t)lev * k.Nx + kf) * k.Nk + c
                                    : (size_t)lev * k.M + (size_t)r * k.Mc + c;
     for (int f = 0; f < nout; ++f) {
@@ -334,7 +340,8 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
   HK<C, CI> k;
   const Dims& d = p.d;
   k.Nx = d.Nx; k.Nk = d.Nk; k.K = d.K; k.Mr = d.Mr; k.Mc = d.Mc; k.M = d.M;
-  k.sx = pad_shift<C>() > 0 ? d.Nx + (d.Nx + 7) / 8 : d.Nx;
+  k.N = d.Nh;
+  k.sx = pad_shift<C>() > 0 ? k.N + (k.N + 7) / 8 : k.N;
   k.levels = a.levels;
   k.full_in = a.full_in;
   k.full_out = a.full_out;
@@ -347,22 +354,22 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
   if (a.form == HF_FLUX) { k.nf1 = 5; k.nprod = k.sponge ? 9 : 6; k.ng = 6; }
   else if (a.form == HF_JAC) { k.nf1 = k.sponge ? 11 : 8; k.nprod = 3; k.ng = 3; }
   else { k.nf1 = 1; k.nprod = 1; k.ng = 1; }
-  k.scale = (T)(1.0 / ((double)d.Nx * (double)d.Nx));
+  k.scale = (T)(1.0 / ((double)d.Nh * (double)d.Nx));
   k.plan = p.plan;
   k.psi = a.psi; k.q = a.q; k.w = a.w; k.th = a.th;
   k.kx_full = t.kx_full; k.ky_full = t.ky_full; k.inv_denom = t.inv_denom;
   k.eta_c = t.eta; k.sponge_phys = t.sponge; k.eta_phys = t.eta_phys;
   k.tw = t.tw; k.perm = t.perm;
   k.Aq = a.Aq; k.Aw = a.Aw; k.Ath = a.Ath;
-  const size_t need1 = (size_t)k.nf1 * a.levels * k.cols_in * d.Nx;
-  const size_t need2 = (size_t)k.ng * a.levels * d.Mc * d.Nx;
+  const size_t need1 = (size_t)k.nf1 * a.levels * k.cols_in * d.Nh;
+  const size_t need2 = (size_t)k.ng * a.levels * d.Mc * d.Nh;
   const size_t cap1 = w.x1_elems * sizeof(double2) / sizeof(C);
   const size_t cap2 = w.x2_elems * sizeof(double2) / sizeof(C);
   if (need1 > cap1 || need2 > cap2) return cudaErrorInvalidValue;
   k.x1 = reinterpret_cast<C*>(w.x1);
   k.x2 = reinterpret_cast<C*>(w.x2);
 
-  const size_t tb = table_bytes<C>(d.Nx);
+  const size_t tb = table_bytes<C>(d.Nh);
   const size_t budget = 200 * 1024;
   // FP64: the FP64 pipe is the limit, large tiles amortise the tables; FP32:
   // shared-memory latency is the limit, small tiles keep 4 CTAs per SM
@@ -375,7 +382,7 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
   size_t sm1 = tb + (size_t)k.nf1 * CB1 * seqb;
   if (sm1 > budget) return cudaErrorInvalidConfiguration;
   int RB = 2;
-  while (RB * 2 <= 16 && d.Nx % (RB * 2) == 0 &&
+  while (RB * 2 <= 16 && d.Nh % (RB * 2) == 0 &&
          tb + (size_t)(k.nf1 + k.nprod) * RB * seqb <= budget2)
     RB *= 2;
   size_t sm2 = tb + (size_t)(k.nf1 + k.nprod) * (RB / 2) * seqb;
@@ -392,7 +399,7 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
   w.prof.begin(sizeof(T) == 4 ? "h1_col_ifft_f32" : "h1_col_ifft", st);
   k_h1<C, CI><<<g1, 256, sm1, st>>>(k, CB1);
   w.prof.end(st);
-  dim3 g2(d.Nx / RB, a.levels);
+  dim3 g2(d.Nh / RB, a.levels);
   w.prof.begin(sizeof(T) == 4 ? "h2_row_products_f32" : "h2_row_products", st);
   k_h2<C, CI><<<g2, 256, sm2, st>>>(k, RB);
   w.prof.end(st);

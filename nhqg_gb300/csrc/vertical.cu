@@ -519,7 +519,7 @@ __global__ void k_gather(Dims d, const double2* full, double2* cmp, int levels, 
     const int kxi = row <= d.Nx / 2 ? row : row - d.Nx;
     const double2 v = full[i];
     if (abs(kxi) <= d.K && c <= d.K) {
-      const int r = kxi >= 0 ? kxi : kxi + 2 * d.K + 1;
+      const int r = kxi >= 0 ? kxi : kxi + d.Mr;
       cmp[(size_t)l * d.M + r * d.Mc + c] = v;
     } else if (v.x != 0.0 || v.y != 0.0) {
       outside_nonzero = true;
@@ -539,14 +539,16 @@ __global__ void k_scatter(Dims d, const double2* cmp, double2* full, int levels)
     const int kxi = row <= d.Nx / 2 ? row : row - d.Nx;
     double2 v = czero();
     if (abs(kxi) <= d.K && c <= d.K) {
-      const int r = kxi >= 0 ? kxi : kxi + 2 * d.K + 1;
+      const int r = kxi >= 0 ? kxi : kxi + d.Mr;
       v = cmp[(size_t)l * d.M + r * d.Mc + c];
     }
     full[i] = v;
   }
 }
 
-// zero the k=0 mode, Hermitian-project the ky=0 column (2/3 band kept)
+// zero the k=0 mode, Hermitian-project the ky=0 column and, in the
+// full-band layout of the 3/2 rule, the ky = Nx/2 column
+// (nhqg/solver.py:107-146, 993-999)
 __global__ void k_finalize(Dims d, const double2* q, const double2* w, const double2* th,
                            double2* qo, double2* wo, double2* to) {
   const int nlev[3] = {d.P, d.G, d.G};
@@ -554,6 +556,7 @@ __global__ void k_finalize(Dims d, const double2* q, const double2* w, const dou
   double2* dst[3] = {qo, wo, to};
   const size_t per = (size_t)d.M;
   const size_t total = (size_t)(d.P + 2 * d.G) * per;
+  const int cnyq = d.pad ? d.Nk - 1 : -1;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     int f = 0;
@@ -563,33 +566,38 @@ __global__ void k_finalize(Dims d, const double2* q, const double2* w, const dou
     const size_t lbase = j - m;
     const int r = m / d.Mc, c = m - r * d.Mc;
     double2 v;
-    if (c != 0) {
+    if (c != 0 && c != cnyq) {
       v = src[f][j];
     } else {
-      const int rm = mirror_row(r, d.K);
-      double2 a = (r == 0) ? czero() : src[f][lbase + (size_t)r * d.Mc];
-      double2 b = (rm == 0) ? czero() : src[f][lbase + (size_t)rm * d.Mc];
+      const int rm = mirror_row(r, d.Mr);
+      const bool z0 = c == 0;  // the zeroed k = 0 mode sits in the ky = 0 column
+      double2 a = (z0 && r == 0) ? czero() : src[f][lbase + (size_t)r * d.Mc + c];
+      double2 b = (z0 && rm == 0) ? czero() : src[f][lbase + (size_t)rm * d.Mc + c];
       v = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
     }
     dst[f][j] = v;
   }
 }
 
-// Hermitian projection of the ky=0 column, in place (no k=0 zeroing)
+// Hermitian projection of the ky=0 column (and of the ky = Nx/2 column in the
+// full-band layout), in place (no k=0 zeroing)
 __global__ void k_hermitian(Dims d, double2* q, double2* w, double2* th) {
   const int nlev[3] = {d.P, d.G, d.G};
   double2* f3[3] = {q, w, th};
-  const int half = d.K;  // rows 1..K pair with 2K..K+1
-  const int total = (d.P + 2 * d.G) * (half + 1);
+  const int half = d.Mr / 2;  // rows 1..half pair with Mr-1..Mr-half
+  const int ncol = d.pad ? 2 : 1;
+  const int per = ncol * (half + 1);
+  const int total = (d.P + 2 * d.G) * per;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
     int f = 0, j = i;
-    while (j >= nlev[f] * (half + 1)) { j -= nlev[f] * (half + 1); ++f; }
-    const int l = j / (half + 1), r = j - l * (half + 1);
-    double2* col = f3[f] + (size_t)l * d.M;  // c = 0 entries at row*Mc
+    while (j >= nlev[f] * per) { j -= nlev[f] * per; ++f; }
+    const int l = j / per, rc = j - l * per;
+    const int ci = rc / (half + 1), r = rc - ci * (half + 1);
+    double2* col = f3[f] + (size_t)l * d.M + (ci == 0 ? 0 : d.Nk - 1);  // entries at row*Mc
     if (r == 0) {
       col[0] = make_double2(col[0].x, 0.0);
     } else {
-      const int rm = mirror_row(r, d.K);
+      const int rm = mirror_row(r, d.Mr);
       const double2 a = col[(size_t)r * d.Mc], b = col[(size_t)rm * d.Mc];
       const double2 h = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
       col[(size_t)r * d.Mc] = h;
@@ -598,10 +606,13 @@ __global__ void k_hermitian(Dims d, double2* q, double2* w, double2* th) {
   }
 }
 
-// mean over the Nx x Nx grid of irfft2(a) * irfft2(b), per level, by Parseval
-// Horizontal mean of a b* per level by Parseval: every mode of the half
-// plane counts twice except the ky = 0 column, which enters through its
-// Hermitian projection.  Each level is split into kParSeg segments, one CTA
+// Horizontal mean of irfft2(a) irfft2(b) per level by Parseval: every mode of
+// the half plane counts twice except the ky = 0 column, which enters through
+// its Hermitian projection.  In the full-band layout of the 3/2 rule the
+// means are those of the zero-padded fields (nhqg/solver.py:204-245): the
+// ky = Nx/2 column is an ordinary column of the padded grid (weight 2), and
+// the kx Nyquist entry of the ky = 0 column sits at kx = -Nx/2 alone, so its
+// Hermitian part contributes Re(a b*)/2.  Each level is split into kParSeg segments, one CTA
 // each; the last CTA of a level to finish adds the segment sums in segment
 // order (deterministic) and resets the level's counter for the next launch.
 constexpr int kParSeg = 8;
@@ -629,12 +640,17 @@ __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const
   for (int r = threadIdx.x; r < d.Mr; r += blockDim.x) {
     const int m = r * d.Mc;
     if (m < m0 || m >= m1) continue;
-    const int rm = mirror_row(r, d.K);
+    const int rm = mirror_row(r, d.Mr);
     const double2 x = al[m], xm = al[rm * d.Mc];
     const double2 y = bl[m], ym = bl[rm * d.Mc];
+    const double xy = fma(x.x, y.x, x.y * y.y);
+    if (rm == r && r != 0) {  // padded kx Nyquist (full-band layout only)
+      acc += 0.5 * xy - 2.0 * xy;
+      continue;
+    }
     const double hx_re = 0.5 * (x.x + xm.x), hx_im = 0.5 * (x.y - xm.y);
     const double hy_re = 0.5 * (y.x + ym.x), hy_im = 0.5 * (y.y - ym.y);
-    acc += fma(hx_re, hy_re, hx_im * hy_im) - 2.0 * fma(x.x, y.x, x.y * y.y);
+    acc += fma(hx_re, hy_re, hx_im * hy_im) - 2.0 * xy;
   }
   const double tot = block_sum(acc, scratch);
   if (threadIdx.x == 0) {

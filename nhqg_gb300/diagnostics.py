@@ -22,7 +22,7 @@ import torch
 
 from . import _native as nat
 from .engine import engine_for
-from .grid import Grid
+from .grid import Grid, compact_layout
 from .solver import to_device
 
 DIAG_KEYS = nat.DIAG_KEYS
@@ -47,8 +47,8 @@ def shell_table(grid: Grid, n_bins: int | None = None):
     """(bin centres, shell index of every compact mode) under the reference's
     test i dk <= |k| < (i+1) dk with dk = 2 pi / L and n_bins = int(k_max / dk)
     + 1 by default, k_max over the whole rfft grid (nhqg/diagnostics.py:56-77).
-    Compact mode m = r (K+1) + c holds kx row r (r <= K) or Nx - (2K+1) + r and
-    ky column c, K = Nx // 3."""
+    Compact mode m = r Mc + c holds kx row rows[r] and ky column c, with
+    (rows, Mc) the engine's compact layout (grid.compact_layout)."""
     key = (id(grid), n_bins)
     if key not in _SHELLS:
         ksq = np.asarray(grid.ksq, dtype=np.float64)
@@ -59,9 +59,8 @@ def shell_table(grid: Grid, n_bins: int | None = None):
         idx = np.full(ksq.shape, -1, dtype=np.int32)
         for i in range(nb):
             idx[(k_mag >= i * dk) & (k_mag < (i + 1) * dk)] = i
-        Nx, K = grid.Nx, grid.Nx // 3
-        rows = [r if r <= K else Nx - (2 * K + 1) + r for r in range(2 * K + 1)]
-        compact = np.ascontiguousarray(idx[rows][:, :K + 1].reshape(-1))
+        rows, ncol = compact_layout(grid)
+        compact = np.ascontiguousarray(idx[rows][:, :ncol].reshape(-1))
         _SHELLS[key] = (np.arange(nb) * dk + dk / 2, compact, grid)
     k_bins, compact, _ = _SHELLS[key]
     return k_bins, compact

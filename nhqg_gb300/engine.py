@@ -13,7 +13,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from .grid import Grid
+from .grid import Grid, _zero_pad
 
 _ENGINES: dict[tuple, "Engine"] = {}
 
@@ -74,14 +74,24 @@ class Engine:
         d.shell_of_mode = rows.ctypes.data_as(nat.c_int_p)
         keep["shell_inv"] = np.ascontiguousarray(g.imex_inv, dtype=np.float64)
         d.shell_inv = _dptr(keep["shell_inv"])
+        self.pad32 = g.horizontal_dealiasing == "32_rule"
+        d.horizontal_dealiasing = nat.DEALIAS[g.horizontal_dealiasing]
         if g.eta_hat is not None:
             e = np.ascontiguousarray(np.asarray(g.eta_hat, dtype=np.complex128))
             keep["eta"] = e
             d.eta_hat = ctypes.cast(e.ctypes.data, nat.c_double_p)
-            eta_phys = g.eta_phys if g.eta_phys is not None else np.fft.irfft2(e, s=(g.Nx, g.Nx))
+            # physical eta on the products' grid, derived from eta_hat so that a
+            # replaced eta_hat cannot disagree with it
+            if self.pad32:
+                eta_phys = np.fft.irfft2(_zero_pad(e, g.Nx, g.Npad), s=(g.Npad, g.Npad))
+            else:
+                eta_phys = np.fft.irfft2(e, s=(g.Nx, g.Nx))
             d.eta_phys = arr("eta_phys", eta_phys)
-        if g.sponge_phys is not None:
-            d.sponge_phys = arr("sponge", g.sponge_phys)
+        sponge = g.sponge_phys_pad if self.pad32 else g.sponge_phys
+        if g.sponge_phys is not None and sponge is None:
+            raise ValueError("a 3/2-rule grid with a sponge needs sponge_phys_pad")
+        if sponge is not None:
+            d.sponge_phys = arr("sponge", sponge)
         if g.mean_solve is not None:
             d.mean_solve = arr("mean_solve", g.mean_solve)
         if getattr(g, "imex_shell_coef", None) is not None:
@@ -206,11 +216,12 @@ class Engine:
         nat.check(self.lib.nhqg_sanitize(self.handle, ctypes.byref(s), _stream_handle()), "nhqg_sanitize")
 
     def triple_advection(self, advection: str, psi, q, w, th, Aq, Aw, Ath) -> None:
+        """The grid's products (2/3 or 3/2 rule) of (levels, Nx, Nk) planes."""
         levels = int(q.shape[0])
-        nat.check(self.lib.nhqg_triple_advection_23(
+        name = "nhqg_triple_advection_32" if self.pad32 else "nhqg_triple_advection_23"
+        nat.check(getattr(self.lib, name)(
             self.handle, nat.ADV[advection], levels, psi.data_ptr(), q.data_ptr(), w.data_ptr(),
-            th.data_ptr(), Aq.data_ptr(), Aw.data_ptr(), Ath.data_ptr(), _stream_handle()),
-            "nhqg_triple_advection_23")
+            th.data_ptr(), Aq.data_ptr(), Aw.data_ptr(), Ath.data_ptr(), _stream_handle()), name)
 
     def diagnostics(self, q, w, th, tb) -> torch.Tensor:
         """NHQG_DIAG_COUNT doubles on the device (order of _native.DIAG_KEYS)."""
@@ -249,13 +260,14 @@ class Engine:
         return self.tiles()
 
     def sponge_product(self, f, out) -> None:
-        nat.check(self.lib.nhqg_sponge_product_23(self.handle, int(f.shape[0]), f.data_ptr(),
-                                                  out.data_ptr(), _stream_handle()),
-                  "nhqg_sponge_product_23")
+        name = "nhqg_sponge_product_32" if self.pad32 else "nhqg_sponge_product_23"
+        nat.check(getattr(self.lib, name)(self.handle, int(f.shape[0]), f.data_ptr(),
+                                          out.data_ptr(), _stream_handle()), name)
 
 
 def _key(grid: Grid) -> tuple:
     return (id(grid.imex_inv), id(grid.V), id(grid.eta_hat), id(grid.sponge_phys),
+            id(grid.sponge_phys_pad), grid.horizontal_dealiasing,
             id(grid.cgl_to_sbp), grid.thermal_closure, grid.mean_exchange_discretization,
             grid.nonlinear_advection, grid.w_bc_top, int(grid.sbp_corrector_substeps),
             float(grid.dt), float(grid.beta), float(grid.mean_temp_eps_sq))

@@ -94,13 +94,17 @@ class Grid(NamedTuple):
     imex_matmul_chunk: int
     # GPU-engine extras
     imex_shell_row: np.ndarray       # (Nx, Nk) row of imex_inv, -1 outside the band
-    eta_phys: np.ndarray | None      # (Nx, Nx) irfft2(eta_hat)
+    eta_phys: np.ndarray | None      # irfft2(eta_hat) on the Nx grid (2/3 rule), or of the
+                                     # zero-padded eta_hat on the Npad grid (3/2 rule)
     mean_solve: np.ndarray | None    # (P, P) inverse of the tau'd legacy mean operator
     imex_shell_coef: np.ndarray      # (rows of imex_inv, 2) alpha_w_eff, (gamma dt)^2 c_k / alpha_q
     cfg: NHQGConfig
+    # (Npad, Npad) irfft2 of the zero-padded sigma, no rescale (nhqg/grid.py:110-113, 663-667)
+    sponge_phys_pad: np.ndarray | None = None
 
 
 _CLOSURES = ("fixed_conduction", "evolve_mean")
+_DEALIASING = ("23_rule", "32_rule")
 _EXCHANGES = ("legacy", "balanced_sbp2", "balanced_sbp2_pc")
 
 
@@ -200,12 +204,41 @@ def _shell_inverse(kv, hyper_order, gamma, dt, nu_q, nu_w, nu_theta, drag, sigma
     return np.linalg.inv(couple - (gamma * dt) ** 2 * c_k * B), coef
 
 
+def _smooth_23(n: int) -> bool:
+    while n % 2 == 0:
+        n //= 2
+    while n % 3 == 0:
+        n //= 3
+    return n == 1
+
+
+def _zero_pad(f_hat: np.ndarray, Nx: int, Npad: int) -> np.ndarray:
+    """(Nx, Nk) spectrum onto the (Npad, Npad//2+1) grid (nhqg/spectral.py:18-34)."""
+    out = np.zeros((Npad, Npad // 2 + 1), dtype=np.complex128)
+    out[:Nx // 2, :Nx // 2 + 1] = f_hat[:Nx // 2]
+    out[Npad - Nx // 2:, :Nx // 2 + 1] = f_hat[Nx // 2:]
+    return out
+
+
+def compact_layout(grid: Grid) -> tuple[np.ndarray, int]:
+    """Rows (fftfreq order) and column count of the engine's compact mode
+    layout: the 2/3-rule keep-rectangle, or every rfft2 mode (3/2 rule)."""
+    Nx = grid.Nx
+    if grid.horizontal_dealiasing == "32_rule":
+        return np.arange(Nx), Nx // 2 + 1
+    K = Nx // 3
+    return np.concatenate([np.arange(K + 1), np.arange(Nx - K, Nx)]), K + 1
+
+
 def make_grid(cfg: NHQGConfig) -> Grid:
     """Build the Grid of ``cfg`` (nhqg/grid.py:439-789)."""
     if cfg.float_dtype != "float64":
         raise ValueError("the GPU time step computes in float64; set float_dtype='float64'")
-    if cfg.horizontal_dealiasing != "23_rule":
-        raise ValueError("the GPU time step implements horizontal_dealiasing='23_rule'")
+    if cfg.horizontal_dealiasing not in _DEALIASING:
+        raise ValueError(f"Unsupported horizontal_dealiasing={cfg.horizontal_dealiasing!r}")
+    full = cfg.horizontal_dealiasing == "32_rule"
+    if full and not _smooth_23(3 * cfg.Nx // 2):
+        raise ValueError(f"the 3/2 rule needs Npad = 3Nx/2 = 2^a 3^b (Nx={cfg.Nx})")
     if cfg.q_boundary != "none":
         raise ValueError(f"Unsupported q_boundary={cfg.q_boundary!r} (GPU path: 'none')")
     if cfg.vertical_dealiasing != "none":
@@ -293,8 +326,10 @@ def make_grid(cfg: NHQGConfig) -> Grid:
     K = Nx // 3
     ii = np.arange(Nx)
     kint = np.where(ii <= Nx // 2, ii, ii - Nx)
-    in_band = (np.abs(kint)[:, None] <= K) & (np.arange(Nk)[None, :] <= K)
-    mask = in_band.astype(np.float64)
+    mask = ((np.abs(kint)[:, None] <= K) & (np.arange(Nk)[None, :] <= K)).astype(np.float64)
+    # modes the engine stores: the 2/3 keep-rectangle, or all of them (3/2 rule)
+    in_band = np.ones((Nx, Nk), dtype=bool) if full else mask != 0
+    Npad = cfg.Npad
 
     if cfg.gamma != 0.0 and cfg.beta != 0.0:
         raise ValueError("gamma (polar trap) and beta (flat beta-plane) are mutually exclusive")
@@ -313,9 +348,12 @@ def make_grid(cfg: NHQGConfig) -> Grid:
             raise ValueError(
                 f"Trap background PV is under-resolved: {e_out / e_tot:.2e} of its spectral "
                 f"energy lies outside the 2/3 band (tolerance 1e-10)")
-        eta_hat = eta_hat * mask
-        eta_phys = np.fft.irfft2(eta_hat, s=(Nx, Nx))
-    sponge_phys = None
+        if full:
+            eta_phys = np.fft.irfft2(_zero_pad(eta_hat, Nx, Npad), s=(Npad, Npad))
+        else:
+            eta_hat = eta_hat * mask
+            eta_phys = np.fft.irfft2(eta_hat, s=(Nx, Nx))
+    sponge_phys = sponge_phys_pad = None
     if cfg.sponge_rate < 0.0:
         raise ValueError("sponge_rate must be >= 0")
     if cfg.sponge_rate > 0.0:
@@ -334,7 +372,10 @@ def make_grid(cfg: NHQGConfig) -> Grid:
             raise ValueError(
                 f"Sponge profile is under-resolved: {s_out / s_tot:.2e} of its spectral "
                 f"energy lies outside the 2/3 band (tolerance 1e-10)")
-        sponge_phys = np.fft.irfft2(sig_hat * mask, s=(Nx, Nx))
+        if not full:
+            sig_hat = sig_hat * mask
+        sponge_phys = np.fft.irfft2(sig_hat, s=(Nx, Nx))
+        sponge_phys_pad = np.fft.irfft2(_zero_pad(sig_hat, Nx, Npad), s=(Npad, Npad))
 
     # implicit coefficient of the scheme (nhqg/grid.py:671-676)
     gamma_imex = 1.0 - 1.0 / np.sqrt(2.0) if cfg.imex_scheme == "ars222" else 0.5
@@ -395,5 +436,5 @@ def make_grid(cfg: NHQGConfig) -> Grid:
         sbp_corrector_substeps=int(cfg.sbp_corrector_substeps),
         imex_matmul_chunk=int(cfg.imex_matmul_chunk),
         imex_shell_row=shell_row, eta_phys=eta_phys, mean_solve=mean_solve,
-        imex_shell_coef=shell_coef, cfg=cfg,
+        imex_shell_coef=shell_coef, cfg=cfg, sponge_phys_pad=sponge_phys_pad,
     )

@@ -15,14 +15,18 @@ import numpy as np
 from .grid import Grid
 
 
-def _sanitize_host(f: np.ndarray, Nx: int, mask: np.ndarray) -> np.ndarray:
+def _sanitize_host(f: np.ndarray, Nx: int, grid: Grid) -> np.ndarray:
+    """sanitize_state on one field (nhqg/solver.py:107-146): Hermitian ky = 0
+    and Nyquist columns, then the 2/3 band limit under the 2/3 rule only."""
     neg = (-np.arange(Nx)) % Nx
     f = f.copy()
     col = f[:, :, 0]
     f[:, :, 0] = 0.5 * (col + np.conj(col[:, neg]))
     col = f[:, :, -1]
     f[:, :, -1] = 0.5 * (col + np.conj(col[:, neg]))
-    return f * mask[None]
+    if grid.horizontal_dealiasing == "23_rule":
+        f = f * grid.mask_23[None]
+    return f
 
 
 def theta_perturbation_state(grid: Grid, seed: int = 0, amplitude: float = 1e-3):
@@ -36,7 +40,7 @@ def theta_perturbation_state(grid: Grid, seed: int = 0, amplitude: float = 1e-3)
     th_gal = th_gal.reshape(P - 2, Nx, Nx // 2 + 1)
     q = np.zeros((P, Nx, Nx // 2 + 1), dtype=np.complex128)
     w = np.zeros_like(th_gal)
-    return (q, w, _sanitize_host(th_gal, Nx, grid.mask_23), np.zeros(P))
+    return (q, w, _sanitize_host(th_gal, Nx, grid), np.zeros(P))
 
 
 # ---------------------------------------------------------------------------
@@ -125,4 +129,4 @@ def make_initial_state(grid: Grid, seed: int = 0, amplitude: float = 1e-3):
         raise ValueError(f"q_boundary={grid.q_boundary!r} is not supported")
     G = grid.Nz - 1
     z = np.zeros((G, Nx, Nk), dtype=np.complex128)
-    return (_sanitize_host(q_hat, Nx, grid.mask_23), z, z.copy(), np.zeros(P))
+    return (_sanitize_host(q_hat, Nx, grid), z, z.copy(), np.zeros(P))

@@ -30,6 +30,9 @@ from .nhqg_oracle import (  # noqa: F401
     triple_conservative_flux_divergence_23,
     triple_jacobian_23,
     sponge_product_23,
+    triple_conservative_flux_divergence_32,
+    triple_jacobian_32,
+    sponge_product_32,
     compute_diagnostics,
     DIAG_KEYS,
     energy_spectrum,

@@ -25,10 +25,37 @@ CFGS = [
 ]
 
 
+# 3/2 rule (full band): every shell has a table row; trap eta (unmasked) and
+# the padded sponge
+CFGS_32 = [
+    dict(CFGS[0], horizontal_dealiasing="32_rule"),
+    dict(Nx=96, Nz=8, L=40.0, gamma=2.2e-3, trap_r_star=8.0, trap_sharpness=5.0, sponge_rate=5.0,
+         sponge_r_start=10.4, sponge_sharpness=5.0, dt=1e-4, horizontal_dealiasing="32_rule"),
+]
+
+
 def _pair(over):
     base = dict(float_dtype="float64", horizontal_dealiasing="23_rule")
     base.update(over)
     return make_grid(NHQGConfig(**base)), oracle.make_grid(OracleConfig(**base))
+
+
+@pytest.mark.parametrize("over", CFGS_32)
+def test_grid_32_rule_matches_oracle(over):
+    g, o = _pair(over)
+    assert g.Npad == o.Npad == 3 * g.Nx // 2
+    assert np.all(g.imex_shell_row >= 0)
+    assert np.array_equal(g.imex_inv[g.imex_shell_row], o.imex_inv[o.ksq_idx])
+    for name in ("eta_hat", "sponge_phys", "sponge_phys_pad"):
+        a, b = getattr(g, name), getattr(o, name)
+        assert (a is None) == (b is None), name
+        if a is not None:
+            assert np.array_equal(np.asarray(a), np.asarray(b)), name
+    if g.eta_hat is not None:
+        pad = np.zeros((g.Npad, g.Npad // 2 + 1), dtype=np.complex128)
+        pad[:g.Nx // 2, :g.Nk] = g.eta_hat[:g.Nx // 2]
+        pad[g.Npad - g.Nx // 2:, :g.Nk] = g.eta_hat[g.Nx // 2:]
+        assert np.allclose(g.eta_phys, np.fft.irfft2(pad, s=(g.Npad, g.Npad)), rtol=0, atol=1e-15)
 
 
 @pytest.mark.parametrize("over", CFGS)
@@ -67,8 +94,10 @@ def test_theta_init_matches_reference_fixture():
 
 
 def test_unsupported_configs_raise():
+    with pytest.raises(ValueError):  # 3/2 rule with Npad = 30 (a factor 5)
+        make_grid(NHQGConfig(Nx=20, Nz=8, float_dtype="float64"))
     with pytest.raises(ValueError):
-        make_grid(NHQGConfig(Nx=32, Nz=8, float_dtype="float64"))  # 3/2 rule
+        make_grid(NHQGConfig(Nx=32, Nz=8, float_dtype="float64", horizontal_dealiasing="45_rule"))
     with pytest.raises(ValueError):
         make_grid(NHQGConfig(Nx=32, Nz=8, float_dtype="float32", horizontal_dealiasing="23_rule"))
     with pytest.raises(ValueError):
