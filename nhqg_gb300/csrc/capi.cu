@@ -274,6 +274,12 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.tw_v, tw.data(), L);
     UP(t.cs_v, cs.data(), L + 1);
     UP(t.perm_v, perm.data(), L);
+    // double-float copies: nearest float, then the rounded remainder
+    std::vector<cdfl> twd(L), csd(L + 1);
+    for (int k = 0; k < L; ++k) twd[k] = cdfl{dfl(tw[k].x), dfl(tw[k].y)};
+    for (int j = 0; j <= L; ++j) csd[j] = cdfl{dfl(cs[j].x), dfl(cs[j].y)};
+    UP(t.tw_v_df, twd.data(), L);
+    UP(t.cs_v_df, csd.data(), L + 1);
   }
 
   // ---- FP32 copies of the horizontal and DCT tables (mixed-precision path) ----
@@ -930,6 +936,7 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
     ca.t_out = c->T1; ca.tb_out = c->tb1;
     ca.wcgl = c->Wcgl; ca.wsbp = c->Wsbp; ca.tsbp = c->Tsbp; ca.tcgl = c->Tcgl;
     ca.total_dt = alpha;
+    ca.df = mixed(c);
     CK(run_corrector(p, c->t, c->w, ca, st, &c->launches));
     t1 = c->T1;
     tb1 = c->tb1;
@@ -984,6 +991,7 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
     ca.t_out = c->T2; ca.tb_out = c->tb2;
     ca.wcgl = c->Wcgl; ca.wsbp = c->Wsbp; ca.tsbp = c->Tsbp; ca.tcgl = nullptr;
     ca.total_dt = pc ? alpha : dt;
+    ca.df = mixed(c);
     if (split_plain) {  // the base step's finalize zeroed the k=0 mode of w
       PCK("finalize", launch_zero_mode0(p, c->W2, p.d.G, st));
       c->launches += 1;

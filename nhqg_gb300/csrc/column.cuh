@@ -15,7 +15,10 @@
 // column instead of 4 (N+1)^2 for the dense product; other lengths use the
 // dense matrix.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
+#include "df64.cuh"
 #include "fft.cuh"
 
 namespace nhqg {
@@ -35,6 +38,8 @@ struct Dct {
   const float2* tw_f;         // [N] FP32 copy (mixed-precision path)
   const double2* cs;          // [N+1] exp(-i pi j / N) = cos - i sin
   const float2* cs_f;         // [N+1] FP32 copy
+  const cdfl* tw_df;          // [N] double-float copies (mixed-precision corrector)
+  const cdfl* cs_df;          // [N+1]
   const int* perm;            // [N] position of frequency k in the FFT output
   const double *V, *Vinv;     // dense fallback [P*P]
 };
@@ -50,6 +55,46 @@ __host__ __device__ inline size_t dct_smem_bytes_t(const Dct& d) {
 }
 __host__ __device__ inline size_t dct_smem_bytes(const Dct& d, bool f32 = false) {
   return f32 ? dct_smem_bytes_t<float2>(d) : dct_smem_bytes_t<double2>(d);
+}
+
+// Arithmetic of a tile type: double2 (FP64) or cdfl (double-float, the
+// mixed-precision corrector).  s() converts an FP64 table value, in() / out()
+// convert FP64 field values on the way into and out of a tile.
+template <typename C> struct Prec;
+template <> struct Prec<double2> {
+  using T = double;
+  static __device__ __forceinline__ double s(double v) { return v; }
+  static __device__ __forceinline__ double2 in(double2 v) { return v; }
+  static __device__ __forceinline__ double2 out(double2 v) { return v; }
+};
+template <> struct Prec<cdfl> {
+  using T = dfl;
+  static __device__ __forceinline__ dfl s(double v) { return df_from_double(v); }
+  static __device__ __forceinline__ cdfl in(double2 v) { return cdf_from(v); }
+  static __device__ __forceinline__ double2 out(cdfl v) { return cdf_to(v); }
+};
+template <typename C> __device__ __forceinline__ C gzero() {
+  using T = typename Prec<C>::T;
+  return gmk<C>(T(0), T(0));
+}
+template <typename C> __device__ __forceinline__ C gneg(C a) { return gmk<C>(-a.x, -a.y); }
+template <typename C, typename T> __device__ __forceinline__ C gaxpy(T s, C a, C acc) {
+  return gmk<C>(fma(s, a.x, acc.x), fma(s, a.y, acc.y));
+}
+// FP64 field columns <-> tiles of type C
+template <typename C>
+__device__ __forceinline__ void tloadp(C* b, const double2* __restrict__ src, int nlev, int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    b[i] = (m < M) ? Prec<C>::in(src[(size_t)l * M + m]) : gzero<C>();
+  }
+}
+template <typename C>
+__device__ __forceinline__ void tstorep(const C* b, double2* __restrict__ dst, int nlev, int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    if (m < M) dst[(size_t)l * M + m] = Prec<C>::out(b[i]);
+  }
 }
 
 __device__ __forceinline__ void tload(double2* b, const double2* __restrict__ src, int nlev,
@@ -116,19 +161,21 @@ __device__ __forceinline__ void tmat(double2* out, const double2* in, const doub
     out[idx] = make_double2(ax, ay);
   }
 }
-__device__ __forceinline__ void tcsr(double2* out, const double2* in, const int* __restrict__ ptr,
+template <typename C>
+__device__ __forceinline__ void tcsr(C* out, const C* in, const int* __restrict__ ptr,
                                      const int* __restrict__ colidx, const double* __restrict__ val,
                                      int nrow) {
+  using T = typename Prec<C>::T;
   for (int idx = threadIdx.x; idx < nrow * TM; idx += blockDim.x) {
     const int i = idx / TM, mm = idx - i * TM;
-    double ax = 0.0, ay = 0.0;
+    T ax = T(0), ay = T(0);
     for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
-      const double v = val[q];
-      const double2 x = in[colidx[q] * TM + mm];
+      const T v = Prec<C>::s(val[q]);
+      const C x = in[colidx[q] * TM + mm];
       ax = fma(v, x.x, ax);
       ay = fma(v, x.y, ay);
     }
-    out[idx] = make_double2(ax, ay);
+    out[idx] = gmk<C>(ax, ay);
   }
 }
 // Dirichlet stencil c_n = -x_n + x_{n-2} (x: G = N-1 entries; c: P)
@@ -158,6 +205,7 @@ __device__ __forceinline__ void tstencil_mixed(double2* c, const double2* x, int
 // reverse = true the sums run from the top index down (suffix sums).
 template <typename Get, typename Put>
 __device__ __forceinline__ void warp_parity_scan(int len, bool reverse, Get get, Put put) {
+  using T = decltype(get(0));
   const int lane = threadIdx.x & 31;
   const int cls = lane >> 4;               // parity class
   const int sl = lane & 15;                // lane within the class
@@ -167,15 +215,15 @@ __device__ __forceinline__ void warp_parity_scan(int len, bool reverse, Get get,
   const int j1 = min(m, j0 + chunk);
   const int top = len - 1 - ((len - 1 - cls) & 1);  // highest index of this class
   auto idx = [&](int j) { return reverse ? top - 2 * j : 2 * j + cls; };
-  double run = 0.0;
+  T run = T(0);
   for (int j = j0; j < j1; ++j) run += get(idx(j));
   // inclusive scan of the 16 chunk totals within each half-warp
-  double incl = run;
+  T incl = run;
   for (int o = 1; o < 16; o <<= 1) {
-    const double t = __shfl_up_sync(0xffffffffu, incl, o, 16);
+    const T t = __shfl_up_sync(0xffffffffu, incl, o, 16);
     if (sl >= o) incl += t;
   }
-  double acc = incl - run;                 // exclusive offset of this chunk
+  T acc = incl - run;                      // exclusive offset of this chunk
   for (int j = j0; j < j1; ++j) {
     const int n = idx(j);
     acc += get(n);
@@ -185,14 +233,16 @@ __device__ __forceinline__ void warp_parity_scan(int len, bool reverse, Get get,
 
 // exact left inverse of the Dirichlet stencil: x_n = x_{n-2} - c_n, i.e.
 // x_n = -(sum of c_i over i <= n, i = n mod 2), n < G.  Needs 2*TM warps.
-__device__ __forceinline__ void tpinv_dir(double2* x, const double2* c, int G) {
+template <typename C>
+__device__ __forceinline__ void tpinv_dir(C* x, const C* c, int G) {
+  using T = typename Prec<C>::T;
   const int w = threadIdx.x >> 5;
   if (w < 2 * TM) {
     const int mm = w >> 1;
     const bool im = w & 1;
     warp_parity_scan(G, false,
-        [&](int n) { return im ? -c[n * TM + mm].y : -c[n * TM + mm].x; },
-        [&](int n, double v) { if (im) x[n * TM + mm].y = v; else x[n * TM + mm].x = v; });
+        [&](int n) -> T { return im ? -c[n * TM + mm].y : -c[n * TM + mm].x; },
+        [&](int n, T v) { if (im) x[n * TM + mm].y = v; else x[n * TM + mm].x = v; });
   }
 }
 
@@ -260,10 +310,12 @@ template <typename C>
 __device__ __forceinline__ const C* dct_tw(const Dct& d);
 template <> __device__ __forceinline__ const double2* dct_tw<double2>(const Dct& d) { return d.tw; }
 template <> __device__ __forceinline__ const float2* dct_tw<float2>(const Dct& d) { return d.tw_f; }
+template <> __device__ __forceinline__ const cdfl* dct_tw<cdfl>(const Dct& d) { return d.tw_df; }
 template <typename C>
 __device__ __forceinline__ const C* dct_cs(const Dct& d);
 template <> __device__ __forceinline__ const double2* dct_cs<double2>(const Dct& d) { return d.cs; }
 template <> __device__ __forceinline__ const float2* dct_cs<float2>(const Dct& d) { return d.cs_f; }
+template <> __device__ __forceinline__ const cdfl* dct_cs<cdfl>(const Dct& d) { return d.cs_df; }
 
 template <typename C = double2>
 __device__ __forceinline__ DctSharedT<C> dct_shared(const Dct& d, void* base) {
@@ -289,14 +341,14 @@ __device__ __forceinline__ DctSharedT<C> dct_shared(const Dct& d, void* base) {
 
 // out[0:nout] = V in (inverse == false) or V^-1 in (inverse == true), per column,
 // in the precision of C.  Caller syncs before (in ready) and after (out
-// ready).  out != in.  The FP32 instantiation requires d.fast.  Needs 2 TM
+// ready).  out != in.  The FP32 and double-float instantiations require d.fast.  Needs 2 TM
 // warps (the odd outputs are a prefix sum per (mode, re/im) column).
 template <typename C>
 __device__ __forceinline__ void tdct(C* out, const C* in, const Dct& d, const DctSharedT<C>& s,
                                      bool inverse, int nout) {
   using T = decltype(C().x);
   const int N = d.N;
-  if constexpr (sizeof(T) == 8) {
+  if constexpr (std::is_same<T, double>::value) {
     if (!d.fast) {
       tmat(out, in, inverse ? d.Vinv : d.V, d.P, nout, d.P);
       return;

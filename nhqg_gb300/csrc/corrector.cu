@@ -21,8 +21,11 @@ namespace {
 
 using col::TM;
 using col::NT;
+using col::Prec;
 using col::tload;
 using col::tstore;
+using col::tloadp;
+using col::tstorep;
 using col::tmat;
 using col::tcsr;
 using col::tpinv_dir;
@@ -70,44 +73,52 @@ CK make_ck(const Params& p, const Tables& t) {
   return k;
 }
 
-__device__ __forceinline__ void tstencil(const CK& k, bool wbasis, double2* c, const double2* x) {
+// Galerkin -> Chebyshev stencil of w (wbasis) or theta on tiles of type C
+template <typename C>
+__device__ __forceinline__ void tstencil(const CK& k, bool wbasis, C* c, const C* x) {
   const bool mixed = wbasis && k.mixed;
   for (int idx = threadIdx.x; idx < k.P * TM; idx += blockDim.x) {
     const int n = idx / TM, mm = idx - n * TM;
-    double2 v;
+    C v;
     if (!mixed) {
-      v = (n < k.G) ? cneg(x[n * TM + mm]) : czero();
-      if (n >= 2 && n - 2 < k.G) v = cadd(v, x[(n - 2) * TM + mm]);
+      v = (n < k.G) ? col::gneg(x[n * TM + mm]) : col::gzero<C>();
+      if (n >= 2 && n - 2 < k.G) v = gadd(v, x[(n - 2) * TM + mm]);
     } else {
-      v = (n < k.G) ? x[n * TM + mm] : czero();
-      if (n >= 1 && n - 1 < k.G) v = caxpy(__ldg(k.wa + n - 1), x[(n - 1) * TM + mm], v);
-      if (n >= 2 && n - 2 < k.G) v = caxpy(__ldg(k.wb + n - 2), x[(n - 2) * TM + mm], v);
+      v = (n < k.G) ? x[n * TM + mm] : col::gzero<C>();
+      if (n >= 1 && n - 1 < k.G) v = col::gaxpy(Prec<C>::s(__ldg(k.wa + n - 1)), x[(n - 1) * TM + mm], v);
+      if (n >= 2 && n - 2 < k.G) v = col::gaxpy(Prec<C>::s(__ldg(k.wb + n - 2)), x[(n - 2) * TM + mm], v);
     }
     c[idx] = v;
   }
 }
 // ------------------------------------------------------------ per-mode kernels
-// Predictor w and theta to nodal CGL values and to the SBP grid (FP64: the
-// mean exchange keeps FP64 in the mixed-precision path too).
+// Tiles of type C: double2 in the plain path; cdfl (double-float on the FP32
+// pipe, about 48 significant bits) in the mixed-precision path, where these
+// transforms carry the state itself and FP32 would be too coarse.  Fields in
+// global memory stay FP64 either way.
+
+// Predictor w and theta to nodal CGL values and to the SBP grid.
+template <typename C>
 __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const double2* tp,
                                                  double2* wcgl, double2* wsbp, double2* tsbp) {
-  extern __shared__ double2 sm[];
+  extern __shared__ double2 sm_raw[];
+  C* sm = reinterpret_cast<C*>(sm_raw);
   const int PT = k.P * TM;
-  double2 *b0 = sm, *b1 = sm + PT;
-  const col::DctShared ds = col::dct_shared(k.dct, sm + 2 * PT);
+  C *b0 = sm, *b1 = sm + PT;
+  const col::DctSharedT<C> ds = col::dct_shared<C>(k.dct, sm + 2 * PT);
   const int m0 = blockIdx.x * TM;
-  tload(b0, wp, k.G, m0, k.M);
+  tloadp(b0, wp, k.G, m0, k.M);
   __syncthreads();
   tstencil(k, true, b1, b0);
   __syncthreads();
   tdct(b0, b1, k.dct, ds, false, k.P);
   __syncthreads();
-  tstore(b0, wcgl, k.P, m0, k.M);
+  tstorep(b0, wcgl, k.P, m0, k.M);
   tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
   __syncthreads();
-  tstore(b1, wsbp, k.P, m0, k.M);
+  tstorep(b1, wsbp, k.P, m0, k.M);
   __syncthreads();
-  tload(b0, tp, k.G, m0, k.M);
+  tloadp(b0, tp, k.G, m0, k.M);
   __syncthreads();
   tstencil(k, false, b1, b0);
   __syncthreads();
@@ -115,25 +126,29 @@ __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const 
   __syncthreads();
   tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
   __syncthreads();
-  tstore(b1, tsbp, k.P, m0, k.M);
+  tstorep(b1, tsbp, k.P, m0, k.M);
 }
 
+template <typename C>
 __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const double2* wsbp,
                                                  const double* g_half, double sub_dt, int last,
                                                  double2* t_out, double2* tcgl) {
-  extern __shared__ double2 sm[];
+  using T = typename Prec<C>::T;
+  extern __shared__ double2 sm_raw[];
+  C* sm = reinterpret_cast<C*>(sm_raw);
   const int PT = k.P * TM;
-  double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT;
-  const col::DctShared ds = col::dct_shared(k.dct, sm + 4 * PT);
-  __shared__ double2 delta[2 * TM];
+  C *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT;
+  const col::DctSharedT<C> ds = col::dct_shared<C>(k.dct, sm + 4 * PT);
+  __shared__ C delta[2 * TM];
   const int m0 = blockIdx.x * TM;
   const int P = k.P;
-  tload(b0, tsbp, P, m0, k.M);
-  tload(b1, wsbp, P, m0, k.M);
+  tloadp(b0, tsbp, P, m0, k.M);
+  tloadp(b1, wsbp, P, m0, k.M);
   __syncthreads();
   for (int i = threadIdx.x; i < PT; i += blockDim.x) {
     const int l = i / TM;
-    b0[i] = (l == 0 || l == P - 1) ? czero() : caxpy(-sub_dt * g_half[l], b1[i], b0[i]);
+    b0[i] = (l == 0 || l == P - 1) ? col::gzero<C>()
+                                   : col::gaxpy(Prec<C>::s(-sub_dt * g_half[l]), b1[i], b0[i]);
   }
   __syncthreads();
   tcsr(b2, b0, k.s2c_ptr, k.s2c_col, k.s2c_val, P);  // y = s2c theta_sbp_new
@@ -144,8 +159,9 @@ __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const doub
       for (int d = warp; d < 4 * TM; d += blockDim.x >> 5) {
         const int mm = d % TM, j = (d / TM) & 1, im = d / (2 * TM);
         const double* F = k.bcF + j * P;
-        double acc = 0.0;
-        for (int l = lane; l < P; l += 32) acc = fma(F[l], im ? b2[l * TM + mm].y : b2[l * TM + mm].x, acc);
+        T acc = T(0);
+        for (int l = lane; l < P; l += 32)
+          acc = fma(Prec<C>::s(F[l]), im ? b2[l * TM + mm].y : b2[l * TM + mm].x, acc);
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (lane == 0) { if (im) delta[j * TM + mm].y = acc; else delta[j * TM + mm].x = acc; }
       }
@@ -153,16 +169,16 @@ __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const doub
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) {
       const int l = i / TM, mm = i - l * TM;
-      double2 v = caxpy(k.bcV[l], delta[mm], b2[i]);
-      b3[i] = caxpy(k.bcV[P + l], delta[TM + mm], v);
+      C v = col::gaxpy(Prec<C>::s(k.bcV[l]), delta[mm], b2[i]);
+      b3[i] = col::gaxpy(Prec<C>::s(k.bcV[P + l]), delta[TM + mm], v);
     }
     __syncthreads();
     if (!last) {
       tcsr(b1, b3, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
       __syncthreads();
-      tstore(b1, tsbp, P, m0, k.M);
+      tstorep(b1, tsbp, P, m0, k.M);
     } else {
-      tstore(b3, tcgl, P, m0, k.M);
+      tstorep(b3, tcgl, P, m0, k.M);
     }
   }
   if (last) {
@@ -171,7 +187,7 @@ __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const doub
     __syncthreads();
     tpinv_dir(b1, b0, k.G);
     __syncthreads();
-    tstore(b1, t_out, k.G, m0, k.M);
+    tstorep(b1, t_out, k.G, m0, k.M);
   }
 }
 
@@ -626,15 +642,19 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   const size_t dsm = col::dct_smem_bytes(k.dct);
   const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2) + dsm;
   const size_t sm4 = 4 * (size_t)p.d.P * TM * sizeof(double2) + dsm;
-  cudaFuncSetAttribute(k_corr_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  cudaFuncSetAttribute(k_corr_sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+  // double-float tiles (same 16-byte complex size) need the fast DCT's tables
+  const bool df = a.df && k.dct.fast && k.dct.tw_df != nullptr;
+  auto pre = df ? k_corr_pre<cdfl> : k_corr_pre<double2>;
+  auto sub = df ? k_corr_sub<cdfl> : k_corr_sub<double2>;
+  cudaFuncSetAttribute(pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  cudaFuncSetAttribute(sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
   const size_t smid = (size_t)p.d.P * kSM * sizeof(double2);
   const bool fused_mid = smid <= 200 * 1024 && t.R_col != nullptr;
   if (fused_mid)
     cudaFuncSetAttribute(k_corr_sub_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
   Profiler& pf = w.prof;
   pf.begin("corr_pre", st);
-  k_corr_pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp);
+  pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp);
   pf.end(st);
   pf.begin("parseval", st);
   launch_parseval(p, a.wsbp, a.wsbp, p.d.P, w.vec + cv.w2(), w, st);
@@ -664,8 +684,8 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
       pf.end(st);
     } else {
       pf.begin(last ? "corr_sub_last" : "corr_sub", st);
-      k_corr_sub<<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt, last,
-                                        a.t_out, a.tcgl);
+      sub<<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt, last, a.t_out,
+                                 a.tcgl);
       pf.end(st);
     }
     n += 2;
@@ -678,8 +698,8 @@ cudaError_t launch_corr_pre(const Params& p, const Tables& t, const double2* w, 
                             double2* wcgl, double2* wsbp, double2* tsbp, cudaStream_t st) {
   CK k = make_ck(p, t);
   const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2) + col::dct_smem_bytes(k.dct);
-  cudaFuncSetAttribute(k_corr_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  k_corr_pre<<<(p.d.M + TM - 1) / TM, NT, sm2, st>>>(k, w, th, wcgl, wsbp, tsbp);
+  cudaFuncSetAttribute(k_corr_pre<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  k_corr_pre<double2><<<(p.d.M + TM - 1) / TM, NT, sm2, st>>>(k, w, th, wcgl, wsbp, tsbp);
   return cudaGetLastError();
 }
 

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "df64.cuh"
 #include "fft.cuh"
 #include "nhqg_gpu.h"
 
@@ -58,6 +59,7 @@ struct Tables {
   double2* tw_v = nullptr;  // [Nz]   exp(-2 pi i k / Nz)
   double2* cs_v = nullptr;  // [Nz+1] exp(-i pi j / Nz)
   int* perm_v = nullptr;    // [Nz]
+  cdfl *tw_v_df = nullptr, *cs_v_df = nullptr;  // double-float copies (mixed-path corrector)
   // vertical operators
   double *V = nullptr, *Vinv = nullptr;        // [P*P]
   double *wst_a = nullptr, *wst_b = nullptr;   // mixed w stencil a_n, b_n [G]; null = Dirichlet
@@ -128,6 +130,8 @@ inline col::Dct make_dct(const Params& p, const Tables& t) {
   d.tw_f = t.tw_v_f;
   d.cs = t.cs_v;
   d.cs_f = t.cs_v_f;
+  d.tw_df = t.tw_v_df;
+  d.cs_df = t.cs_v_df;
   d.perm = t.perm_v;
   d.V = t.V;
   d.Vinv = t.Vinv;
@@ -344,6 +348,7 @@ struct CorrArgs {
   double* tb_out;          // corrected th_bar
   double2 *wcgl, *wsbp, *tsbp, *tcgl;  // work; tcgl may be null
   double total_dt;
+  bool df;  // double-float column tiles (the mixed-precision path)
 };
 cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrArgs& a,
                           cudaStream_t st, int* nlaunch);
