@@ -416,6 +416,15 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.R_val, rval.data(), rval.size());
     UP(t.Fs, Fs.data(), Fs.size());
     UP(t.Us, Us.data(), Us.size());
+    auto dfv = [](const std::vector<double>& v) {
+      std::vector<dfl> o(v.size());
+      for (size_t i = 0; i < v.size(); ++i) o[i] = dfl(v[i]);
+      return o;
+    };
+    std::vector<dfl> rvd = dfv(rval), fsd = dfv(Fs), usd = dfv(Us);
+    UP(t.R_val_df, rvd.data(), rvd.size());
+    UP(t.Fs_df, fsd.data(), fsd.size());
+    UP(t.Us_df, usd.data(), usd.size());
   }
 
   // ---- shells present in the band ----

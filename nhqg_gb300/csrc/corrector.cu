@@ -201,38 +201,44 @@ constexpr int kSM = 16;
 constexpr int kSubThreads = 256;
 constexpr int kLG = kSubThreads / kSM;  // level groups
 
+template <typename V>
 struct SubK {
   int P, M, rw;
   const int* Rcol;
-  const double *Rval, *Fs, *Us, *g_half;
-  double sub_dt;
+  const V *Rval, *Fs, *Us;  // V = double, or dfl for double-float tiles
+  const double* g_half;
+  V sub_dt;
 };
 
-__global__ void __launch_bounds__(kSubThreads) k_corr_sub_mid(SubK k, double2* __restrict__ tsbp,
+template <typename C>
+__global__ void __launch_bounds__(kSubThreads) k_corr_sub_mid(SubK<typename Prec<C>::T> k,
+                                                              double2* __restrict__ tsbp,
                                                               const double2* __restrict__ wsbp) {
-  extern __shared__ double2 xs[];          // [P][kSM]
-  __shared__ double2 part[2][kLG][kSM];    // partial dot products
+  using T = typename Prec<C>::T;
+  extern __shared__ double2 xs_raw[];      // [P][kSM]
+  C* xs = reinterpret_cast<C*>(xs_raw);
+  __shared__ C part[2][kLG][kSM];          // partial dot products
   const int P = k.P, M = k.M;
   const int mm = threadIdx.x % kSM, lg = threadIdx.x / kSM;
   const int m = blockIdx.x * kSM + mm;
   const bool ok = m < M;
-  double2 d0 = czero(), d1 = czero();
+  C d0 = col::gzero<C>(), d1 = col::gzero<C>();
   for (int l = lg; l < P; l += kLG) {
-    double2 x = czero();
+    C x = col::gzero<C>();
     if (ok && l > 0 && l < P - 1) {
       const size_t g = (size_t)l * M + m;
-      x = caxpy(-k.sub_dt * k.g_half[l], wsbp[g], tsbp[g]);
+      x = col::gaxpy(-k.sub_dt * Prec<C>::s(k.g_half[l]), Prec<C>::in(wsbp[g]), Prec<C>::in(tsbp[g]));
     }
     xs[l * kSM + mm] = x;
-    d0 = caxpy(k.Fs[l], x, d0);
-    d1 = caxpy(k.Fs[P + l], x, d1);
+    d0 = col::gaxpy(k.Fs[l], x, d0);
+    d1 = col::gaxpy(k.Fs[P + l], x, d1);
   }
   part[0][lg][mm] = d0;
   part[1][lg][mm] = d1;
   __syncthreads();
   if (lg < 2) {  // 32 threads: (j, mm) totals, summed in a fixed order
-    double2 acc = czero();
-    for (int q = 0; q < kLG; ++q) acc = cadd(acc, part[lg][q][mm]);
+    C acc = col::gzero<C>();
+    for (int q = 0; q < kLG; ++q) acc = gadd(acc, part[lg][q][mm]);
     part[lg][0][mm] = acc;
   }
   __syncthreads();
@@ -240,11 +246,11 @@ __global__ void __launch_bounds__(kSubThreads) k_corr_sub_mid(SubK k, double2* _
   d1 = part[1][0][mm];
   if (!ok) return;
   for (int l = lg; l < P; l += kLG) {
-    double2 v = caxpy(k.Us[P + l], d1, cscale(d0, k.Us[l]));
+    C v = col::gaxpy(k.Us[P + l], d1, gscale(d0, k.Us[l]));
     const int* rc = k.Rcol + (size_t)l * k.rw;
-    const double* rv = k.Rval + (size_t)l * k.rw;
-    for (int q = 0; q < k.rw; ++q) v = caxpy(rv[q], xs[rc[q] * kSM + mm], v);
-    tsbp[(size_t)l * M + m] = v;
+    const T* rv = k.Rval + (size_t)l * k.rw;
+    for (int q = 0; q < k.rw; ++q) v = col::gaxpy(rv[q], xs[rc[q] * kSM + mm], v);
+    tsbp[(size_t)l * M + m] = Prec<C>::out(v);
   }
 }
 
@@ -650,17 +656,19 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   cudaFuncSetAttribute(sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
   const size_t smid = (size_t)p.d.P * kSM * sizeof(double2);
   const bool fused_mid = smid <= 200 * 1024 && t.R_col != nullptr;
-  if (fused_mid)
-    cudaFuncSetAttribute(k_corr_sub_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
+  if (fused_mid) {
+    cudaFuncSetAttribute(k_corr_sub_mid<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
+    cudaFuncSetAttribute(k_corr_sub_mid<cdfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
+  }
   Profiler& pf = w.prof;
   pf.begin("corr_pre", st);
   pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp);
   pf.end(st);
   pf.begin("parseval", st);
-  launch_parseval(p, a.wsbp, a.wsbp, p.d.P, w.vec + cv.w2(), w, st);
+  launch_parseval(p, a.wsbp, a.wsbp, p.d.P, w.vec + cv.w2(), w, st, df);
   pf.end(st);
   pf.begin("parseval", st);
-  launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st);
+  launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st, df);
   pf.end(st);
   pf.begin("corr_init_1d", st);
   k_corr_init<<<1, NT, 10 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, a.tbp, sub_dt);
@@ -670,7 +678,7 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
     const int last = (s == nsub - 1);
     if (s > 0) {
       pf.begin("parseval", st);
-      launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st);
+      launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st, df);
       pf.end(st);
       ++n;
     }
@@ -678,9 +686,15 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
     k_corr_tstep<<<1, NT, 11 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, sub_dt, last, a.tb_out);
     pf.end(st);
     if (!last && fused_mid) {
-      SubK sk{p.d.P, p.d.M, t.R_w, t.R_col, t.R_val, t.Fs, t.Us, w.vec + cv.g_half(), sub_dt};
       pf.begin("corr_sub_mid", st);
-      k_corr_sub_mid<<<(p.d.M + kSM - 1) / kSM, kSubThreads, smid, st>>>(sk, a.tsbp, a.wsbp);
+      if (df && t.R_val_df) {
+        SubK<dfl> sk{p.d.P, p.d.M, t.R_w, t.R_col, t.R_val_df, t.Fs_df, t.Us_df, w.vec + cv.g_half(),
+                     dfl(sub_dt)};
+        k_corr_sub_mid<cdfl><<<(p.d.M + kSM - 1) / kSM, kSubThreads, smid, st>>>(sk, a.tsbp, a.wsbp);
+      } else {
+        SubK<double> sk{p.d.P, p.d.M, t.R_w, t.R_col, t.R_val, t.Fs, t.Us, w.vec + cv.g_half(), sub_dt};
+        k_corr_sub_mid<double2><<<(p.d.M + kSM - 1) / kSM, kSubThreads, smid, st>>>(sk, a.tsbp, a.wsbp);
+      }
       pf.end(st);
     } else {
       pf.begin(last ? "corr_sub_last" : "corr_sub", st);

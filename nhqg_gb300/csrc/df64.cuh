@@ -12,7 +12,7 @@
 // butterflies need.  Every operation is written with the _rn intrinsics so
 // that the compiler neither contracts a product into a later sum nor
 // reorders the compensated steps.  The exponent range is FP32's: values
-// below about 2^-100 lose their low word (the transforms' operands are
+// below about 2^-103 lose their low word (the transforms' operands are
 // relative to column norms far above that).
 #pragma once
 #include <cstdint>
@@ -27,7 +27,7 @@ using ::__shfl_xor_sync;
 using ::__shfl_up_sync;
 using ::__shfl_down_sync;
 
-struct dfl {
+struct __align__(8) dfl {
   float hi, lo;
   dfl() = default;
   __host__ __device__ constexpr dfl(float h, float l) : hi(h), lo(l) {}
@@ -36,7 +36,9 @@ struct dfl {
   __host__ __device__ dfl(double v) : hi((float)v), lo((float)(v - (double)(float)v)) {}
 };
 
-struct cdfl {
+// 16-byte aligned like double2, so that a complex value moves in one
+// 128-bit shared-memory access
+struct __align__(16) cdfl {
   dfl x, y;
 };
 
@@ -89,11 +91,14 @@ __device__ __forceinline__ dfl __shfl_down_sync(unsigned mask, dfl v, unsigned d
   return dfl(__shfl_down_sync(mask, v.hi, d, width), __shfl_down_sync(mask, v.lo, d, width));
 }
 
-// FP64 <-> double-float without FP64 arithmetic on the way in: the high word
-// is the significand truncated to 24 bits, the low word the next 29 bits
-// (rounded to 24) scaled by the exponent, both in integer arithmetic.  Zero,
-// magnitudes below 2^-126 and non-finite values are not expected here; the
-// first two flush to zero.
+// FP64 -> double-float in integer arithmetic (no FP64 operation): the high
+// word is the significand truncated to 24 bits, the low word the remaining 29
+// bits rounded to 24 and scaled by the exponent (relative error below
+// 2^-46.7 for magnitudes above 2^-103; smaller magnitudes keep the high word
+// only, and below 2^-126 flush to zero).  Back to FP64: both words widened
+// exactly in integer arithmetic, then one FP64 addition (an integer assembly
+// of the sum itself, with 64-bit shifts, rounding and renormalisation,
+// measured slower on GB300).
 __device__ __forceinline__ dfl df_from_double(double v) {
   const uint64_t b = static_cast<uint64_t>(__double_as_longlong(v));
   const uint32_t hw = static_cast<uint32_t>(b >> 32);
@@ -103,14 +108,25 @@ __device__ __forceinline__ dfl df_from_double(double v) {
   if (e <= 0) return dfl(0.f, 0.f);
   const uint32_t m = ((hw & 0xFFFFFu) << 3) | static_cast<uint32_t>((b >> 29) & 7u);
   const float hi = __uint_as_float(sgn | (static_cast<uint32_t>(e) << 23) | m);
-  // remainder: the low 29 significand bits times 2^(eb - 1023 - 52)
+  // remainder: the low 29 significand bits times 2^(eb-1075) = 2^-29 2^(eb-1046)
   const uint32_t rbits = static_cast<uint32_t>(b & 0x1FFFFFFFu);
-  const int er = eb - 1023 - 52 + 127;  // biased FP32 exponent of 2^(eb-1075)
+  const int er = eb - 1046 + 127;
   float lo = 0.f;
-  if (er > 0) lo = __uint2float_rn(rbits) * __uint_as_float(static_cast<uint32_t>(er) << 23);
+  if (er > 0)
+    lo = __fmul_rn(__fmul_rn(__uint2float_rn(rbits), __uint_as_float(static_cast<uint32_t>(127 - 29) << 23)),
+                   __uint_as_float(static_cast<uint32_t>(er) << 23));
   return dfl(hi, sgn ? -lo : lo);
 }
-__device__ __forceinline__ double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
+// float -> double by rebiasing the exponent in integer arithmetic (exact;
+// zero and magnitudes below 2^-126 give 0)
+__device__ __forceinline__ double f2d_bits(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint32_t hw = e ? (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3) : 0u;
+  const uint32_t lw = e ? (u << 29) : 0u;
+  return __hiloint2double(static_cast<int>(hw), static_cast<int>(lw));
+}
+__device__ __forceinline__ double df_to_double(dfl a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
 
 __device__ __forceinline__ cdfl cdf_from(double2 v) { return cdfl{df_from_double(v.x), df_from_double(v.y)}; }
 __device__ __forceinline__ double2 cdf_to(cdfl v) { return make_double2(df_to_double(v.x), df_to_double(v.y)); }

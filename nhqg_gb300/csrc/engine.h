@@ -76,6 +76,7 @@ struct Tables {
   int R_w = 0;
   double* Fs = nullptr;     // [2*P]
   double* Us = nullptr;     // [2*P]
+  dfl *R_val_df = nullptr, *Fs_df = nullptr, *Us_df = nullptr;  // double-float copies
   double* proj = nullptr;   // [P*P] proj_dirichlet
   double* D1 = nullptr;     // [P*P] SBP first derivative
   double* Lsbp = nullptr;   // [P*P] SBP Laplacian
@@ -321,7 +322,7 @@ cudaError_t launch_scatter(const Params& p, const double2* compact, double2* ful
 cudaError_t launch_finalize(const Params& p, const double2* q, const double2* w, const double2* th,
                             double2* qo, double2* wo, double2* to, cudaStream_t st);
 cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
-                            double* out, Work& w, cudaStream_t st);
+                            double* out, Work& w, cudaStream_t st, bool df = false);
 size_t parseval_partials(int levels);
 cudaError_t launch_hermitian(const Params& p, double2* q, double2* w, double2* th, cudaStream_t st);
 cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStream_t st);

@@ -615,10 +615,14 @@ __global__ void k_hermitian(Dims d, double2* q, double2* w, double2* th) {
 // Hermitian part contributes Re(a b*)/2.  Each level is split into kParSeg segments, one CTA
 // each; the last CTA of a level to finish adds the segment sums in segment
 // order (deterministic) and resets the level's counter for the next launch.
+// C = cdfl accumulates the per-thread sums in double-float (the mixed path;
+// the FP64 pipe bounds the FP64 form on GB300); CTA totals are FP64.
 constexpr int kParSeg = 8;
+template <typename C>
 __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const double2* b,
                                                  double* out, double scale, double* partials,
                                                  unsigned* counters) {
+  using T = typename col::Prec<C>::T;
   __shared__ double scratch[32];
   __shared__ bool is_last;
   const int l = blockIdx.y, seg = blockIdx.x;
@@ -626,16 +630,18 @@ __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const
   const double2* bl = b + (size_t)l * d.M;
   const int chunk = (d.M + kParSeg - 1) / kParSeg;
   const int m0 = seg * chunk, m1 = min(d.M, m0 + chunk);
-  // two FMAs per element on two accumulators (the FP64 pipe, not HBM, bounds
-  // this reduction on GB300); the half-plane weight 2 is applied once
-  double accr = 0.0, acci = 0.0;
+  // two FMAs per element on two accumulators; the half-plane weight 2 is
+  // applied once
+  T accr = T(0), acci = T(0);
 #pragma unroll 4
   for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
-    const double2 x = al[m], y = bl[m];
+    const C x = col::Prec<C>::in(al[m]), y = col::Prec<C>::in(bl[m]);
     accr = fma(x.x, y.x, accr);
     acci = fma(x.y, y.y, acci);
   }
-  double acc = 2.0 * (accr + acci);
+  double acc;
+  if constexpr (std::is_same<C, double2>::value) acc = 2.0 * (accr + acci);
+  else acc = 2.0 * df_to_double(accr + acci);
   // the ky = 0 column: replace the doubled term by the Hermitian projection
   for (int r = threadIdx.x; r < d.Mr; r += blockDim.x) {
     const int m = r * d.Mc;
@@ -871,10 +877,11 @@ cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStrea
 size_t parseval_partials(int levels) { return (size_t)levels * kParSeg; }
 
 cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
-                            double* out, Work& w, cudaStream_t st) {
+                            double* out, Work& w, cudaStream_t st, bool df) {
   const double n2 = (double)p.d.Nx * (double)p.d.Nx;
-  k_parseval<<<dim3(kParSeg, levels), NT, 0, st>>>(p.d, a, b, out, 1.0 / (n2 * n2), w.partials,
-                                                    w.counters);
+  auto kern = df ? k_parseval<cdfl> : k_parseval<double2>;
+  kern<<<dim3(kParSeg, levels), NT, 0, st>>>(p.d, a, b, out, 1.0 / (n2 * n2), w.partials,
+                                             w.counters);
   return cudaGetLastError();
 }
 
