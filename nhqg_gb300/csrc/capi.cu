@@ -780,6 +780,7 @@ VArgs base_vargs(nhqg_ctx* c) {
   if (mixed(c)) {
     a.Aqf = c->Aqf; a.Awf = c->Awf; a.Atf = c->Atf;
     a.af_coef = c->p.tc_vertical;
+    a.df = true;  // double-float tiles where the operands arrive as coefficients
   }
   a.E1q = c->E1q; a.E1w = c->E1w; a.E1t = c->E1t;
   a.Wn = c->Wn;
@@ -795,7 +796,7 @@ int solve_back(nhqg_ctx* c, double2* qo, double2* wo, double2* to, bool zero_mea
   } else {
     PCK("shell_solve", launch_shell(p, c->t, c->rhs, wo, st));
   }
-  PCK("vpost", launch_vpost(p, c->t, c->Rq, c->Rt, wo, qo, to, zero_mean, st));
+  PCK("vpost", launch_vpost(p, c->t, c->Rq, c->Rt, wo, qo, to, zero_mean, st, mixed(c)));
   c->launches += 2;
   return NHQG_OK;
 }

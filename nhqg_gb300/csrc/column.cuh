@@ -64,13 +64,17 @@ template <typename C> struct Prec;
 template <> struct Prec<double2> {
   using T = double;
   static __device__ __forceinline__ double s(double v) { return v; }
+  static __device__ __forceinline__ double i(int v) { return (double)v; }
   static __device__ __forceinline__ double2 in(double2 v) { return v; }
+  static __device__ __forceinline__ double2 in(float2 v) { return make_double2((double)v.x, (double)v.y); }
   static __device__ __forceinline__ double2 out(double2 v) { return v; }
 };
 template <> struct Prec<cdfl> {
   using T = dfl;
   static __device__ __forceinline__ dfl s(double v) { return df_from_double(v); }
+  static __device__ __forceinline__ dfl i(int v) { return dfl((float)v, 0.f); }  // |v| < 2^24
   static __device__ __forceinline__ cdfl in(double2 v) { return cdf_from(v); }
+  static __device__ __forceinline__ cdfl in(float2 v) { return cdfl{dfl(v.x, 0.f), dfl(v.y, 0.f)}; }
   static __device__ __forceinline__ double2 out(cdfl v) { return cdf_to(v); }
 };
 template <typename C> __device__ __forceinline__ C gzero() {
@@ -84,6 +88,13 @@ template <typename C, typename T> __device__ __forceinline__ C gaxpy(T s, C a, C
 // FP64 field columns <-> tiles of type C
 template <typename C>
 __device__ __forceinline__ void tloadp(C* b, const double2* __restrict__ src, int nlev, int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    b[i] = (m < M) ? Prec<C>::in(src[(size_t)l * M + m]) : gzero<C>();
+  }
+}
+template <typename C>
+__device__ __forceinline__ void tloadp(C* b, const float2* __restrict__ src, int nlev, int m0, int M) {
   for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
     const int l = i / TM, mm = i - l * TM, m = m0 + mm;
     b[i] = (m < M) ? Prec<C>::in(src[(size_t)l * M + m]) : gzero<C>();
@@ -179,23 +190,25 @@ __device__ __forceinline__ void tcsr(C* out, const C* in, const int* __restrict_
   }
 }
 // Dirichlet stencil c_n = -x_n + x_{n-2} (x: G = N-1 entries; c: P)
-__device__ __forceinline__ void tstencil_dir(double2* c, const double2* x, int P, int G) {
+template <typename C>
+__device__ __forceinline__ void tstencil_dir(C* c, const C* x, int P, int G) {
   for (int idx = threadIdx.x; idx < P * TM; idx += blockDim.x) {
     const int n = idx / TM, mm = idx - n * TM;
-    double2 v = (n < G) ? cneg(x[n * TM + mm]) : czero();
-    if (n >= 2 && n - 2 < G) v = cadd(v, x[(n - 2) * TM + mm]);
+    C v = (n < G) ? gneg(x[n * TM + mm]) : gzero<C>();
+    if (n >= 2 && n - 2 < G) v = gadd(v, x[(n - 2) * TM + mm]);
     c[idx] = v;
   }
 }
 // open-top basis T_n + a_n T_{n+1} + b_n T_{n+2}
-__device__ __forceinline__ void tstencil_mixed(double2* c, const double2* x, int P, int G,
+template <typename C>
+__device__ __forceinline__ void tstencil_mixed(C* c, const C* x, int P, int G,
                                                const double* __restrict__ wa,
                                                const double* __restrict__ wb) {
   for (int idx = threadIdx.x; idx < P * TM; idx += blockDim.x) {
     const int n = idx / TM, mm = idx - n * TM;
-    double2 v = (n < G) ? x[n * TM + mm] : czero();
-    if (n >= 1 && n - 1 < G) v = caxpy(__ldg(wa + n - 1), x[(n - 1) * TM + mm], v);
-    if (n >= 2 && n - 2 < G) v = caxpy(__ldg(wb + n - 2), x[(n - 2) * TM + mm], v);
+    C v = (n < G) ? x[n * TM + mm] : gzero<C>();
+    if (n >= 1 && n - 1 < G) v = gaxpy(Prec<C>::s(__ldg(wa + n - 1)), x[(n - 1) * TM + mm], v);
+    if (n >= 2 && n - 2 < G) v = gaxpy(Prec<C>::s(__ldg(wb + n - 2)), x[(n - 2) * TM + mm], v);
     c[idx] = v;
   }
 }
@@ -247,18 +260,20 @@ __device__ __forceinline__ void tpinv_dir(C* x, const C* c, int G) {
 }
 
 // exact left inverse of the open-top stencil: x_n = c_n - a_{n-1} x_{n-1} - b_{n-2} x_{n-2}
-__device__ __forceinline__ void tpinv_mixed(double2* x, const double2* c, int G,
+template <typename C>
+__device__ __forceinline__ void tpinv_mixed(C* x, const C* c, int G,
                                             const double* __restrict__ wa,
                                             const double* __restrict__ wb) {
+  using T = typename Prec<C>::T;
   const int t = threadIdx.x;
   if (t < 2 * TM) {
     const int mm = t >> 1;
     const bool im = t & 1;
-    double xm2 = 0.0, xm1 = 0.0;
+    T xm2 = T(0), xm1 = T(0);
     for (int n = 0; n < G; ++n) {
-      double v = im ? c[n * TM + mm].y : c[n * TM + mm].x;
-      if (n >= 1) v = fma(-__ldg(wa + n - 1), xm1, v);
-      if (n >= 2) v = fma(-__ldg(wb + n - 2), xm2, v);
+      T v = im ? c[n * TM + mm].y : c[n * TM + mm].x;
+      if (n >= 1) v = fma(Prec<C>::s(-__ldg(wa + n - 1)), xm1, v);
+      if (n >= 2) v = fma(Prec<C>::s(-__ldg(wb + n - 2)), xm2, v);
       if (im) x[n * TM + mm].y = v; else x[n * TM + mm].x = v;
       xm2 = xm1;
       xm1 = v;
@@ -268,7 +283,9 @@ __device__ __forceinline__ void tpinv_mixed(double2* x, const double2* c, int G,
 // d/dZ on Chebyshev coefficients, G_Z = 2 G_xi (nhqg/grid.py:148-169):
 // b_k = sum_{j > k, j - k odd} 4 j a_j for 1 <= k <= N-1, b_N = 0,
 // b_0 = b_2 / 2 + 2 a_1 -- suffix sums over a parity class.  Needs 2*TM warps.
-__device__ __forceinline__ void tgz(double2* b, const double2* a, int N) {
+template <typename C>
+__device__ __forceinline__ void tgz(C* b, const C* a, int N) {
+  using T = typename Prec<C>::T;
   const int w = threadIdx.x >> 5;
   if (w < 2 * TM) {
     const int mm = w >> 1;
@@ -276,22 +293,22 @@ __device__ __forceinline__ void tgz(double2* b, const double2* a, int N) {
     // t_j = 4 j a_j for j = 1..N, scanned from the top: U_j = sum_{i>=j, i=j mod 2} t_i
     // stored as b_{j-1} = U_j (j = 2..N), b_0 fixed up below
     warp_parity_scan(N, true,
-        [&](int n) {  // n = j - 1 in [0, N-1]
-          const double av = im ? a[(n + 1) * TM + mm].y : a[(n + 1) * TM + mm].x;
-          return (4.0 * (n + 1)) * av;
+        [&](int n) -> T {  // n = j - 1 in [0, N-1]
+          const T av = im ? a[(n + 1) * TM + mm].y : a[(n + 1) * TM + mm].x;
+          return Prec<C>::i(4 * (n + 1)) * av;
         },
-        [&](int n, double v) { if (n >= 1) { if (im) b[n * TM + mm].y = v; else b[n * TM + mm].x = v; } });
+        [&](int n, T v) { if (n >= 1) { if (im) b[n * TM + mm].y = v; else b[n * TM + mm].x = v; } });
     if ((threadIdx.x & 31) == 0) {
-      if (im) b[N * TM + mm].y = 0.0; else b[N * TM + mm].x = 0.0;
+      if (im) b[N * TM + mm].y = T(0); else b[N * TM + mm].x = T(0);
     }
   }
   __syncthreads();
   if (threadIdx.x < 2 * TM) {
     const int mm = threadIdx.x >> 1;
     const bool im = threadIdx.x & 1;
-    const double b2 = N >= 2 ? (im ? b[2 * TM + mm].y : b[2 * TM + mm].x) : 0.0;
-    const double a1 = im ? a[TM + mm].y : a[TM + mm].x;
-    const double b0 = fma(0.5, b2, 2.0 * a1);
+    const T b2 = N >= 2 ? (im ? b[2 * TM + mm].y : b[2 * TM + mm].x) : T(0);
+    const T a1 = im ? a[TM + mm].y : a[TM + mm].x;
+    const T b0 = fma(T(0.5), b2, T(2.0) * a1);
     if (im) b[mm].y = b0; else b[mm].x = b0;
   }
 }

@@ -262,6 +262,7 @@ struct VArgs {
   double c_E1, c_E2;  // dt*delta, dt*(1-delta)
   double omega;       // dt*(1-gamma)
   double inv_alpha_c; // 1/alpha for the corrector tendency (0 = none)
+  bool df;            // double-float tiles (mixed path with coefficient operands)
 };
 cudaError_t launch_vfwd(const Params& p, const Tables& t, const double2* q, const double2* w,
                         const double2* th, double2* qn, double2* wn, double2* tn, cudaStream_t st);
@@ -311,7 +312,7 @@ cudaError_t launch_shell(const Params& p, const Tables& t, const double2* rhs_w,
                          cudaStream_t st);
 cudaError_t launch_vpost(const Params& p, const Tables& t, const double2* Rq, const double2* Rt,
                          const double2* w_new, double2* q_out, double2* t_out, bool zero_mean,
-                         cudaStream_t st);
+                         cudaStream_t st, bool df = false);
 size_t corrector_vec_doubles(int P);
 cudaError_t launch_itend(const Params& p, const Tables& t, const double2* q, const double2* w,
                          const double2* th, double2* Iq, double2* Iw, double2* It, cudaStream_t st);

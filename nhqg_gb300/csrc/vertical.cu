@@ -58,11 +58,13 @@ VK make_vk(const Params& p, const Tables& t) {
   return k;
 }
 
-__device__ __forceinline__ void tstencil_w(const VK& k, double2* c, const double2* x) {
+template <typename C>
+__device__ __forceinline__ void tstencil_w(const VK& k, C* c, const C* x) {
   if (!k.mixed) tstencil_dir(c, x, k.P, k.G);
   else col::tstencil_mixed(c, x, k.P, k.G, k.wa, k.wb);
 }
-__device__ __forceinline__ void tpinv_w(const VK& k, double2* x, const double2* c) {
+template <typename C>
+__device__ __forceinline__ void tpinv_w(const VK& k, C* x, const C* c) {
   if (!k.mixed) tpinv_dir(x, c, k.G);
   else col::tpinv_mixed(x, c, k.G, k.wa, k.wb);
 }
@@ -133,15 +135,15 @@ enum AKind {
 
 // Chebyshev coefficients (FP64 tile out) of the explicit operand A, read in
 // the form AK; tmp is a free tile.
-template <int AK, typename DS>
+template <int AK, typename DS, typename C>
 __device__ __forceinline__ void a_to_coef(const VK& k, const DS& ds, const double2* Ad,
-                                          const float2* Af, double2* tmp, double2* out, int m0) {
-  if constexpr (AK == AK_F64) {
+                                          const float2* Af, C* tmp, C* out, int m0) {
+  if constexpr (AK == AK_F32_COEF) {
+    col::tloadp(out, Af, k.P, m0, k.M);
+  } else if constexpr (AK == AK_F64) {
     tload(tmp, Ad, k.P, m0, k.M);
     __syncthreads();
     tdct(out, tmp, k.dct, ds, true, k.P);
-  } else if constexpr (AK == AK_F32_COEF) {
-    tload_f2d(out, Af, k.P, m0, k.M);
   } else {
     float2* fi = reinterpret_cast<float2*>(tmp);
     float2* fo = fi + k.P * TM;
@@ -154,17 +156,26 @@ __device__ __forceinline__ void a_to_coef(const VK& k, const DS& ds, const doubl
 }
 
 // =========================================================== back + stage + solve-pre
-template <int MODE, int AK>
+// Tiles of type C: double2, or cdfl (double-float, the mixed path with the
+// tensor-core inverse, AK_F32_COEF) -- fields in global memory stay FP64.
+template <int MODE, int AK, typename C = double2>
 __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
-  extern __shared__ double2 sm[];
+  static_assert(std::is_same<C, double2>::value || AK == AK_F32_COEF,
+                "double-float tiles read the explicit operand as coefficients");
+  using T = typename col::Prec<C>::T;
+  using Pr = col::Prec<C>;
+  extern __shared__ double2 sm_raw[];
+  C* sm = reinterpret_cast<C*>(sm_raw);
   const int PT = k.P * TM;
-  double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT, *b4 = sm + 4 * PT;
+  C *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT, *b3 = sm + 3 * PT, *b4 = sm + 4 * PT;
   using CA = typename std::conditional<AK == AK_F32_NODAL, float2, double2>::type;
   col::DctSharedT<CA> ds{};
-  if constexpr (AK != AK_F32_COEF) ds = col::dct_shared<CA>(k.dct, sm + 5 * PT);
+  if constexpr (AK != AK_F32_COEF) ds = col::dct_shared<CA>(k.dct, sm_raw + 5 * PT);
   const int m0 = blockIdx.x * TM;
   const int P = k.P, G = k.G, M = k.M;
   const size_t Ms = (size_t)M;
+  const T alpha = Pr::s(a.alpha), cE1 = Pr::s(a.c_E1), cE2 = Pr::s(a.c_E2);
+  const T omega = Pr::s(a.omega), gdt = Pr::s(k.gdt), Ra = Pr::s(k.Ra);
 
   // ------------------------------------------------------------- q
   if (MODE != VB_SOLVE) {
@@ -175,26 +186,26 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
     for (int i = threadIdx.x; i < PT; i += blockDim.x) {
       const int l = i / TM, m = mode_of(i, m0);
       if (m >= M) continue;
-      double2 e = (AK == AK_F32_COEF) ? b1[i] : cneg(b1[i]);
+      C e = (AK == AK_F32_COEF) ? b1[i] : col::gneg(b1[i]);
       if (k.beta != 0.0) {
-        const double s = k.beta * k.kx[m] * k.inv_denom[m];
-        const double2 qv = qs[(size_t)l * Ms + m];
-        e = make_double2(fma(-s, qv.y, e.x), fma(s, qv.x, e.y));
+        const T sb = Pr::s(k.beta * k.kx[m] * k.inv_denom[m]);
+        const C qv = Pr::in(qs[(size_t)l * Ms + m]);
+        e = gmk<C>(fma(-sb, qv.y, e.x), fma(sb, qv.x, e.y));
       }
-      if (a.Cq) e = cadd(e, a.Cq[(size_t)l * Ms + m]);  // learned closure
+      if (a.Cq) e = gadd(e, Pr::in(a.Cq[(size_t)l * Ms + m]));  // learned closure
       b1[i] = e;
     }
     __syncthreads();
     if (MODE == VB_RHS) {
-      tstore(b1, a.Eq, P, m0, M);
+      col::tstorep(b1, a.Eq, P, m0, M);
     } else if (MODE == VB_STAGE1) {
-      tstore(b1, a.E1q, P, m0, M);
+      col::tstorep(b1, a.E1q, P, m0, M);
       for (int i = threadIdx.x; i < PT; i += blockDim.x) {
         const int l = i / TM, m = mode_of(i, m0);
-        if (m < M) b1[i] = caxpy(a.alpha, b1[i], a.q0[(size_t)l * Ms + m]);
+        if (m < M) b1[i] = col::gaxpy(alpha, b1[i], Pr::in(a.q0[(size_t)l * Ms + m]));
       }
     } else {  // STAGE2: I_q = G_Z S_w w1
-      tload(b2, a.w1, G, m0, M);
+      col::tloadp(b2, a.w1, G, m0, M);
       __syncthreads();
       tstencil_w(k, b3, b2);
       __syncthreads();
@@ -204,32 +215,32 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
         const int l = i / TM, m = mode_of(i, m0);
         if (m >= M) continue;
         const size_t g = (size_t)l * Ms + m;
-        double2 r = a.q0[g];
-        r = caxpy(a.c_E1, a.E1q[g], r);
-        r = caxpy(a.c_E2, b1[i], r);
-        r = caxpy(a.omega, b2[i], r);
-        r = caxpy(-a.omega * k.drq[m], a.q1[g], r);
+        C r = Pr::in(a.q0[g]);
+        r = col::gaxpy(cE1, Pr::in(a.E1q[g]), r);
+        r = col::gaxpy(cE2, b1[i], r);
+        r = col::gaxpy(omega, b2[i], r);
+        r = col::gaxpy((-omega) * Pr::s(k.drq[m]), Pr::in(a.q1[g]), r);
         b1[i] = r;
       }
     }
     __syncthreads();
   } else {
-    tload(b1, a.q0, P, m0, M);  // R_q given
+    col::tloadp(b1, a.q0, P, m0, M);  // R_q given
     __syncthreads();
   }
   if (MODE != VB_RHS) {
-    tstore(b1, a.Rq, P, m0, M);
+    col::tstorep(b1, a.Rq, P, m0, M);
     // temp = R_q / alpha_q ; d_gal = pinv_w(inv_denom * G_Z temp)
     for (int i = threadIdx.x; i < PT; i += blockDim.x) {
       const int m = mode_of(i, m0);
-      b2[i] = (m < M) ? cscale(b1[i], k.inv_aq[m]) : czero();
+      b2[i] = (m < M) ? gscale(b1[i], Pr::s(k.inv_aq[m])) : col::gzero<C>();
     }
     __syncthreads();
     tgz(b3, b2, k.N);
     __syncthreads();
     for (int i = threadIdx.x; i < PT; i += blockDim.x) {
       const int m = mode_of(i, m0);
-      b3[i] = (m < M) ? cscale(b3[i], k.inv_denom[m]) : czero();
+      b3[i] = (m < M) ? gscale(b3[i], Pr::s(k.inv_denom[m])) : col::gzero<C>();
     }
     __syncthreads();
     tpinv_w(k, b4, b3);
@@ -239,35 +250,35 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   // ------------------------------------------------------------- w
   if (MODE != VB_SOLVE) {
     if constexpr (AK == AK_F32_COEF) {  // E_w in the Galerkin basis
-      tload_f2d(b2, a.Awf, G, m0, M);
+      col::tloadp(b2, a.Awf, G, m0, M);
     } else {
       a_to_coef<AK>(k, ds, a.Aw, a.Awf, b0, b1, m0);
       __syncthreads();
-      for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
+      for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = col::gneg(b1[i]);
       __syncthreads();
       tpinv_w(k, b2, b1);
     }
     __syncthreads();
     if (MODE == VB_RHS) {
-      tstore(b2, a.Ew, G, m0, M);
+      col::tstorep(b2, a.Ew, G, m0, M);
     } else if (MODE == VB_STAGE1) {
-      tstore(b2, a.E1w, G, m0, M);
+      col::tstorep(b2, a.E1w, G, m0, M);
       for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
         const int l = i / TM, m = mode_of(i, m0);
-        if (m < M) b2[i] = caxpy(a.alpha, b2[i], a.w0[(size_t)l * Ms + m]);
+        if (m < M) b2[i] = col::gaxpy(alpha, b2[i], Pr::in(a.w0[(size_t)l * Ms + m]));
       }
     } else {  // I_w = pinv_w(inv_denom G_Z q1 + Ra S_dir t1)
-      tload(b0, a.q1, P, m0, M);
+      col::tloadp(b0, a.q1, P, m0, M);
       __syncthreads();
       tgz(b1, b0, k.N);
       __syncthreads();
-      tload(b0, a.t1, G, m0, M);
+      col::tloadp(b0, a.t1, G, m0, M);
       __syncthreads();
       tstencil_dir(b3, b0, P, G);
       __syncthreads();
       for (int i = threadIdx.x; i < PT; i += blockDim.x) {
         const int m = mode_of(i, m0);
-        b1[i] = (m < M) ? caxpy(k.Ra, b3[i], cscale(b1[i], k.inv_denom[m])) : czero();
+        b1[i] = (m < M) ? col::gaxpy(Ra, b3[i], gscale(b1[i], Pr::s(k.inv_denom[m]))) : col::gzero<C>();
       }
       __syncthreads();
       tpinv_w(k, b0, b1);
@@ -276,21 +287,21 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
         const int l = i / TM, m = mode_of(i, m0);
         if (m >= M) continue;
         const size_t g = (size_t)l * Ms + m;
-        double2 r = a.w0[g];
-        r = caxpy(a.c_E1, a.E1w[g], r);
-        r = caxpy(a.c_E2, b2[i], r);
-        r = caxpy(a.omega, b0[i], r);
-        r = caxpy(-a.omega * k.drw[m], a.w1[g], r);
+        C r = Pr::in(a.w0[g]);
+        r = col::gaxpy(cE1, Pr::in(a.E1w[g]), r);
+        r = col::gaxpy(cE2, b2[i], r);
+        r = col::gaxpy(omega, b0[i], r);
+        r = col::gaxpy((-omega) * Pr::s(k.drw[m]), Pr::in(a.w1[g]), r);
         b2[i] = r;
       }
     }
     __syncthreads();
   } else {
-    tload(b2, a.w0, G, m0, M);  // R_w given
+    col::tloadp(b2, a.w0, G, m0, M);  // R_w given
     __syncthreads();
   }
   if (MODE != VB_RHS) {
-    for (int i = threadIdx.x; i < G * TM; i += blockDim.x) b4[i] = caxpy(k.gdt, b4[i], b2[i]);
+    for (int i = threadIdx.x; i < G * TM; i += blockDim.x) b4[i] = col::gaxpy(gdt, b4[i], b2[i]);
     __syncthreads();
   }
 
@@ -311,24 +322,24 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
       a_to_coef<AK>(k, ds, nullptr, a.Atf, b0, b1, m0);
     }
     if constexpr (AK == AK_F32_COEF) {  // E_theta in the Galerkin basis
-      tload_f2d(b2, a.Atf, G, m0, M);
+      col::tloadp(b2, a.Atf, G, m0, M);
     } else {
       __syncthreads();
-      for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = cneg(b1[i]);
+      for (int i = threadIdx.x; i < PT; i += blockDim.x) b1[i] = col::gneg(b1[i]);
       __syncthreads();
       tpinv_dir(b2, b1, G);
     }
     __syncthreads();
     if (MODE == VB_RHS) {
-      tstore(b2, a.Et, G, m0, M);
+      col::tstorep(b2, a.Et, G, m0, M);
     } else if (MODE == VB_STAGE1) {
-      tstore(b2, a.E1t, G, m0, M);
+      col::tstorep(b2, a.E1t, G, m0, M);
       for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
         const int l = i / TM, m = mode_of(i, m0);
-        if (m < M) b2[i] = caxpy(a.alpha, b2[i], a.t0[(size_t)l * Ms + m]);
+        if (m < M) b2[i] = col::gaxpy(alpha, b2[i], Pr::in(a.t0[(size_t)l * Ms + m]));
       }
     } else {  // I_t = w1 (shared basis) or pinv_dir(S_w w1)
-      tload(b0, a.w1, G, m0, M);
+      col::tloadp(b0, a.w1, G, m0, M);
       __syncthreads();
       if (k.mixed) {
         tstencil_w(k, b1, b0);
@@ -336,32 +347,34 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
         tpinv_dir(b0, b1, G);
         __syncthreads();
       }
+      const T iac = Pr::s(a.inv_alpha_c);
       for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
         const int l = i / TM, m = mode_of(i, m0);
         if (m >= M) continue;
         const size_t g = (size_t)l * Ms + m;
-        double2 r = a.t0[g];
-        r = caxpy(a.c_E1, a.E1t[g], r);
-        r = caxpy(a.c_E2, b2[i], r);
-        r = caxpy(a.omega, b0[i], r);
-        r = caxpy(-a.omega * k.drt[m], a.t1[g], r);
+        C r = Pr::in(a.t0[g]);
+        r = col::gaxpy(cE1, Pr::in(a.E1t[g]), r);
+        r = col::gaxpy(cE2, b2[i], r);
+        r = col::gaxpy(omega, b0[i], r);
+        const C t1v = Pr::in(a.t1[g]);
+        r = col::gaxpy((-omega) * Pr::s(k.drt[m]), t1v, r);
         if (a.inv_alpha_c != 0.0) {
-          const double2 c = cscale(csub(a.t1[g], a.t1p[g]), a.inv_alpha_c);
-          r = caxpy(a.omega, c, r);
+          const C c = gscale(gsub(t1v, Pr::in(a.t1p[g])), iac);
+          r = col::gaxpy(omega, c, r);
         }
         b2[i] = r;
       }
     }
     __syncthreads();
   } else {
-    tload(b2, a.t0, G, m0, M);  // R_th given
+    col::tloadp(b2, a.t0, G, m0, M);  // R_th given
     __syncthreads();
   }
   if (MODE != VB_RHS) {
-    tstore(b2, a.Rt, G, m0, M);
+    col::tstorep(b2, a.Rt, G, m0, M);
     for (int i = threadIdx.x; i < G * TM; i += blockDim.x) {
       const int m = mode_of(i, m0);
-      b0[i] = (m < M) ? cscale(b2[i], k.inv_at[m]) : czero();
+      b0[i] = (m < M) ? gscale(b2[i], Pr::s(k.inv_at[m])) : col::gzero<C>();
     }
     __syncthreads();
     if (k.mixed) {  // theta basis -> w basis
@@ -370,23 +383,27 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
       tpinv_w(k, b0, b1);
       __syncthreads();
     }
-    const double c = k.gdt * k.Ra;
-    for (int i = threadIdx.x; i < G * TM; i += blockDim.x) b4[i] = caxpy(c, b0[i], b4[i]);
+    const T c = Pr::s(k.gdt * k.Ra);
+    for (int i = threadIdx.x; i < G * TM; i += blockDim.x) b4[i] = col::gaxpy(c, b0[i], b4[i]);
     __syncthreads();
-    tstore(b4, a.rhs_w, G, m0, M);
+    col::tstorep(b4, a.rhs_w, G, m0, M);
   }
 }
 
 // =========================================================== back-substitution
+template <typename C = double2>
 __global__ void __launch_bounds__(NT) k_vpost(VK k, const double2* Rq, const double2* Rt,
                                               const double2* wn, double2* qo, double2* to,
                                               bool zero_mean) {
-  extern __shared__ double2 sm[];
+  using Pr = col::Prec<C>;
+  extern __shared__ double2 sm_raw[];
+  C* sm = reinterpret_cast<C*>(sm_raw);
   const int PT = k.P * TM;
-  double2 *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT;
+  C *b0 = sm, *b1 = sm + PT, *b2 = sm + 2 * PT;
   const int m0 = blockIdx.x * TM;
   const int M = k.M;
-  tload(b0, wn, k.G, m0, M);
+  const typename Pr::T gdt = Pr::s(k.gdt);
+  col::tloadp(b0, wn, k.G, m0, M);
   __syncthreads();
   tstencil_w(k, b1, b0);  // w Chebyshev coefficients
   __syncthreads();
@@ -396,7 +413,8 @@ __global__ void __launch_bounds__(NT) k_vpost(VK k, const double2* Rq, const dou
     const int l = i / TM, m = mode_of(i, m0);
     if (m >= M) continue;
     const size_t g = (size_t)l * M + m;
-    qo[g] = (zero_mean && m == 0) ? czero() : cscale(caxpy(k.gdt, b2[i], Rq[g]), k.inv_aq[m]);
+    qo[g] = (zero_mean && m == 0) ? czero()
+                                  : Pr::out(gscale(col::gaxpy(gdt, b2[i], Pr::in(Rq[g])), Pr::s(k.inv_aq[m])));
   }
   if (k.mixed) {  // w basis -> theta basis
     __syncthreads();
@@ -407,7 +425,8 @@ __global__ void __launch_bounds__(NT) k_vpost(VK k, const double2* Rq, const dou
     const int l = i / TM, m = mode_of(i, m0);
     if (m >= M) continue;
     const size_t g = (size_t)l * M + m;
-    to[g] = (zero_mean && m == 0) ? czero() : cscale(caxpy(k.gdt, b0[i], Rt[g]), k.inv_at[m]);
+    to[g] = (zero_mean && m == 0) ? czero()
+                                  : Pr::out(gscale(col::gaxpy(gdt, b0[i], Pr::in(Rt[g])), Pr::s(k.inv_at[m])));
   }
 }
 
@@ -698,15 +717,16 @@ cudaError_t vfwd_t(const Params& p, const Tables& t, const double2* q, const dou
   return cudaGetLastError();
 }
 
-template <int MODE, int AK>
+template <int MODE, int AK, typename C = double2>
 void vback_t(const VK& k, const VArgs& a, size_t sm, int grid, cudaStream_t st) {
-  cudaFuncSetAttribute(k_vback<MODE, AK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_vback<MODE, AK><<<grid, NT, sm, st>>>(k, a);
+  cudaFuncSetAttribute(k_vback<MODE, AK, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_vback<MODE, AK, C><<<grid, NT, sm, st>>>(k, a);
 }
 template <int MODE>
 void vback_ak(int ak, const VK& k, const VArgs& a, size_t sm, int grid, cudaStream_t st) {
   if (ak == AK_F64) vback_t<MODE, AK_F64>(k, a, sm, grid, st);
   else if (ak == AK_F32_NODAL) vback_t<MODE, AK_F32_NODAL>(k, a, sm, grid, st);
+  else if (a.df) vback_t<MODE, AK_F32_COEF, cdfl>(k, a, sm, grid, st);
   else vback_t<MODE, AK_F32_COEF>(k, a, sm, grid, st);
 }
 
@@ -829,11 +849,12 @@ cudaError_t launch_shell(const Params& p, const Tables& t, const double2* rhs_w,
 
 cudaError_t launch_vpost(const Params& p, const Tables& t, const double2* Rq, const double2* Rt,
                          const double2* w_new, double2* q_out, double2* t_out, bool zero_mean,
-                         cudaStream_t st) {
+                         cudaStream_t st, bool df) {
   VK k = make_vk(p, t);
   const size_t sm = vsmem(p, 3);
-  cudaFuncSetAttribute(k_vpost, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  k_vpost<<<vgrid(p), NT, sm, st>>>(k, Rq, Rt, w_new, q_out, t_out, zero_mean);
+  auto kern = df ? k_vpost<cdfl> : k_vpost<double2>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  kern<<<vgrid(p), NT, sm, st>>>(k, Rq, Rt, w_new, q_out, t_out, zero_mean);
   return cudaGetLastError();
 }
 
