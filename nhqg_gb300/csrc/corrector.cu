@@ -195,9 +195,10 @@ __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const doub
 // at the two end levels), the round trip above is
 //   theta_sbp' = R x + u_0 (Fs_0 . x) + u_1 (Fs_1 . x)
 // with R = c2s s2c (a few nonzeros per row), Fs_j = s2c^T F_j, u_j = c2s V[:,N-1+j].
-// One CTA holds kSM consecutive modes (coalesced 256-byte level rows);
-// thread (level group lg, mode mm) visits levels lg, lg + 16, ...
-constexpr int kSM = 16;
+// One CTA holds kSM consecutive modes (coalesced 128-byte level rows; the
+// 33 KB tile lets six CTAs share an SM); thread (level group lg, mode mm)
+// visits levels lg, lg + kLG, ...
+constexpr int kSM = 8;
 constexpr int kSubThreads = 256;
 constexpr int kLG = kSubThreads / kSM;  // level groups
 
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(kSubThreads) k_corr_sub_mid(SubK<typename Prec
   part[0][lg][mm] = d0;
   part[1][lg][mm] = d1;
   __syncthreads();
-  if (lg < 2) {  // 32 threads: (j, mm) totals, summed in a fixed order
+  if (lg < 2) {  // 2 kSM threads: (j, mm) totals, summed in a fixed order
     C acc = col::gzero<C>();
     for (int q = 0; q < kLG; ++q) acc = gadd(acc, part[lg][q][mm]);
     part[lg][0][mm] = acc;
