@@ -667,6 +667,7 @@ def run_closure(args, ws, rank):
     from nhqg_gb300 import NHQGConfig, make_grid, theta_perturbation_state
     from nhqg_gb300 import closure as CL
     from nhqg_gb300 import solver as S
+    from nhqg_gb300.diagnostics import compute_diagnostics
     from nhqg_gb300.engine import Engine
 
     def cfg(nz):
@@ -674,9 +675,18 @@ def run_closure(args, ws, rank):
         c.update(dt=5e-5)
         return c
     fine, coarse = make_grid(NHQGConfig(**cfg(256))), make_grid(NHQGConfig(**cfg(64)))
+    base = None
+    if args.closure_spinup > 0:
+        # one spun-up fine state (mixed step: 1e-11 of the plain one) from
+        # which every run branches with its own seeded theta' perturbation
+        base = S.to_device(theta_perturbation_state(fine, seed=1000, amplitude=args.closure_amp))
+        S.step_inplace(base, fine, args.closure_spinup, check=True, precision="mixed")
     runs = []
     for r in range(args.closure_runs):
         s = S.to_device(theta_perturbation_state(fine, seed=r, amplitude=args.closure_amp))
+        if base is not None:
+            s = S.sanitize_state(S.State(base.q_hat.clone(), base.w_hat.clone(),
+                                         base.th_hat + 1e-2 * s.th_hat, base.th_bar.clone()), fine)
         snaps = []
         for _ in range(args.closure_steps // 40):
             S.step_inplace(s, fine, 40)
@@ -706,6 +716,9 @@ def run_closure(args, ws, rank):
     e_cl.step(*s_cl, n_steps=k)
     ref = s_f.q_hat[:coarse.Nz + 1]
     err = lambda s: float(torch.linalg.norm(s.q_hat - ref) / torch.linalg.norm(ref))  # noqa: E731
+    diag = {lab: compute_diagnostics(st, g) for lab, st, g in
+            (("fine", s_f, fine), ("coarse", s_plain, coarse), ("coarse_closure", s_cl, coarse))}
+    pick = lambda key: {lab: d[key] for lab, d in diag.items()}  # noqa: E731
     if rank != 0:
         return None
     return {
@@ -713,7 +726,10 @@ def run_closure(args, ws, rank):
         "value": round(held_ratio, 4), "unit": "ratio (closure / no closure)", "n_gpus": ws,
         "higher_is_better": False, "vs_baseline": None, "dtype": "bf16 weights, fp32 accumulation",
         "data": (f"{args.closure_runs} fine runs of {args.closure_steps} steps from seeded theta' "
-                 f"(amplitude {args.closure_amp}), snapshots every 40 steps; the last run held out"),
+                 f"(amplitude {args.closure_amp}"
+                 + (f", added at 1e-2 to a state spun up for {args.closure_spinup} steps"
+                    if args.closure_spinup > 0 else "")
+                 + "), snapshots every 40 steps; the last run held out"),
         "config": {"workload": "closure study, fine 128^2x256, coarse 128^2x64, ncoef 64, dt=5e-5, "
                                "evolve_mean SBP2-PC sub4", "params": CL.n_params()},
         "train_loss_first_last_epoch": [round(hist[0], 5), round(hist[-1], 5)],
@@ -722,7 +738,8 @@ def run_closure(args, ws, rank):
         "a_posteriori": {"steps": k, "q_rel_err_no_closure": err(s_plain), "q_rel_err_closure": err(s_cl),
                          "tail_fraction_above_48": {"fine": _tail_fraction(fine, ref, 48),
                                                     "coarse": _tail_fraction(coarse, s_plain.q_hat, 48),
-                                                    "coarse_closure": _tail_fraction(coarse, s_cl.q_hat, 48)}},
+                                                    "coarse_closure": _tail_fraction(coarse, s_cl.q_hat, 48)},
+                         "Nusselt": pick("Nusselt"), "KE_tot": pick("KE_tot")},
     }
 
 
@@ -767,10 +784,12 @@ def main():
     ap.add_argument("--closure", action="store_true",
                     help="run the learned-closure study instead (its own JSON line)")
     ap.add_argument("--closure-runs", type=int, default=3)
-    ap.add_argument("--closure-steps", type=int, default=400)
-    ap.add_argument("--closure-amp", type=float, default=1e-3)
+    ap.add_argument("--closure-steps", type=int, default=800)
+    ap.add_argument("--closure-amp", type=float, default=0.1)
     ap.add_argument("--closure-epochs", type=int, default=30)
     ap.add_argument("--closure-post-steps", type=int, default=200)
+    ap.add_argument("--closure-spinup", type=int, default=30000,
+                    help="fine steps (mixed precision) to a common spun-up state the runs branch from")
     ap.add_argument("--ensemble", action="store_true",
                     help="time the 48-member batched ensemble instead (its own JSON line)")
     args = ap.parse_args()
