@@ -147,15 +147,19 @@ int nhqg_step(nhqg_ctx *ctx, nhqg_state *state, int n_steps, void *stream);
  * every array.
  *   NHQG_PRECISION_FP64 (default): the plain path, all FP64, the reference's
  *     dense per-shell inverses.
- *   NHQG_PRECISION_MIXED: the 2/3-rule products and the Chebyshev <-> nodal
- *     transforms that feed them and read them back run in FP32; the Galerkin
- *     stencils, stage combinations, the SBP2 mean exchange and the implicit w
- *     solve stay FP64, the last as an O(Nz) Chebyshev-tau solve per mode
- *     instead of the dense shell inverse.  Not supported
+ *   NHQG_PRECISION_MIXED: the horizontal products and the Chebyshev <-> nodal
+ *     transforms that feed them and read them back run in FP32 (TF32 split
+ *     products on the tensor cores for the transforms); the Galerkin
+ *     stencils, stage combinations and the SBP2 corrector's column transforms
+ *     run in double-float (an FP32 pair, about 48 significant bits, on the
+ *     FP32 pipe; fields stay FP64 in memory); the 1-D mean-temperature solves
+ *     and the implicit w solve stay FP64, the latter as an O(Nz)
+ *     Chebyshev-tau solve per mode instead of the dense shell inverse.  Not
+ *     supported
  *     (NHQG_ERR_UNSUPPORTED): legacy evolve_mean (its nodal exchange
  *     product), Nz whose 2*Nz is not 2^a 3^b, and a descriptor
  *     without shell_coef.
- * The first switch to MIXED allocates 6 FP32 fields of (Nz+1) x (2/3-band
+ * The first switch to MIXED allocates 6 FP32 fields of (Nz+1) x (stored
  * modes) each. */
 int nhqg_set_precision(nhqg_ctx *ctx, int precision);
 

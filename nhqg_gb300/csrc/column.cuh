@@ -138,15 +138,6 @@ __device__ __forceinline__ void tstore(const float2* b, float2* __restrict__ dst
     if (m < M) dst[(size_t)l * M + m] = b[i];
   }
 }
-// FP32 global field -> FP64 tile
-__device__ __forceinline__ void tload_f2d(double2* b, const float2* __restrict__ src, int nlev,
-                                          int m0, int M) {
-  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
-    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
-    const float2 v = (m < M) ? src[(size_t)l * M + m] : make_float2(0.f, 0.f);
-    b[i] = make_double2((double)v.x, (double)v.y);
-  }
-}
 __device__ __forceinline__ void tcvt(float2* f, const double2* b, int nlev) {
   for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x)
     f[i] = make_float2((float)b[i].x, (float)b[i].y);

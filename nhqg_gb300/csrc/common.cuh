@@ -10,11 +10,8 @@
 
 namespace nhqg {
 
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
-__device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
 // i * a
 __device__ __forceinline__ double2 cmul_i(double2 a) { return make_double2(-a.y, a.x); }
 // a * b

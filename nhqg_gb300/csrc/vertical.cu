@@ -29,7 +29,6 @@ using col::NT;
 using col::tload;
 using col::tstore;
 using col::tcvt;
-using col::tload_f2d;
 using col::tmat;
 using col::tstencil_dir;
 using col::tpinv_dir;

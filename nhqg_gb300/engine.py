@@ -141,8 +141,9 @@ class Engine:
         return int(self.lib.nhqg_last_launch_count(self.handle))
 
     def set_precision(self, precision: str) -> None:
-        """'fp64' (plain path) or 'mixed' (FP32 products and transforms, FP64
-        solves and mean exchange) for the following step / RHS / solve calls."""
+        """'fp64' (plain path) or 'mixed' (FP32 products and transforms,
+        double-float column algebra and corrector transforms, FP64 solves) for
+        the following step / RHS / solve calls."""
         if precision not in nat.PRECISION:
             raise ValueError(f"precision must be one of {sorted(nat.PRECISION)}, got {precision!r}")
         if precision != self.precision:

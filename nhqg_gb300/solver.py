@@ -13,8 +13,8 @@ place for drivers that own their buffers (the analogue of donation).
 ``precision`` (an addition without a reference counterpart) selects the
 plain FP64 path ('fp64', the default) or the mixed-precision path ('mixed':
 FP32 horizontal products and the Chebyshev <-> nodal transforms around them,
-FP64 Galerkin stencils, stage combinations, implicit solves and SBP2 mean
-exchange).
+double-float Galerkin stencils, stage combinations and SBP2 corrector
+transforms, FP64 implicit and 1-D mean-temperature solves).
 
 Every computation runs in the CUDA engine; there is no CPU path.
 """
