@@ -1,0 +1,56 @@
+"""CPU checks of bench.py: the reference arm's JSON contract on a tiny
+workload (both dealiasing rules), and the per-kernel work model that the
+roofline figures are computed from."""
+
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+
+import bench  # noqa: E402
+from nhqg_gb300 import NHQGConfig, make_grid  # noqa: E402
+
+
+@pytest.mark.parametrize("rule", ["23_rule", "32_rule"])
+def test_reference_arm_json(rule):
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--nx", "16",
+                          "--nz", "8", "--steps", "1", "--warmup", "1", "--rule", rule],
+                         capture_output=True, text=True, timeout=300, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "steps/s"
+    assert line["higher_is_better"] is True and line["steps"] == 1
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert ("3/2 rule" in line["config"]["workload"]) == (rule == "32_rule")
+
+
+@pytest.mark.parametrize("rule", ["23_rule", "32_rule"])
+def test_kernel_work_model(rule):
+    g = make_grid(NHQGConfig(**bench.workload(48, 16, rule)))
+    names = ["h1_col_ifft", "h2_row_products", "h3_col_fft", "h2_row_products_f32", "vfwd",
+             "vback_stage1", "vback_stage2", "shell_solve", "tau_solve", "corr_pre", "corr_sub_mid",
+             "corr_sub_last", "vpost", "to_f32", "tc_to_nodal", "tc_to_coef"]
+    for tc in (False, True):
+        for n in names:
+            flops, bytes_, pipe = bench.kernel_work(n, g, 1, tc)
+            assert bytes_ > 0 and flops >= 0, n
+            assert pipe in ("fp64", "fp32", "df64", "hbm"), (n, pipe)
+        # the mixed (tensor-core) step runs its column kernels in double-float
+        assert bench.kernel_work("corr_pre", g, 1, True)[2] == "df64"
+        assert bench.kernel_work("corr_pre", g, 1, False)[2] == "fp64"
+
+
+def test_kernel_work_padded_products():
+    """The 3/2 rule transforms Npad = 3Nx/2 points over the full band: about
+    2.4 times the 2/3 rule's row-product work."""
+    f23 = bench.kernel_work("h2_row_products", make_grid(NHQGConfig(**bench.workload(48, 16))), 1)[0]
+    f32 = bench.kernel_work("h2_row_products", make_grid(NHQGConfig(**bench.workload(48, 16, "32_rule"))), 1)[0]
+    assert 2.0 * f23 < f32 < 3.0 * f23
