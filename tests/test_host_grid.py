@@ -83,8 +83,11 @@ def test_shell_tables_bitwise(over):
     assert np.all(rows[~band] == -1)
 
 
-def test_theta_init_matches_reference_fixture():
-    meta, arrays = fixtures.load_case("prod16")
+@pytest.mark.parametrize("case", ["prod16", "pad32p16", "pad32l24"])
+def test_theta_init_matches_reference_fixture(case):
+    """The seeded theta' start against the reference's own, under the 2/3
+    rule (band-limited) and the 3/2 rule (full band)."""
+    meta, arrays = fixtures.load_case(case)
     cfg = dict(meta["cfg"])
     g = make_grid(NHQGConfig(**cfg))
     s = theta_perturbation_state(g, seed=meta["seed"])
