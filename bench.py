@@ -389,6 +389,29 @@ def _roofline(prof, grid, steps, peaks):
     return out
 
 
+def dominant_roofline(prof, roof, workload_key, peaks) -> dict:
+    """The roofline entry of the kernel class with the largest time share,
+    with its DRAM traffic per launch (ncu, where measured for this workload)
+    and the HBM view of that traffic beside its limiting-pipe figure."""
+    dname = max(prof.items(), key=lambda kv: kv[1][1])[0]
+    dom = dict(roof[dname])
+    dom["kernel"] = dname
+    dom["bound"] = dom.pop("pipe")
+    dom["traffic"] = None
+    dom["peak_source"] = {"fp64": "cuBLAS DGEMM 8192^3 measured in this run",
+                          "df64": "cuBLAS DGEMM 8192^3 measured in this run (FP64-equivalent flops)",
+                          "fp32": "cuBLAS SGEMM 8192^3 (TF32 off) measured in this run",
+                          "hbm": "MEASURED_PEAKS.json hbm_gbs"}[dom["bound"]]
+    if workload_key == (256, 256, "23_rule") and dname in NCU_TRAFFIC_256:
+        dom["traffic"] = NCU_TRAFFIC_256[dname]
+        dom["traffic_source"] = NCU_TRAFFIC_SOURCE
+        if peaks.get("hbm"):
+            gbs = dom["traffic"] / (dom["avg_launch_ms"] * 1e-3) / 1e9
+            dom["hbm_view"] = {"achieved_gbs": round(gbs, 1), "peak_gbs": peaks["hbm"],
+                               "frac": round(gbs / peaks["hbm"], 4)}
+    return dom
+
+
 def run_ours(args, ws, rank, local):
     import torch
     from nhqg_gb300 import NHQGConfig, make_grid, theta_perturbation_state
@@ -481,18 +504,7 @@ def run_ours(args, ws, rank, local):
         return None
     roof_mixed = _roofline(prof_mixed, grid, args.steps, peaks)
     roof_plain = _roofline(prof_plain, grid, args.steps, peaks)
-    dname = max(prof_mixed.items(), key=lambda kv: kv[1][1])[0]
-    dom = dict(roof_mixed[dname])
-    dom["kernel"] = dname
-    dom["bound"] = dom.pop("pipe")
-    dom["traffic"] = None
-    dom["peak_source"] = {"fp64": "cuBLAS DGEMM 8192^3 measured in this run",
-                          "df64": "cuBLAS DGEMM 8192^3 measured in this run (FP64-equivalent flops)",
-                          "fp32": "cuBLAS SGEMM 8192^3 (TF32 off) measured in this run",
-                          "hbm": "MEASURED_PEAKS.json hbm_gbs"}[dom["bound"]]
-    if (args.nx, args.nz, args.rule) == (256, 256, "23_rule") and dname in NCU_TRAFFIC_256:
-        dom["traffic"] = NCU_TRAFFIC_256[dname]
-        dom["traffic_source"] = NCU_TRAFFIC_SOURCE
+    dom = dominant_roofline(prof_mixed, roof_mixed, (args.nx, args.nz, args.rule), peaks)
 
     def shares(prof):
         tot = sum(v[1] for v in prof.values())

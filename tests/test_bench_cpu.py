@@ -54,3 +54,19 @@ def test_kernel_work_padded_products():
     f23 = bench.kernel_work("h2_row_products", make_grid(NHQGConfig(**bench.workload(48, 16))), 1)[0]
     f32 = bench.kernel_work("h2_row_products", make_grid(NHQGConfig(**bench.workload(48, 16, "32_rule"))), 1)[0]
     assert 2.0 * f23 < f32 < 3.0 * f23
+
+
+def test_dominant_roofline_entry():
+    """The JSON roofline block of the dominant kernel, from a synthetic
+    profile: largest-share class, bound and peak source, the ncu traffic of
+    the headline workload and its HBM view."""
+    g = make_grid(NHQGConfig(**bench.workload(48, 16)))
+    prof = {"h2_row_products_f32": (20, 13.0), "corr_pre": (20, 8.0), "corr_sub_mid": (60, 5.0)}
+    peaks = {"fp64": 1.1, "fp32": 70.0, "hbm": 6500.0}
+    roof = bench._roofline(prof, g, 10, peaks)
+    dom = bench.dominant_roofline(prof, roof, (256, 256, "23_rule"), peaks)
+    assert dom["kernel"] == "h2_row_products_f32" and dom["bound"] == "fp32"
+    assert dom["traffic"] == bench.NCU_TRAFFIC_256["h2_row_products_f32"]
+    assert 0.0 < dom["hbm_view"]["frac"] < 1.0 and dom["frac"] > 0
+    other = bench.dominant_roofline(prof, roof, (128, 256, "23_rule"), peaks)
+    assert other["traffic"] is None and "hbm_view" not in other
