@@ -35,6 +35,7 @@ from .nhqg_oracle import (  # noqa: F401
     sponge_product_32,
     compute_diagnostics,
     DIAG_KEYS,
+    DIAG_EXTRA_KEYS,
     energy_spectrum,
     vertical_mode_energy,
     high_mode_fraction,

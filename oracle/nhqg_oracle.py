@@ -1053,8 +1053,22 @@ def compute_diagnostics(state: OracleState, grid: OracleGrid) -> dict:
     out = dict(KE_bt=KE_bt, KE_bc=KE_tot - KE_bt, KE_tot=KE_tot, enstrophy=0.5 * q_sq,
                Nusselt=1.0 + vol_tw, Nusselt_dealiased=1.0 + vol_tw_d, vol_avg_tw=vol_tw,
                vol_avg_tw_dealiased=vol_tw_d, q_rms=np.sqrt(q_sq), w_rms=np.sqrt(w_sq),
-               th_rms=np.sqrt(th_sq), th_bar_max=float(np.max(np.abs(tb))))
+               th_rms=np.sqrt(th_sq), th_bar_max=float(np.max(np.abs(tb))),
+               heat_flux_mismatch=vol_tw_d - vol_tw)
+    # physical-space maxima over the Nx grid at every CGL level
+    # (nhqg/diagnostics.py:631-641)
+    kx3, ky3 = grid.kx[None], grid.ky[None]
+    u = _irfft2(-1j * ky3 * psi_n, Nx)
+    v = _irfft2(1j * kx3 * psi_n, Nx)
+    wp = _irfft2(w_n, Nx)
+    tp = _irfft2(th_n, Nx)
+    out.update(max_speed=np.max(np.sqrt(u ** 2 + v ** 2)), max_w=np.max(np.abs(wp)),
+               max_theta=np.max(np.abs(tp)), max_tw=np.max(np.abs(wp * tp)))
     return {k: float(v) for k, v in out.items()}
+
+
+# the further scalars of compute_diagnostics (nhqg/diagnostics.py:680-699)
+DIAG_EXTRA_KEYS = ("max_speed", "max_w", "max_theta", "max_tw", "heat_flux_mismatch")
 
 
 # ---------------------------------------------------------------------------

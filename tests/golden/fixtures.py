@@ -81,6 +81,14 @@ def load_diagnostics() -> dict:
         return {k: np.array(z[k]) for k in z.files}
 
 
+def load_diagnostics_extra() -> dict:
+    """Reference compute_diagnostics physical-space maxima and heat-flux
+    mismatch: ``<case>.<state>`` -> values in the order of ``keys``
+    (tests/golden/diagnostics_extra.npz; 2/3- and 3/2-rule cases)."""
+    with np.load(GOLDEN_DIR / "diagnostics_extra.npz") as z:
+        return {k: np.array(z[k]) for k in z.files}
+
+
 SPEC_KEYS = ("k_bins", "E_bt", "E_bc", "E_tot", "q", "w", "th")
 
 

@@ -5,6 +5,7 @@ tests)::
 
     python tests/golden/make_golden.py /path/to/NHQG
     python tests/golden/make_golden.py /path/to/NHQG --diagnostics
+    python tests/golden/make_golden.py /path/to/NHQG --diagnostics-extra
     python tests/golden/make_golden.py /path/to/NHQG --spectra
     python tests/golden/make_golden.py /path/to/NHQG --rk443
     python tests/golden/make_golden.py /path/to/NHQG --pad32
@@ -312,6 +313,44 @@ def diagnostics_main(ref_root: str) -> None:
     print(f"diagnostics: {len(out)} entries")
 
 
+DIAG_EXTRA_KEYS = ("max_speed", "max_w", "max_theta", "max_tw", "heat_flux_mismatch")
+
+
+def diagnostics_extra_main(ref_root: str) -> None:
+    """The further compute_diagnostics scalars (nhqg/diagnostics.py:631-641,
+    680-699: physical-space maxima at the CGL nodes and the heat-flux
+    mismatch) at the ``r`` and ``s0`` states of the 2/3- and 3/2-rule cases
+    -> ``diagnostics_extra.npz`` (``<case>.<state>`` = values in
+    DIAG_EXTRA_KEYS order)."""
+    sys.path.insert(0, str(HERE / "refshim"))
+    sys.path.insert(0, ref_root)
+    from nhqg import diagnostics, solver  # noqa: E402
+    from nhqg.config import NHQGConfig  # noqa: E402
+    from nhqg.grid import make_grid  # noqa: E402
+    import jax.numpy as jnp  # the stand-in  # noqa: E402
+
+    global jnp_asarray
+    jnp_asarray = jnp.asarray
+    out = {}
+    for name, over in {**CASES, **PAD_CASES}.items():
+        cfgd = dict(BASE)
+        cfgd.update(over)
+        override = cfgd.pop("_override_eta_sponge", False)
+        grid = make_grid(NHQGConfig(**cfgd))
+        if override:
+            eta_hat, sponge_phys = smooth_eta_sponge(grid)
+            grid = grid._replace(eta_hat=jnp.asarray(eta_hat), sponge_phys=jnp.asarray(sponge_phys))
+            if grid.horizontal_dealiasing == "32_rule":
+                grid = grid._replace(sponge_phys_pad=jnp.asarray(
+                    padded_sponge(sponge_phys, grid.Nx, int(grid.Npad))))
+        for label, st in (("r", rich_state(grid, solver, seed=0)),
+                          ("s0", theta_init(grid, solver, seed=0))):
+            d = diagnostics.compute_diagnostics(st, grid)
+            out[f"{name}.{label}"] = np.array([float(np.asarray(d[k])) for k in DIAG_EXTRA_KEYS])
+    np.savez_compressed(HERE / "diagnostics_extra.npz", keys=np.array(DIAG_EXTRA_KEYS), **out)
+    print(f"diagnostics_extra: {len(out)} entries")
+
+
 SPEC_KEYS = ("k_bins", "E_bt", "E_bc", "E_tot", "q", "w", "th")
 
 
@@ -385,6 +424,8 @@ if __name__ == "__main__":
     root = args[0] if args else "/root/reference"
     if "--diagnostics" in sys.argv:
         diagnostics_main(root)
+    elif "--diagnostics-extra" in sys.argv:
+        diagnostics_extra_main(root)
     elif "--spectra" in sys.argv:
         spectra_main(root)
     elif "--rk443" in sys.argv:

@@ -111,6 +111,25 @@ def test_oracle_diagnostics_golden(case):
             assert abs(got[key] - ref[i]) <= 1e-12 * max(abs(ref[i]), 1e-300) + 1e-300, (case, label, key)
 
 
+@pytest.mark.parametrize("case", fixtures.CASES + fixtures.PAD_CASES)
+def test_oracle_diagnostics_extra_golden(case):
+    """Physical-space maxima at the CGL nodes (max |u|, |w|, |theta|,
+    |w theta|) and the heat-flux mismatch against the reference's
+    compute_diagnostics (tests/golden/diagnostics_extra.npz,
+    nhqg/diagnostics.py:631-641, 680-699), both dealiasing rules."""
+    meta, arrays = fixtures.load_case(case)
+    grid = _grid(meta, arrays)
+    gd = fixtures.load_diagnostics_extra()
+    keys = [str(k) for k in gd["keys"]]
+    assert tuple(keys) == oracle.DIAG_EXTRA_KEYS
+    for label in ("r", "s0"):
+        got = oracle.compute_diagnostics(_state(arrays, label), grid)
+        ref = gd[f"{case}.{label}"]
+        for i, key in enumerate(keys):
+            tol = 1e-12 * max(abs(ref[i]), 1e-300) if key != "heat_flux_mismatch" else 1e-13
+            assert abs(got[key] - ref[i]) <= tol + 1e-300, (case, label, key, got[key], ref[i])
+
+
 @pytest.mark.parametrize("case", fixtures.CASES)
 def test_oracle_spectra_golden(case):
     """Shell and vertical spectra against the reference's energy_spectrum and
