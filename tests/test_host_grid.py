@@ -136,3 +136,12 @@ def test_ctx_create_rejects_bad_descriptor():
     assert lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(h)) == 2  # NHQG_ERR_UNSUPPORTED
     d.Nx = 32
     assert lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(h)) == 1  # null tables
+    # dealiasing rule: unknown value, and a 3/2 rule whose padded grid 3*20/2 = 30
+    # has a factor 5 (checked before any table or device allocation)
+    d.horizontal_dealiasing = 7
+    assert lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(h)) == 1  # NHQG_ERR_BAD_ARG
+    d.horizontal_dealiasing, d.Nx = 1, 20
+    assert lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(h)) == 2  # NHQG_ERR_UNSUPPORTED
+    d.Nx = 32  # Npad = 48: accepted up to the missing tables
+    assert lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(h)) == 1
+    assert not h.value
