@@ -145,3 +145,16 @@ def test_ctx_create_rejects_bad_descriptor():
     d.Nx = 32  # Npad = 48: accepted up to the missing tables
     assert lib.nhqg_ctx_create(ctypes.byref(d), ctypes.byref(h)) == 1
     assert not h.value
+
+
+def test_padded_spectral_arguments_checked_on_host():
+    """The 3/2-rule plane operators reject an Npad other than 3*Nx//2 (the
+    reference's Npad, nhqg/config.py:76-78) before touching the device."""
+    from nhqg_gb300 import spectral as SP
+    z = np.zeros((1, 16, 9), dtype=complex)
+    kx, ky = np.zeros((16, 1)), np.zeros((1, 9))
+    for fn in (SP.triple_jacobian, SP.triple_conservative_flux_divergence):
+        with pytest.raises(ValueError):
+            fn(z, z, z, z, kx, ky, 16, 16)
+    with pytest.raises(ValueError):
+        SP.sponge_product_32(z, np.zeros((24, 24)), 16, 32)
