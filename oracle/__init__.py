@@ -42,4 +42,6 @@ from .nhqg_oracle import (  # noqa: F401
     psi_ke_vertical_spectrum,
     shell_bin_index,
     spectra,
+    shell_spectrum,
+    field_shell_spectra,
 )

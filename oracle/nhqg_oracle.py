@@ -1129,6 +1129,26 @@ def energy_spectrum(psi_nodal: np.ndarray, ksq: np.ndarray, cc_weights: np.ndarr
     return k_bins, E_bt, E_tot - E_bt, E_tot
 
 
+def shell_spectrum(field_nodal: np.ndarray, ksq: np.ndarray, cc_weights: np.ndarray, L: float,
+                   n_bins: int | None = None):
+    """Depth-integrated shell spectrum of a horizontally spectral field:
+    (k_bins, sum over each shell of w_k sum_j cc_j |f_j(k)|^2), unnormalised
+    (nhqg/diagnostics.py:104-111)."""
+    f2 = np.einsum("j,j...->...", cc_weights, np.abs(field_nodal) ** 2)
+    return shell_bin_sum(f2 * horizontal_rfft_weight(ksq), ksq, L, n_bins)
+
+
+def field_shell_spectra(state: OracleState, grid: OracleGrid, n_bins: int | None = None) -> dict:
+    """The q, w, theta horizontal shell spectra of compute_diagnostics at the
+    CGL nodes (nhqg/diagnostics.py:667-669)."""
+    q, w, th, _ = state
+    cc, ksq, L = grid.cc_weights, grid.ksq, grid.cfg.L
+    k_bins, qs = shell_spectrum(vmat(grid.V, q), ksq, cc, L, n_bins)
+    _, ws = shell_spectrum(vmat(grid.V, vmat(grid.w_stencil, w)), ksq, cc, L, n_bins)
+    _, ts = shell_spectrum(vmat(grid.V, vmat(grid.dirichlet_stencil, th)), ksq, cc, L, n_bins)
+    return dict(k_bins=k_bins, q=qs, w=ws, th=ts)
+
+
 def vertical_mode_energy(field_hat: np.ndarray) -> np.ndarray:
     """Sum over the horizontal modes of |f_n|^2 per Chebyshev index
     (nhqg/diagnostics.py:583-585)."""

@@ -89,6 +89,13 @@ def load_diagnostics_extra() -> dict:
         return {k: np.array(z[k]) for k in z.files}
 
 
+def load_field_spectra() -> dict:
+    """Reference horizontal shell spectra of q, w, theta at the CGL nodes:
+    ``<case>.<state>.<k_bins|q|w|th>`` (tests/golden/field_spectra.npz)."""
+    with np.load(GOLDEN_DIR / "field_spectra.npz") as z:
+        return {k: np.array(z[k]) for k in z.files}
+
+
 SPEC_KEYS = ("k_bins", "E_bt", "E_bc", "E_tot", "q", "w", "th")
 
 

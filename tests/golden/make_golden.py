@@ -317,11 +317,12 @@ DIAG_EXTRA_KEYS = ("max_speed", "max_w", "max_theta", "max_tw", "heat_flux_misma
 
 
 def diagnostics_extra_main(ref_root: str) -> None:
-    """The further compute_diagnostics scalars (nhqg/diagnostics.py:631-641,
-    680-699: physical-space maxima at the CGL nodes and the heat-flux
-    mismatch) at the ``r`` and ``s0`` states of the 2/3- and 3/2-rule cases
-    -> ``diagnostics_extra.npz`` (``<case>.<state>`` = values in
-    DIAG_EXTRA_KEYS order)."""
+    """The further compute_diagnostics outputs (nhqg/diagnostics.py:631-641,
+    667-669, 680-699) at the ``r`` and ``s0`` states of the 2/3- and 3/2-rule
+    cases: the physical-space maxima at the CGL nodes and the heat-flux
+    mismatch -> ``diagnostics_extra.npz`` (``<case>.<state>`` = values in
+    DIAG_EXTRA_KEYS order), and the q, w, theta horizontal shell spectra ->
+    ``field_spectra.npz`` (``<case>.<state>.<k_bins|q|w|th>``)."""
     sys.path.insert(0, str(HERE / "refshim"))
     sys.path.insert(0, ref_root)
     from nhqg import diagnostics, solver  # noqa: E402
@@ -331,7 +332,7 @@ def diagnostics_extra_main(ref_root: str) -> None:
 
     global jnp_asarray
     jnp_asarray = jnp.asarray
-    out = {}
+    out, spec = {}, {}
     for name, over in {**CASES, **PAD_CASES}.items():
         cfgd = dict(BASE)
         cfgd.update(over)
@@ -347,8 +348,12 @@ def diagnostics_extra_main(ref_root: str) -> None:
                           ("s0", theta_init(grid, solver, seed=0))):
             d = diagnostics.compute_diagnostics(st, grid)
             out[f"{name}.{label}"] = np.array([float(np.asarray(d[k])) for k in DIAG_EXTRA_KEYS])
+            for key, ref_key in (("k_bins", "k_bins"), ("q", "q_horiz_spec"), ("w", "w_horiz_spec"),
+                                 ("th", "th_horiz_spec")):
+                spec[f"{name}.{label}.{key}"] = np.asarray(d[ref_key], dtype=np.float64)
     np.savez_compressed(HERE / "diagnostics_extra.npz", keys=np.array(DIAG_EXTRA_KEYS), **out)
-    print(f"diagnostics_extra: {len(out)} entries")
+    np.savez_compressed(HERE / "field_spectra.npz", **spec)
+    print(f"diagnostics_extra: {len(out)} entries; field_spectra: {len(spec)} arrays")
 
 
 SPEC_KEYS = ("k_bins", "E_bt", "E_bc", "E_tot", "q", "w", "th")

@@ -130,6 +130,23 @@ def test_oracle_diagnostics_extra_golden(case):
             assert abs(got[key] - ref[i]) <= tol + 1e-300, (case, label, key, got[key], ref[i])
 
 
+@pytest.mark.parametrize("case", fixtures.CASES + fixtures.PAD_CASES)
+def test_oracle_field_spectra_golden(case):
+    """Horizontal shell spectra of q, w, theta (compute_diagnostics' q/w/th
+    horizontal spectra, nhqg/diagnostics.py:104-111, 667-669) against the
+    reference: 1e-12 relative to each spectrum's largest entry."""
+    meta, arrays = fixtures.load_case(case)
+    grid = _grid(meta, arrays)
+    gs = fixtures.load_field_spectra()
+    for label in ("r", "s0"):
+        got = oracle.field_shell_spectra(_state(arrays, label), grid)
+        for key in ("k_bins", "q", "w", "th"):
+            ref = gs[f"{case}.{label}.{key}"]
+            assert got[key].shape == ref.shape, (case, label, key)
+            scale = max(float(np.max(np.abs(ref))), 1e-300)
+            assert float(np.max(np.abs(got[key] - ref))) <= 1e-12 * scale, (case, label, key)
+
+
 @pytest.mark.parametrize("case", fixtures.CASES)
 def test_oracle_spectra_golden(case):
     """Shell and vertical spectra against the reference's energy_spectrum and
