@@ -206,7 +206,9 @@ int nhqg_sbp2_corrector(nhqg_ctx *ctx, const nhqg_state *in, nhqg_state *out,
 
 /* triple_conservative_flux_divergence_23 / triple_jacobian_23
  * (nhqg/spectral.py:331-358) on `levels` planes (Nx, Nk) complex128 each:
- * inputs psi, q, w, th; outputs Aq, Aw, Ath (masked). advection = NHQG_ADV_*. */
+ * inputs psi, q, w, th; outputs Aq, Aw, Ath (masked). advection = NHQG_ADV_*.
+ * The outputs are written while inputs are still being read: no output may
+ * overlap an input. */
 int nhqg_triple_advection_23(nhqg_ctx *ctx, int advection, int levels,
                              const void *psi, const void *q, const void *w,
                              const void *th, void *Aq, void *Aw, void *Ath,
@@ -215,17 +217,21 @@ int nhqg_triple_advection_23(nhqg_ctx *ctx, int advection, int levels,
 /* Allocation-free variant of nhqg_triple_advection_23.  It has no
  * counterpart in the reference.  It is for callers that must not allocate
  * device memory themselves: XLA FFI handlers (all buffers come from XLA's
- * allocator), code inside CUDA-graph capture, fixed device-memory pools.  No
- * context is needed and nothing is allocated: the FFT tables and the H1/H2
+ * allocator) and hosts that run on a fixed device-memory pool.  No context is
+ * needed and nothing is allocated: the FFT tables and the H1/H2
  * intermediates live in one static __device__ array of
  * NHQG_NOALLOC_SCRATCH_BYTES per GPU, held from library load until process
  * exit.  kx (Nx doubles) and ky (Nx/2+1 doubles) are device pointers with the
- * reference's wavenumbers; planes as in nhqg_triple_advection_23.  Levels are
- * processed in chunks that fit the array; Nx above 2048, or an Nx whose single
- * level does not fit, returns NHQG_ERR_UNSUPPORTED / NHQG_ERR_SCRATCH_TOO_SMALL.
+ * reference's wavenumbers; planes as in nhqg_triple_advection_23, and no
+ * output may overlap an input (NHQG_ERR_BAD_ARG).  Levels are processed in
+ * chunks that fit the array.  One level must fit: with the 32 MiB array that
+ * holds up to Nx = 648 (flux) and Nx = 576 (Jacobian); a larger Nx returns
+ * NHQG_ERR_SCRATCH_TOO_SMALL, and Nx above 2048 NHQG_ERR_UNSUPPORTED.
  * The first call on each device sets up the array's address with that device
- * current (make it before any stream capture).  All calls share the array, so
- * calls that overlap on the GPU race on it. */
+ * current (make it before any stream capture); a device reset makes that
+ * address stale, so do not call this again in a process that reset the
+ * device.  All calls share the array, so calls that overlap on the GPU race
+ * on it. */
 #define NHQG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 int nhqg_triple_advection_23_noalloc(int advection, int Nx, int levels,
                                      const double *kx, const double *ky,

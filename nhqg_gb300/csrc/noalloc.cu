@@ -1,18 +1,21 @@
 // Allocation-free variant of the 2/3-rule triple advection.
 //
 // Some callers cannot allocate device memory themselves: an XLA FFI custom
-// call must take every buffer from XLA's allocator, work inside CUDA-graph
-// capture must not call cudaMalloc, and hosts with a fixed device-memory pool
-// forbid allocations outside it.  nhqg_triple_advection_23_noalloc serves
-// them: it creates no context and allocates nothing.  Its working storage (the
-// FFT twiddle/permutation tables and the H1/H2 intermediates) lives in one
-// file-scope __device__ array of NHQG_NOALLOC_SCRATCH_BYTES, which every GPU
-// that loads this library holds from module load until process exit.
+// call must take every buffer from XLA's allocator, and hosts that run on a
+// fixed device-memory pool forbid allocations outside it.
+// nhqg_triple_advection_23_noalloc serves them: it creates no context and
+// allocates nothing.  Its working storage (the FFT twiddle/permutation tables
+// and the H1/H2 intermediates) lives in one file-scope __device__ array of
+// NHQG_NOALLOC_SCRATCH_BYTES, which every GPU that loads this library holds
+// from module load until process exit.
 //
 // The host reaches that array only through the address that
 // cudaGetSymbolAddress returns (the symbol's name in host code is a host-side
 // stand-in, not a device address).  The first call on each device looks it up
-// with that device current; make that first call before any stream capture.
+// with that device current and keeps it for later calls; make that first call
+// before any stream capture.  cudaDeviceReset destroys the context that holds
+// the array, so after a reset the cached address is stale: do not call this
+// entry point again in a process that reset the device.
 // All calls share the array and it keeps the last call's contents, so calls
 // that overlap on the GPU (other streams, other host threads on the same
 // device) race on it and must be serialised by the caller.
@@ -93,6 +96,15 @@ extern "C" int nhqg_triple_advection_23_noalloc(int advection, int Nx, int level
   const size_t work_bytes = NHQG_NOALLOC_SCRATCH_BYTES - kTableBytes;
   const int chunk = (int)std::min<size_t>((size_t)levels, work_bytes / per_level);
   if (chunk < 1) return NHQG_ERR_SCRATCH_TOO_SMALL;
+  {
+    // the outputs are zeroed before any input is read: no output may overlap an input
+    const size_t bytes = (size_t)levels * Nx * (Nx / 2 + 1) * 16;
+    const char* ins[4] = {(const char*)psi, (const char*)q, (const char*)w, (const char*)th};
+    const char* outs[3] = {(const char*)Aq, (const char*)Aw, (const char*)Ath};
+    for (const char* o : outs)
+      for (const char* i : ins)
+        if (o < i + bytes && i < o + bytes) return NHQG_ERR_BAD_ARG;
+  }
 
   void* base = nullptr;
   int rc = scratch_address(&base);
@@ -110,6 +122,8 @@ extern "C" int nhqg_triple_advection_23_noalloc(int advection, int Nx, int level
   wk.x2 = wk.x1 + wk.x1_elems;
   wk.x2_elems = (size_t)ng * chunk * d.Mc * d.Nx;
 
+  // an error left pending by other code on this thread stays for its owner to read
+  if (cudaPeekAtLastError() != cudaSuccess) return NHQG_ERR_CUDA;
   k_noalloc_tables<<<(Nx + 255) / 256, 256, 0, st>>>(plan, t.tw, t.perm);
   if (cudaGetLastError() != cudaSuccess) return NHQG_ERR_CUDA;
   const size_t plane = (size_t)d.Nx * d.Nk;

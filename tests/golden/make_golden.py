@@ -426,7 +426,10 @@ def jaxprng_main(ref_root: str) -> None:
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    root = args[0] if args else "/root/reference"
+    if not args:
+        sys.exit("usage: make_golden.py <path to the NHQG reference checkout> [--diagnostics | "
+                 "--diagnostics-extra | --spectra | --rk443 | --pad32 | --jaxprng]")
+    root = args[0]
     if "--diagnostics" in sys.argv:
         diagnostics_main(root)
     elif "--diagnostics-extra" in sys.argv:

@@ -1,8 +1,8 @@
 """Allocation-free triple advection against the context-based entry point.
 
 Callers that must not allocate device memory themselves -- XLA FFI handlers
-(every buffer comes from XLA's allocator), code running under CUDA-graph
-capture, hosts with a fixed device-memory pool -- use
+(every buffer comes from XLA's allocator), hosts with a fixed device-memory
+pool -- use
 ``nhqg_triple_advection_23_noalloc``, which keeps its working storage in one
 static device array instead of a context.  The test calls it through the C ABI
 twice in a row (the second call starts from the first call's leftover scratch)
@@ -38,7 +38,9 @@ def _wavenumbers(Nx, L=31.0):
     return kx, ky
 
 
-@pytest.mark.parametrize("form,Nx,levels", [("flux", 64, 5), ("jacobian", 48, 3), ("flux", 256, 9)])
+# Nx=256 with 9 levels runs in two chunks in both forms (6 + 3 levels)
+@pytest.mark.parametrize("form,Nx,levels", [("flux", 64, 5), ("jacobian", 48, 3), ("flux", 256, 9),
+                                            ("jacobian", 256, 9)])
 def test_noalloc_matches_context_entry_point(form, Nx, levels):
     lib = nat.load()
     rng = np.random.default_rng(Nx + levels)
@@ -74,3 +76,24 @@ def test_noalloc_rejects_sizes_beyond_scratch():
     rc = lib.nhqg_triple_advection_23_noalloc(nat.ADV["flux"], 4096, 1, p, p, p, p, p, p, p, p, p,
                                               stream)
     assert rc == 2  # NHQG_ERR_UNSUPPORTED
+    # one flux level at Nx=768 needs ~43 MB (the largest flux size that fits is 648)
+    rc = lib.nhqg_triple_advection_23_noalloc(nat.ADV["flux"], 768, 1, p, p, p, p, p, p, p, p, p,
+                                              stream)
+    assert rc == 6
+
+
+def test_noalloc_rejects_outputs_overlapping_inputs():
+    lib = nat.load()
+    Nx, levels = 16, 2
+    shp = (levels, Nx, Nx // 2 + 1)
+    buf = [torch.zeros(shp, dtype=torch.complex128, device="cuda") for _ in range(4)]
+    kx, ky = _wavenumbers(Nx)
+    kx_d = torch.tensor(kx, dtype=torch.float64, device="cuda")
+    ky_d = torch.tensor(ky, dtype=torch.float64, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = [torch.zeros_like(buf[0]) for _ in range(2)]
+    # Aq == q (in-place use) is rejected before anything runs
+    rc = lib.nhqg_triple_advection_23_noalloc(
+        nat.ADV["flux"], Nx, levels, kx_d.data_ptr(), ky_d.data_ptr(),
+        *(b.data_ptr() for b in buf), buf[1].data_ptr(), out[0].data_ptr(), out[1].data_ptr(), stream)
+    assert rc == 1  # NHQG_ERR_BAD_ARG
