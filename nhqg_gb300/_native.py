@@ -21,7 +21,7 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libnhqg_gpu.so"
-SOURCES = ("horizontal.cu", "vertical.cu", "corrector.cu", "capi.cu", "noalloc.cu", "tau_solve.cu",
+SOURCES = ("horizontal.cu", "horizontal_reg.cu", "vertical.cu", "corrector.cu", "capi.cu", "noalloc.cu", "tau_solve.cu",
            "diag.cu", "closure.cu", "tc_vertical.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]

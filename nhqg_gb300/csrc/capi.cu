@@ -486,6 +486,12 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
       p.tc_vertical = !(e && e[0] == '0');
     }
   }
+  {
+    // FP32 products with register-resident FFTs where the length allows
+    // (NHQG_REG_FFT=0 selects the shared-memory FFT kernels)
+    const char* e = getenv("NHQG_REG_FFT");
+    p.reg_fft = !(e && e[0] == '0');
+  }
 
   // ---- work buffers ----
   Work& w = c->w;

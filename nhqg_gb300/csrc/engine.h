@@ -114,6 +114,9 @@ struct Params {
   int h_col_kib[2], h_row_kib[2];
   // mixed-precision vertical transforms on the tensor cores (else FP32 DCT)
   bool tc_vertical;
+  // FP32 horizontal products with register-resident FFTs (horizontal_reg.cu)
+  // where the transform length allows, else the shared-memory FFT kernels
+  bool reg_fft;
   int scheme;  // NHQG_SCHEME_*
 };
 
@@ -223,6 +226,12 @@ cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const H
 
 cudaError_t launch_horizontal_f32(const Params& p, const Tables& t, Work& w,
                                   const HorizArgsT<float2, float2>& a, cudaStream_t st, int* nlaunch);
+// register-resident FFT variant (transform lengths 64, 128, 256 of the 2/3
+// rule); cudaErrorNotSupported for other lengths
+bool horizontal_reg_supported(int N);
+cudaError_t launch_horizontal_f32_reg(const Params& p, const Tables& t, Work& w,
+                                      const HorizArgsT<float2, float2>& a, cudaStream_t st,
+                                      int* nlaunch);
 
 // learned vertical-tail closure for q (csrc/closure.cu)
 struct ClosureModel {

@@ -424,6 +424,8 @@ cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const H
 cudaError_t launch_horizontal_f32(const Params& p, const Tables& t, Work& w,
                                   const HorizArgsT<float2, float2>& a, cudaStream_t st,
                                   int* nlaunch) {
+  if (p.reg_fft && !p.d.pad && horizontal_reg_supported(p.d.Nh))
+    return launch_horizontal_f32_reg(p, t, w, a, st, nlaunch);
   HTables<float2> ht{t.kx_f, t.ky_f, t.inv_denom, t.eta_f, t.sponge_f, t.eta_phys_f, t.tw_f, t.perm};
   return launch_horizontal_t<float2, float2>(p, ht, w, a, st, nlaunch);
 }
