@@ -273,55 +273,39 @@ def workload_name(nx: int, nz: int, rule: str = "23_rule") -> str:
             "L=10Lc, Ra=100, Pr=1, dt=2e-5")
 
 
-def cpu_reference(cfgd: dict, samples: int = 1, warmup: int = 0) -> dict:
-    """Time the NumPy/SciPy port of the reference step on all host cores.
+def cpu_reference(cfgd: dict, steps: int = 2, warmup: int = 1, label: str | None = None) -> dict:
+    """Time whole steps of the NumPy/SciPy port of the reference step
+    (``oracle.imex_step``) on all host cores.
 
-    A full oracle step at 256^2 x 256 is minutes of CPU time, so one sample
-    is one evaluation of each operator of the step, and the step time is
-    their sum weighted by how often one ARS(2,2,2) + SBP2-PC step calls them:
-    2 x explicit RHS, 2 x implicit solve, 1 x implicit tendency,
-    2 x SBP2 corrector (4 substeps each), 3 x stage combination.  The per-shell
-    table build (reference make_grid work) is excluded, as on the GPU side.
-    ``samples`` samples after ``warmup`` untimed ones; the value is their mean."""
+    The grid and its per-shell tables are built first and excluded (the
+    reference builds them once in make_grid); then ``warmup`` untimed steps
+    and ``steps`` timed ones from the seeded theta' start; the value is
+    steps / elapsed.  In a same-machine comparison the unmodified reference
+    source under the NumPy stand-in for jax took 3.3x (256^2 x 256) and 1.3x
+    (64^2 x 32) the port's time per step (oracle/time_reference_cpu.py), so
+    the port is the faster of the two CPU paths."""
     import oracle
-    from oracle.nhqg_oracle import OracleConfig, OracleState
+    from oracle.nhqg_oracle import OracleConfig
     cores = os.cpu_count() or 1
     oracle.nhqg_oracle.set_threads(cores)
-    g = oracle.make_grid(OracleConfig(**cfgd), with_shell_inverses=False)
-    base = g.replace(thermal_closure="fixed_conduction", mean_exchange_discretization="legacy")
-    s = oracle.theta_perturbation_state(g, seed=0)
     t0 = time.perf_counter()
-    oracle.imex_implicit_solve(s.q_hat, s.w_hat, s.th_hat, base)  # builds the shell table
-    t_table = time.perf_counter() - t0
-    oracle.explicit_rhs(s, base)  # warm-up (FFT plans, BLAS pools)
-
-    def timed(fn):
-        t = time.perf_counter()
-        out = fn()
-        return time.perf_counter() - t, out
-
-    alpha = g.gamma_imex * g.dt
-
-    def one():
-        tE, E = timed(lambda: oracle.explicit_rhs(s, base))
-        tI, _ = timed(lambda: oracle.implicit_tendency(s, base))
-        tS, _ = timed(lambda: oracle.imex_implicit_solve(s.q_hat, s.w_hat, s.th_hat, base))
-        tC, _ = timed(lambda: oracle.apply_balanced_sbp2_corrector(s, g, alpha))
-        tX, _ = timed(lambda: OracleState(*(a + alpha * e for a, e in zip(s, E))))
-        return (tE, tS, tI, tC, tX)
-
+    g = oracle.make_grid(OracleConfig(**cfgd))
+    t_grid = time.perf_counter() - t0
+    s = oracle.theta_perturbation_state(g, seed=0)
     for _ in range(warmup):
-        one()
-    parts = np.mean([one() for _ in range(max(1, samples))], axis=0)
-    tE, tS, tI, tC, tX = (float(x) for x in parts)
-    t_step = 2 * tE + 2 * tS + tI + 2 * tC + 3 * tX
-    return {"value": 1.0 / t_step, "unit": "steps/s", "cores": cores, "kind": "port",
-            "sample": (f"{max(1, samples)} sample(s), each one evaluation of every step operator at "
-                       f"{cfgd['Nx']}^2x{cfgd['Nz']} (mean RHS {tE:.2f}s, implicit solve {tS:.2f}s, "
-                       f"implicit tendency {tI:.2f}s, SBP2 corrector {tC:.2f}s, stage combination "
-                       f"{tX:.3f}s) summed as 2E+2S+I+2C+3X; shell-table build excluded "
-                       f"({t_table:.0f}s); NumPy/SciPy execution of the reference algorithm, plain "
-                       "FP64 (not XLA)")}
+        s = oracle.imex_step(s, g)
+    t0 = time.perf_counter()
+    for _ in range(max(1, steps)):
+        s = oracle.imex_step(s, g)
+    t = time.perf_counter() - t0
+    n = max(1, steps)
+    return {"value": n / t, "unit": "steps/s", "cores": cores, "kind": "port",
+            "sample": (f"{n} whole steps (oracle.imex_step, after {warmup} untimed) of "
+                       f"{label or workload_name(cfgd['Nx'], cfgd['Nz'], cfgd['horizontal_dealiasing'])} "
+                       f"from the seeded theta' start, {t / n:.2f} s each; grid and shell tables built "
+                       f"beforehand ({t_grid:.1f} s, excluded); NumPy/SciPy restatement of the reference "
+                       "step on all host cores, plain FP64 (JAX is not installed; the unmodified reference "
+                       "source under a NumPy stand-in for jax is slower than this port)")}
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -412,6 +396,110 @@ def dominant_roofline(prof, roof, workload_key, peaks) -> dict:
     return dom
 
 
+def _tendency_shares(S, grid, state) -> dict:
+    """|E_f| / |I_f| per field: the explicit (advective) tendency against the
+    implicit (linear) one, a measure of how nonlinear the state is."""
+    import torch
+    E = S.explicit_rhs(state, grid)
+    I = S.implicit_tendency(state, grid)  # noqa: E741
+    return {n: float(torch.linalg.norm(e) / torch.linalg.norm(i)) if float(torch.linalg.norm(i)) > 0 else None
+            for n, e, i in zip(("q_hat", "w_hat", "th_hat"), E[:3], I[:3])}
+
+
+def _precision_study(S, grid, state, err_steps: int, label: str) -> dict:
+    """Mixed against plain from the same state: per-field relative L2 after 1
+    and ``err_steps`` steps, the 1-step increments, and the diagnostics; plus
+    the state's Nusselt number, kinetic energy and tendency shares."""
+    from nhqg_gb300.diagnostics import compute_diagnostics
+    names = ("q_hat", "w_hat", "th_hat", "th_bar")
+    d0 = compute_diagnostics(state, grid)
+    ref = S.State(*(t.clone() for t in state))
+    mix = S.State(*(t.clone() for t in state))
+    S.step_inplace(ref, grid, 1, check=True)
+    S.step_inplace(mix, grid, 1, check=True, precision="mixed")
+    err1 = {n: _rel(a, b) for n, a, b in zip(names, mix, ref)}
+    inc1 = {n: _rel(a - s0, b - s0) for n, a, b, s0 in zip(names, mix, ref, state)}
+    S.step_inplace(ref, grid, err_steps - 1, check=True)
+    S.step_inplace(mix, grid, err_steps - 1, check=True, precision="mixed")
+    errN = {n: _rel(a, b) for n, a, b in zip(names, mix, ref)}
+    d_ref, d_mix = compute_diagnostics(ref, grid), compute_diagnostics(mix, grid)
+    diag_cmp = {k: {"plain": d_ref[k], "mixed": d_mix[k],
+                    "rel_diff": abs(d_mix[k] - d_ref[k]) / abs(d_ref[k]) if d_ref[k] else abs(d_mix[k])}
+                for k in ("Nusselt", "Nusselt_dealiased", "KE_tot", "KE_bt", "w_rms", "th_rms")}
+    fields = names[:3]
+    return {"start": label,
+            "state": {"Nusselt_minus_1": d0["Nusselt"] - 1.0, "KE_tot": d0["KE_tot"],
+                      "w_rms": d0["w_rms"], "explicit_over_implicit_tendency": _tendency_shares(S, grid, state)},
+            "after_1_step": err1, "increment_1_step": inc1, f"after_{err_steps}_steps": errN,
+            "max_field_rel_err_after_1_step": max(err1[n] for n in fields),
+            f"max_field_rel_err_after_{err_steps}_steps": max(errN[n] for n in fields),
+            f"diagnostics_after_{err_steps}_steps": diag_cmp}
+
+
+def convecting_state(S, grid, coarse_nz: int, coarse_steps: int, settle_steps: int, amp: float = 1.0):
+    """A convecting start on ``grid``: a seeded theta' of amplitude ``amp``
+    stepped ``coarse_steps`` mixed steps on a coarse grid of the same box
+    (Nx/2 x coarse_nz, dt = 5e-5), spectrally prolonged onto ``grid``
+    (solver.prolong_state), then ``settle_steps`` plain steps on ``grid``."""
+    from nhqg_gb300 import make_grid, theta_perturbation_state
+    gc = make_grid(grid.cfg.with_updates(Nx=grid.Nx // 2, Nz=coarse_nz, dt=5e-5))
+    sc = S.to_device(theta_perturbation_state(gc, seed=0, amplitude=amp))
+    S.step_inplace(sc, gc, coarse_steps, check=True, precision="mixed")
+    fine = S.prolong_state(sc, gc, grid)
+    del sc
+    S.step_inplace(fine, grid, settle_steps, check=True)
+    desc = (f"seeded theta' (amplitude {amp}, PCG64 seed 0) stepped {coarse_steps} mixed steps "
+            f"(t = {coarse_steps * 5e-5:g}) on {grid.Nx // 2}^2x{coarse_nz}, prolonged onto "
+            f"{grid.Nx}^2x{grid.Nz}, then {settle_steps} plain steps")
+    return fine, desc
+
+
+def _e2e(S, grid, state, steps: int, ws: int) -> dict:
+    """End to end through the public API with pinned host buffers (mixed
+    path): every step uploads its input state and downloads its result.
+    imex_step_many overlaps those copies with the steps on two copy streams;
+    the serial imex_step call per step is timed beside it."""
+    import torch
+    pinned = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in S.to_host(state)]
+    outs = [tuple(torch.empty_like(p).pin_memory() for p in pinned) for _ in range(2)]
+    S.imex_step_many([pinned] * 2, grid, precision="mixed", out=outs)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ee0 = torch.cuda.Event(enable_timing=True)
+    ee1 = torch.cuda.Event(enable_timing=True)
+    ee0.record()
+    S.imex_step_many([pinned] * steps, grid, precision="mixed", out=outs)
+    ee1.record()
+    torch.cuda.synchronize()
+    e2e_ms = allmax(ee0.elapsed_time(ee1), ws)
+    barrier(ws)
+    es0 = torch.cuda.Event(enable_timing=True)
+    es1 = torch.cuda.Event(enable_timing=True)
+    es0.record()
+    for _ in range(steps):
+        res = S.imex_step(pinned, grid, precision="mixed")
+        for o, r in zip(outs[0], res):
+            o.copy_(r, non_blocking=True)
+    es1.record()
+    torch.cuda.synchronize()
+    e2e_serial_ms = allmax(es0.elapsed_time(es1), ws)
+    bytes_state = int(sum(p.numel() * p.element_size() for p in pinned))
+    return {"value": round(ws * steps / (e2e_ms * 1e-3), 4), "unit": "steps/s",
+            "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state, "steps": steps,
+            "api": ("nhqg_gb300.solver.imex_step_many(pinned host States, precision='mixed'): each step "
+                    "uploads its input and downloads its result, on two copy streams overlapped "
+                    "with the steps"),
+            "serial_imex_step": {"value": round(ws * steps / (e2e_serial_ms * 1e-3), 4), "unit": "steps/s",
+                                 "api": "imex_step(pinned host State) + D2H of the result, one "
+                                        "call per step, no overlap"}}
+
+
+def _shares(prof, steps: int) -> dict:
+    tot = sum(v[1] for v in prof.values())
+    return {k: {"launches": n, "ms_per_step": round(t / steps, 4), "share": round(t / tot, 4)}
+            for k, (n, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+
+
 def run_ours(args, ws, rank, local):
     import torch
     from nhqg_gb300 import NHQGConfig, make_grid, theta_perturbation_state
@@ -423,8 +511,6 @@ def run_ours(args, ws, rank, local):
     grid = make_grid(NHQGConfig(**cfgd))
     t_grid = time.perf_counter() - t0
     log(f"[rank {rank}] grid {args.nx}^2x{args.nz}: {t_grid:.1f}s, {grid.imex_inv.shape[0]} shells")
-    host0 = theta_perturbation_state(grid, seed=0)
-    state = S.to_device(host0)
     eng = engine_for(grid)
     peaks = {"fp64": dgemm_peak_tflops(), "fp32": sgemm_peak_tflops(), "hbm": measured_hbm_gbs()}
     tiles = None
@@ -433,26 +519,20 @@ def run_ours(args, ws, rank, local):
         tiles = eng.autotune()
         eng.set_precision("fp64")
 
-    # spin-up (plain FP64) from the seeded start, then the accuracy of the
-    # mixed step against the plain step from the same state
-    S.step_inplace(state, grid, args.spinup, check=True)
+    # precision study 1: the benchmark's own start, spun up by plain FP64 steps
+    t0 = time.perf_counter()
+    lin = S.to_device(theta_perturbation_state(grid, seed=0))
+    S.step_inplace(lin, grid, args.spinup, check=True)
+    study_lin = _precision_study(S, grid, lin, args.err_steps,
+                                 f"seeded theta' 1e-3 N(0,1) sin(pi Z) (PCG64 seed 0), {args.spinup} plain "
+                                 "FP64 steps")
+    del lin
+    # precision study 2: a convecting state (the timed steps start from it too)
+    state, conv_desc = convecting_state(S, grid, args.convect_nz, args.convect_steps, args.settle_steps)
+    study_conv = _precision_study(S, grid, state, args.err_steps, conv_desc)
     torch.cuda.synchronize()
-    ref = S.State(*(t.clone() for t in state))
-    mix = S.State(*(t.clone() for t in state))
-    S.step_inplace(ref, grid, 1, check=True)
-    S.step_inplace(mix, grid, 1, check=True, precision="mixed")
-    names = ("q_hat", "w_hat", "th_hat", "th_bar")
-    err1 = {n: _rel(a, b) for n, a, b in zip(names, mix, ref)}
-    inc1 = {n: _rel(a - s0, b - s0) for n, a, b, s0 in zip(names, mix, ref, state)}
-    S.step_inplace(ref, grid, args.err_steps - 1, check=True)
-    S.step_inplace(mix, grid, args.err_steps - 1, check=True, precision="mixed")
-    errN = {n: _rel(a, b) for n, a, b in zip(names, mix, ref)}
-    from nhqg_gb300.diagnostics import compute_diagnostics
-    d_ref, d_mix = compute_diagnostics(ref, grid), compute_diagnostics(mix, grid)
-    diag_cmp = {k: {"plain": d_ref[k], "mixed": d_mix[k],
-                    "rel_diff": abs(d_mix[k] - d_ref[k]) / abs(d_ref[k]) if d_ref[k] else abs(d_mix[k])}
-                for k in ("Nusselt", "Nusselt_dealiased", "KE_tot", "KE_bt", "w_rms", "th_rms")}
-    del ref, mix
+    t_studies = time.perf_counter() - t0
+    log(f"[rank {rank}] precision studies: {t_studies:.1f}s")
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -470,46 +550,13 @@ def run_ours(args, ws, rank, local):
     value = ws * args.steps / (ms_mixed * 1e-3)
     value_plain = ws * args.steps / (ms_plain * 1e-3)
 
-    # end to end through the public API with pinned host buffers (mixed path):
-    # every step uploads its input state and downloads its result.
-    # imex_step_many overlaps those copies with the steps on two copy streams;
-    # the serial imex_step call per step is timed beside it.
-    pinned = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in S.to_host(state)]
-    outs = [tuple(torch.empty_like(p).pin_memory() for p in pinned) for _ in range(2)]
-    e2e_steps = max(1, min(args.steps, 10))
-    S.imex_step_many([pinned] * 2, grid, precision="mixed", out=outs)
-    torch.cuda.synchronize()
-    barrier(ws)
-    ee0 = torch.cuda.Event(enable_timing=True)
-    ee1 = torch.cuda.Event(enable_timing=True)
-    ee0.record()
-    S.imex_step_many([pinned] * e2e_steps, grid, precision="mixed", out=outs)
-    ee1.record()
-    torch.cuda.synchronize()
-    e2e_ms = allmax(ee0.elapsed_time(ee1), ws)
-    barrier(ws)
-    es0 = torch.cuda.Event(enable_timing=True)
-    es1 = torch.cuda.Event(enable_timing=True)
-    es0.record()
-    for _ in range(e2e_steps):
-        res = S.imex_step(pinned, grid, precision="mixed")
-        for o, r in zip(outs[0], res):
-            o.copy_(r, non_blocking=True)
-    es1.record()
-    torch.cuda.synchronize()
-    e2e_serial_ms = allmax(es0.elapsed_time(es1), ws)
-    bytes_state = int(sum(p.numel() * p.element_size() for p in pinned))
+    e2e = _e2e(S, grid, state, max(1, min(args.steps, 10)), ws)
 
     if rank != 0:
         return None
     roof_mixed = _roofline(prof_mixed, grid, args.steps, peaks)
     roof_plain = _roofline(prof_plain, grid, args.steps, peaks)
     dom = dominant_roofline(prof_mixed, roof_mixed, (args.nx, args.nz, args.rule), peaks)
-
-    def shares(prof):
-        tot = sum(v[1] for v in prof.values())
-        return {k: {"launches": n, "ms_per_step": round(t / args.steps, 4), "share": round(t / tot, 4)}
-                for k, (n, t) in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 
     line = {
         "metric": METRIC,
@@ -524,47 +571,131 @@ def run_ours(args, ws, rank, local):
         "vs_baseline": None,
         "dtype": ("f32 products + tf32x3 tensor-core vertical transforms + double-float (f32 pair) "
                   "column algebra and corrector + f64 solves"),
-        "data": (f"synthetic: seeded theta' 1e-3 N(0,1) sin(pi Z) (PCG64 seed 0), spun up by "
-                 f"{args.spinup} plain FP64 steps"),
+        "data": f"synthetic: {conv_desc}",
         "config": {"workload": workload_name(args.nx, args.nz, args.rule), "path": "mixed", "Nx": args.nx, "Nz": args.nz,
                    "timed": "one step_inplace call of `steps` steps on a device-resident state",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
                    "l2": "state and per-step traffic >> 129 MB L2; no flush needed"},
         "plain_fp64": {"value": round(value_plain, 4), "unit": "steps/s",
                        "ms_per_step": round(ms_plain / args.steps, 4),
-                       "kernels": shares(prof_plain), "roofline": roof_plain},
+                       "kernels": _shares(prof_plain, args.steps), "roofline": roof_plain},
         "mixed_over_plain": round(value / value_plain, 3),
         "vertical_transforms": ("tcgen05 kind::tf32 tensor cores, TF32 hi/lo split operands (3 products), "
                                 "FP32 accumulation" if tc else "FP32 fast DCT-I on the CUDA cores"),
         "mixed_cuda_core_dct": (None if ms_dct is None else
                                 {"value": round(ws * args.steps / (ms_dct * 1e-3), 4), "unit": "steps/s",
                                  "ms_per_step": round(ms_dct / args.steps, 4)}),
-        "rel_err_vs_plain": {"after_1_step": err1, "increment_1_step": inc1,
-                             f"after_{args.err_steps}_steps": errN,
-                             f"diagnostics_after_{args.err_steps}_steps": diag_cmp},
+        "rel_err_vs_plain": study_conv,
+        "precision_study_config3_start": study_lin,
         "simulated_time_per_wall_hour": round(3600.0 * cfgd["dt"] * value / ws, 6),
         "gpu_launches": sum(n for n, _ in prof_mixed.values()),
         "roofline": dom,
-        "kernels": shares(prof_mixed),
+        "kernels": _shares(prof_mixed, args.steps),
         "roofline_by_kernel": roof_mixed,
         "autotuned_tiles_kib": tiles,
         "peaks": {"fp64_tflops": round(peaks["fp64"], 4), "fp32_tflops": round(peaks["fp32"], 3),
                   "hbm_gbs": peaks["hbm"], "fp32_nominal_tflops": round(NOMINAL_FP32_TFLOPS, 1)},
         "clocks": clk,
-        "e2e": {"value": round(ws * e2e_steps / (e2e_ms * 1e-3), 4), "unit": "steps/s",
-                "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state,
-                "api": ("nhqg_gb300.solver.imex_step_many(pinned host States, precision='mixed'): each step "
-                        "uploads its input and downloads its result, on two copy streams overlapped "
-                        "with the steps"),
-                "serial_imex_step": {"value": round(ws * e2e_steps / (e2e_serial_ms * 1e-3), 4),
-                                     "unit": "steps/s",
-                                     "api": "imex_step(pinned host State) + D2H of the result, one "
-                                            "call per step, no overlap"}},
+        "e2e": e2e,
         "finite": finite,
-        "grid_build_s": round(t_grid, 2),
     }
     if ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(cfgd)
+    line["setup_s"] = {"grid": round(t_grid, 2), "precision_studies": round(t_studies, 1)}
+    return line
+
+
+POLAR_METRIC = "NHQG steps/s at 256^2x32 polar trap: mixed-precision and plain FP64 on GB300"
+POLAR_NAME = ("256^2x32 polar trap ARS222, evolve_mean balanced_sbp2_pc sub4, flux, 2/3 rule, L=24Lc, Ra=100, "
+              "dt=5e-5, gamma=2.2e-3, trap_r_star=0.4L, trap_sharpness=20, sponge_rate=50, sponge_r_start=52, "
+              "sponge_sharpness=30, Neumann w top")
+
+
+def polar_workload() -> dict:
+    """The polar-trap configuration: 256^2 x 32, L = 24 L_c, Ra = 100,
+    dt = 5e-5, radial background-PV trap gamma = 2.2e-3 with the Rayleigh
+    sponge outside it, Neumann w at the top, evolve_mean + balanced SBP2-PC
+    (4 substeps).  Trap radius and sponge are the production-scaled values
+    (the default trap radius fails the eta resolution guard at this size)."""
+    L = 24 * L_C
+    c = workload(256, 32)
+    c.update(L=L, dt=5e-5, gamma=2.2e-3, w_bc_top="neumann", trap_r_star=0.4 * L, trap_sharpness=20.0,
+             sponge_rate=50.0, sponge_r_start=52.0, sponge_sharpness=30.0)
+    return c
+
+
+def run_polar(args, ws, rank, local):
+    """Polar-trap configuration: plain and mixed steps/s on a device-resident
+    state, a --polar-steps run of each from the seeded theta' start (finite,
+    diagnostics, mixed against plain), end to end through imex_step_many."""
+    import torch
+    from nhqg_gb300 import NHQGConfig, make_grid, theta_perturbation_state
+    from nhqg_gb300 import solver as S
+    from nhqg_gb300.diagnostics import compute_diagnostics
+    from nhqg_gb300.engine import engine_for
+
+    cfgd = polar_workload()
+    t0 = time.perf_counter()
+    grid = make_grid(NHQGConfig(**cfgd))
+    t_grid = time.perf_counter() - t0
+    eng = engine_for(grid)
+    peaks = {"fp64": dgemm_peak_tflops(), "fp32": sgemm_peak_tflops(), "hbm": measured_hbm_gbs()}
+    s0 = S.to_device(theta_perturbation_state(grid, seed=0))
+    # the configuration's run from the seeded start, both paths
+    runs = {}
+    for prec in ("fp64", "mixed"):
+        s = S.State(*(t.clone() for t in s0))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        S.step_inplace(s, grid, args.polar_steps, check=True, precision=prec)
+        e1.record()
+        torch.cuda.synchronize()
+        fin = all(bool(torch.isfinite(torch.view_as_real(t) if t.is_complex() else t).all()) for t in s)
+        runs[prec] = (s, e0.elapsed_time(e1), fin)
+    names = ("q_hat", "w_hat", "th_hat", "th_bar")
+    err = {n: _rel(a, b) for n, a, b in zip(names, runs["mixed"][0], runs["fp64"][0])}
+    diag = {p: compute_diagnostics(runs[p][0], grid) for p in runs}
+    state = runs["fp64"][0]
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_plain, prof_plain = _timed_arm(S, grid, eng, S.State(*(t.clone() for t in state)), "fp64", args, ws)
+    ms_mixed, prof_mixed = _timed_arm(S, grid, eng, S.State(*(t.clone() for t in state)), "mixed", args, ws)
+    clk = clocks.stop()
+    e2e = _e2e(S, grid, state, max(1, min(args.steps, 10)), ws)
+    if rank != 0:
+        return None
+    value = ws * args.steps / (ms_mixed * 1e-3)
+    value_plain = ws * args.steps / (ms_plain * 1e-3)
+    roof_mixed = _roofline(prof_mixed, grid, args.steps, peaks)
+    dom = dominant_roofline(prof_mixed, roof_mixed, (256, 32, "polar"), peaks)
+    keys = ("Nusselt", "Nusselt_dealiased", "KE_tot", "w_rms", "th_rms", "th_bar_max")
+    line = {
+        "metric": POLAR_METRIC, "value": round(value, 4), "unit": "steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms_mixed / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 products + f32 DCT vertical transforms (open-top w basis) + double-float column algebra "
+                 "and corrector + f64 solves",
+        "data": f"synthetic: seeded theta' 1e-3 N(0,1) sin(pi Z) (PCG64 seed 0), {args.polar_steps} plain steps",
+        "config": {"workload": POLAR_NAME, "path": "mixed", "Nx": 256, "Nz": 32,
+                   "timed": "one step_inplace call of `steps` steps on a device-resident state",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
+                   "l2": "state 60 MB < L2 at this size; per-step traffic (intermediates, tables) > L2"},
+        "plain_fp64": {"value": round(value_plain, 4), "unit": "steps/s", "ms_per_step": round(ms_plain / args.steps, 4),
+                       "kernels": _shares(prof_plain, args.steps)},
+        "mixed_over_plain": round(value / value_plain, 3),
+        f"run_{args.polar_steps}_steps": {
+            p: {"finite": runs[p][2], "ms_per_step": round(runs[p][1] / args.polar_steps, 4),
+                "diagnostics": {k: diag[p][k] for k in keys}} for p in runs},
+        f"mixed_vs_plain_after_{args.polar_steps}_steps": err,
+        "simulated_time_per_wall_hour": round(3600.0 * cfgd["dt"] * value / ws, 6),
+        "gpu_launches": sum(n for n, _ in prof_mixed.values()),
+        "roofline": dom, "kernels": _shares(prof_mixed, args.steps),
+        "clocks": clk, "e2e": e2e,
+        "setup_s": {"grid": round(t_grid, 2)},
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_reference(cfgd, label=POLAR_NAME)
     return line
 
 
@@ -756,20 +887,24 @@ def run_closure(args, ws, rank):
 
 
 def run_reference(args, ws, rank):
-    """CPU arm: the oracle port of the reference step on the host cores, on
-    this arm's workload, metric and units; rank 0 only."""
+    """CPU arm: whole steps of the oracle port of the reference step on the
+    host cores, on this arm's workload, metric and units; rank 0 only."""
     if rank != 0:
         return None
-    cfgd = workload(args.nx, args.nz, args.rule)
-    cb = cpu_reference(cfgd, samples=args.steps, warmup=max(0, min(args.warmup, 1)))
+    if args.config == "polar":
+        cfgd, metric, wname = polar_workload(), POLAR_METRIC, POLAR_NAME
+    else:
+        cfgd, metric = workload(args.nx, args.nz, args.rule), METRIC
+        wname = workload_name(args.nx, args.nz, args.rule)
+    cb = cpu_reference(cfgd, steps=args.steps, warmup=args.warmup, label=wname)
     cb["value"] = round(cb["value"], 6)  # the line's value
     return {
-        "metric": METRIC, "value": cb["value"], "unit": "steps/s", "n_gpus": ws,
+        "metric": metric, "value": cb["value"], "unit": "steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 / cb["value"], 2),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded theta' start)", "impl": "reference",
-        "config": {"workload": workload_name(args.nx, args.nz, args.rule), "path": "cpu_port",
-                   "Nx": args.nx, "Nz": args.nz, "parallelism": "host cores"},
+        "config": {"workload": wname, "path": "cpu_port", "Nx": cfgd["Nx"], "Nz": cfgd["Nz"],
+                   "parallelism": "host cores"},
         "cpu_baseline": cb,
         "e2e": {"value": round(cb["value"], 6), "unit": "steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -786,9 +921,20 @@ def main():
     ap.add_argument("--nz", type=int, default=256)
     ap.add_argument("--rule", default="23_rule", choices=["23_rule", "32_rule"],
                     help="horizontal dealiasing of the workload (the headline uses the 2/3 rule)")
-    ap.add_argument("--spinup", type=int, default=1000,
-                    help="plain FP64 steps from the seeded start before measuring "
-                         "(the precision study's configuration uses 5000)")
+    ap.add_argument("--config", default="headline", choices=["headline", "polar"],
+                    help="headline: 256^2x256 (the metric's configuration); polar: the 256^2x32 "
+                         "polar-trap configuration (its own JSON line)")
+    ap.add_argument("--spinup", type=int, default=5000,
+                    help="plain FP64 steps from the seeded 1e-3 theta' start before the first precision "
+                         "study (the configuration's 5000)")
+    ap.add_argument("--convect-nz", type=int, default=64,
+                    help="Nz of the coarse grid (Nx/2) the convecting state is spun up on")
+    ap.add_argument("--convect-steps", type=int, default=8000,
+                    help="mixed steps (dt=5e-5) of the coarse spin-up from a seeded theta' of amplitude 1")
+    ap.add_argument("--settle-steps", type=int, default=200,
+                    help="plain steps on the full grid after the prolongation")
+    ap.add_argument("--polar-steps", type=int, default=2000,
+                    help="steps of the polar configuration's run from the seeded start")
     ap.add_argument("--err-steps", type=int, default=500,
                     help="steps of the mixed-vs-plain accuracy comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -809,6 +955,8 @@ def main():
     ws, rank, local = dist_init()
     if args.impl == "reference":
         line = run_reference(args, ws, rank)
+    elif args.config == "polar":
+        line = run_polar(args, ws, rank, local)
     elif args.ensemble:
         line = run_ensemble(args, ws, rank)
     elif args.closure:

@@ -117,6 +117,14 @@ typedef struct nhqg_grid_desc {
   int horizontal_dealiasing;                   /* NHQG_DEALIAS_*; Nh = Nx for the
                                                   2/3 rule, Npad = 3Nx/2 for the
                                                   3/2 rule */
+  const double *eta_x_phys, *eta_y_phys;       /* (Nh,Nh) d eta/dx, d eta/dy on
+                                                  the grid of eta_phys, or NULL.
+                                                  The mixed path carries the trap
+                                                  PV as u . grad(eta) beside the
+                                                  products of q itself (no FP32
+                                                  cancellation of q against
+                                                  eta); NULL with eta_hat set
+                                                  disables NHQG_PRECISION_MIXED */
 } nhqg_grid_desc;
 
 typedef struct nhqg_ctx nhqg_ctx;
@@ -268,16 +276,21 @@ int nhqg_mean_temp_solve(nhqg_ctx *ctx, const double *R_th_bar, double *out,
                          int thermal_closure, void *stream);
 
 /* Scalar diagnostics of a state: the depth-integrated energies, rms values
- * and Nusselt numbers of compute_diagnostics (nhqg/diagnostics.py:597-690;
- * its spectra and budgets are not computed).  out: NHQG_DIAG_COUNT doubles
- * in DEVICE memory, written stream-ordered in the NHQG_DIAG_* order.  The
- * dealiased heat flux follows the mean equation's path (SBP grid for the
- * balanced SBP2 exchange).  Needs cc_weights in the descriptor. */
+ * and Nusselt numbers of compute_diagnostics (nhqg/diagnostics.py:597-690),
+ * the physical-space maxima over the Nx grid at every CGL node
+ * (max_speed = max sqrt(u^2 + v^2), max_w, max_theta, max_tw = max |w theta|;
+ * nhqg/diagnostics.py:631-641) and the heat-flux mismatch
+ * vol_avg_tw_dealiased - vol_avg_tw (its budgets are not computed).  out:
+ * NHQG_DIAG_COUNT doubles in DEVICE memory, written stream-ordered in the
+ * NHQG_DIAG_* order.  The dealiased heat flux follows the mean equation's
+ * path (SBP grid for the balanced SBP2 exchange).  Needs cc_weights in the
+ * descriptor. */
 enum {
   NHQG_DIAG_KE_BT = 0, NHQG_DIAG_KE_BC, NHQG_DIAG_KE_TOT, NHQG_DIAG_ENSTROPHY,
   NHQG_DIAG_NUSSELT, NHQG_DIAG_NUSSELT_DEALIASED, NHQG_DIAG_VOL_AVG_TW,
   NHQG_DIAG_VOL_AVG_TW_DEALIASED, NHQG_DIAG_Q_RMS, NHQG_DIAG_W_RMS, NHQG_DIAG_TH_RMS,
-  NHQG_DIAG_TH_BAR_MAX, NHQG_DIAG_COUNT
+  NHQG_DIAG_TH_BAR_MAX, NHQG_DIAG_MAX_SPEED, NHQG_DIAG_MAX_W, NHQG_DIAG_MAX_THETA,
+  NHQG_DIAG_MAX_TW, NHQG_DIAG_HEAT_FLUX_MISMATCH, NHQG_DIAG_COUNT
 };
 int nhqg_diagnostics(nhqg_ctx *ctx, const nhqg_state *state, double *out, void *stream);
 
@@ -287,7 +300,10 @@ int nhqg_diagnostics(nhqg_ctx *ctx, const nhqg_state *state, double *out, void *
  *   then (Nz+1) + (Nz-1) + (Nz-1) values: vertical_mode_energy (:583-585)
  *                       of q_hat, w_hat, th_hat per Chebyshev index;
  *   then (Nz+1) values: the psi kinetic energy per Chebyshev index,
- *                       sum_k w_k |k|^2 |psi_n(k)|^2 (w_k the rfft weights).
+ *                       sum_k w_k |k|^2 |psi_n(k)|^2 (w_k the rfft weights);
+ *   then 3 n_bins:      the horizontal shell spectra of q, w, theta at the
+ *                       CGL nodes (compute_diagnostics, nhqg/diagnostics.py:
+ *                       104-111, 667-669): per shell sum w_k sum_j cc_j |f_j|^2.
  * mode_bin: DEVICE int array of nhqg_mode_count() entries, the shell of each
  * compact mode (row r = kx index 0..2K with K = Nx/3, rows above K holding
  * kx = r - (2K+1); column c = ky index 0..K; m = r (K+1) + c) under the

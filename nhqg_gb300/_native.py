@@ -42,7 +42,8 @@ PRECISION = {"fp64": 0, "mixed": 1}
 SCHEME = {"ars222": 0, "rk443": 1}
 DEALIAS = {"23_rule": 0, "32_rule": 1}
 DIAG_KEYS = ("KE_bt", "KE_bc", "KE_tot", "enstrophy", "Nusselt", "Nusselt_dealiased",
-             "vol_avg_tw", "vol_avg_tw_dealiased", "q_rms", "w_rms", "th_rms", "th_bar_max")
+             "vol_avg_tw", "vol_avg_tw_dealiased", "q_rms", "w_rms", "th_rms", "th_bar_max",
+             "max_speed", "max_w", "max_theta", "max_tw", "heat_flux_mismatch")
 
 
 class NativeError(RuntimeError):
@@ -117,6 +118,7 @@ class GridDesc(ctypes.Structure):
         ("shell_coef", c_double_p), ("cc_weights", c_double_p),
         ("imex_scheme", ctypes.c_int),
         ("horizontal_dealiasing", ctypes.c_int),
+        ("eta_x_phys", c_double_p), ("eta_y_phys", c_double_p),
     ]
 
 

@@ -27,7 +27,8 @@ struct nhqg_ctx {
   // 1-D vectors [P]
   double *tb0, *tb1p, *tb1, *tb2p, *tb2, *E1tb, *E2tb, *Itb, *flux, *dtb;
   double* diag_part = nullptr;  // diagnostics block partials
-  double* spec_mode = nullptr;  // spectra: per-mode energies [2*M], allocated on first use
+  unsigned long long* diag_max = nullptr;  // physical-space maxima (bit patterns of doubles >= 0)
+  double* spec_mode = nullptr;  // spectra: per-mode energies [5*M], allocated on first use
   // ARS(4,4,3) (scheme RK443, legacy exchange): explicit E_0..E_3 and implicit
   // K_1..K_4 derivatives of (q, w, theta) [P*M] and of th_bar [P]
   double2* rkE[4][3] = {};
@@ -264,6 +265,20 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.tw, tw.data(), d.Nh);
     UP(t.perm, perm.data(), d.Nh);
   }
+  // transforms of length Nx for the physical-space diagnostics (the 3/2 rule's
+  // products run at Npad, the reference's maxima are taken on the Nx grid)
+  p.plan_nx = make_fft_plan(d.Nx);
+  if (d.Nh == d.Nx) {
+    t.tw_nx = t.tw;
+    t.perm_nx = t.perm;
+  } else if (p.plan_nx.npass > 0) {
+    std::vector<double2> tw(d.Nx);
+    for (int k = 0; k < d.Nx; ++k) tw[k] = twiddle(k, d.Nx);
+    std::vector<int> perm(d.Nx);
+    make_fft_perm(p.plan_nx, perm.data());
+    UP(t.tw_nx, tw.data(), d.Nx);
+    UP(t.perm_nx, perm.data(), d.Nx);
+  }
   if (p.fast_dct) {
     const int L = d.Nz;
     std::vector<double2> tw(L), cs(L + 1);
@@ -318,6 +333,14 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
       UP(t.eta_phys_f, v.data(), v.size());
       std::vector<float2> e = c32(eta);
       UP(t.eta_f, e.data(), e.size());
+      if (g->eta_x_phys && g->eta_y_phys) {  // FP32 products carry u . grad(eta)
+        std::vector<double> gx(g->eta_x_phys, g->eta_x_phys + nh2), gy(g->eta_y_phys, g->eta_y_phys + nh2);
+        for (double& x : gx) x *= hscale;
+        for (double& x : gy) x *= hscale;
+        std::vector<float> fx = f32(gx.data(), nh2), fy = f32(gy.data(), nh2);
+        UP(t.eta_x_f, fx.data(), fx.size());
+        UP(t.eta_y_f, fy.data(), fy.size());
+      }
     }
   }
 
@@ -344,6 +367,7 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.cc, g->cc_weights, (size_t)P);
     if (dalloc(c, &c->diag_part, (size_t)diag_blocks(p) * kDiagTerms) != cudaSuccess)
       return fail(NHQG_ERR_CUDA);
+    if (dalloc(c, &c->diag_max, (size_t)kDiagMaxima) != cudaSuccess) return fail(NHQG_ERR_CUDA);
   }
   {
     CSR a = to_csr(g->cgl_to_sbp, P), b = to_csr(g->sbp_to_cgl, P);
@@ -371,6 +395,30 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     }
     UP(t.bcF, F.data(), F.size());
     UP(t.bcV, bv.data(), bv.size());
+    // 1-D corrector maps as single dense rows, applied by many CTAs at once:
+    // c2sV = c2s V (predictor th_bar coefficients -> SBP grid) and
+    // tauVinv = P_tau V^-1 (CGL values -> coefficients with the Dirichlet tau
+    // projection of rows N-1, N)
+    std::vector<double> c2sV((size_t)P * P, 0.0), tauVinv((size_t)P * P, 0.0);
+    for (int i = 0; i < P; ++i)
+      for (int kk = 0; kk < P; ++kk) {
+        const double a = g->cgl_to_sbp[(size_t)i * P + kk];
+        if (a == 0.0) continue;
+        for (int j = 0; j < P; ++j) c2sV[(size_t)i * P + j] += a * g->V[(size_t)kk * P + j];
+      }
+    for (int i = 0; i < P; ++i) {
+      if (i < N - 1) {
+        for (int j = 0; j < P; ++j) tauVinv[(size_t)i * P + j] = g->V_inv[(size_t)i * P + j];
+      } else {
+        for (int kk = 0; kk < N - 1; ++kk) {
+          const double a = g->proj_dirichlet[(size_t)i * P + kk];
+          if (a == 0.0) continue;
+          for (int j = 0; j < P; ++j) tauVinv[(size_t)i * P + j] += a * g->V_inv[(size_t)kk * P + j];
+        }
+      }
+    }
+    UP(t.c2sV, c2sV.data(), c2sV.size());
+    UP(t.tauVinv, tauVinv.data(), tauVinv.size());
     // fused substep tables: R = c2s s2c, Fs_j = s2c^T F_j, u_j = c2s bcV_j
     const double* c2s = g->cgl_to_sbp;
     const double* s2c = g->sbp_to_cgl;
@@ -616,6 +664,7 @@ int nhqg_set_precision(nhqg_ctx* c, int precision) {
   if (!p.fast_dct || !c->t.tw_v_f || !c->t.tau_tab) return NHQG_ERR_UNSUPPORTED;
   if (p.closure == NHQG_CLOSURE_EVOLVE_MEAN && p.exchange == NHQG_EXCHANGE_LEGACY)
     return NHQG_ERR_UNSUPPORTED;
+  if (p.has_eta && !c->t.eta_x_f) return NHQG_ERR_UNSUPPORTED;  // no eta gradient tables
   if (!c->Qf) {
     const size_t fe = (size_t)p.d.P * p.d.M;
     float2** bufs[] = {&c->Qf, &c->Wf, &c->Tf, &c->Aqf, &c->Awf, &c->Atf};
@@ -1129,7 +1178,13 @@ int nhqg_diagnostics(nhqg_ctx* c, const nhqg_state* s, double* out, void* stream
   } else {
     CK(launch_parseval(p, c->Wn, c->Tn, p.d.P, c->flux, c->w, st));
   }
-  CK(launch_diag_final(p, c->t, c->diag_part, c->flux, sbp, c->tb0, out, st));
+  if (p.plan_nx.npass > 0) {
+    CK(launch_phys_maxima(p, c->t, c->w, c->Qn, c->Wn, c->Tn, c->diag_max, st));
+    c->launches += 3;
+  } else {
+    CK(cudaMemsetAsync(c->diag_max, 0xff, kDiagMaxima * sizeof(unsigned long long), st));  // NaN
+  }
+  CK(launch_diag_final(p, c->t, c->diag_part, c->flux, sbp, c->tb0, c->diag_max, out, st));
   c->launches += sbp ? 5 : 4;
   return NHQG_OK;
 }
@@ -1140,13 +1195,14 @@ int nhqg_spectra(nhqg_ctx* c, const nhqg_state* s, const int* mode_bin, int n_bi
   if (!c->t.cc) return NHQG_ERR_UNSUPPORTED;
   cudaStream_t st = S(stream);
   c->launches = 0;
-  if (!c->spec_mode && dalloc(c, &c->spec_mode, 2 * (size_t)c->p.d.M) != cudaSuccess)
+  if (!c->spec_mode && dalloc(c, &c->spec_mode, 5 * (size_t)c->p.d.M) != cudaSuccess)
     return NHQG_ERR_CUDA;
   int rc = gather_state(c, s, st);
   if (rc) return rc;
   const Params& p = c->p;
-  CK(launch_vfwd(p, c->t, c->q0, nullptr, nullptr, c->Qn, nullptr, nullptr, st));
-  CK(launch_spectra(p, c->t, c->Qn, c->q0, c->w0, c->t0, mode_bin, n_bins, c->spec_mode, out, st));
+  CK(launch_vfwd(p, c->t, c->q0, c->w0, c->t0, c->Qn, c->Wn, c->Tn, st));
+  CK(launch_spectra(p, c->t, c->Qn, c->Wn, c->Tn, c->q0, c->w0, c->t0, mode_bin, n_bins, c->spec_mode,
+                    out, st));
   c->launches += 4;
   return NHQG_OK;
 }

@@ -38,7 +38,6 @@ struct CV {
   __host__ __device__ int flux() const { return P; }
   __host__ __device__ int tb_sbp() const { return 2 * P; }
   __host__ __device__ int g_half() const { return 3 * P; }
-  __host__ __device__ int tmp() const { return 4 * P; }
   __host__ __device__ int tmp2() const { return 5 * P; }
   __host__ __device__ int Aband() const { return 6 * P; }   // 5P: diag offsets -2..2
   __host__ __device__ int Bband() const { return 11 * P; }  // 5P
@@ -55,6 +54,7 @@ struct CK {
   const int *c2s_ptr, *c2s_col, *s2c_ptr, *s2c_col;
   const double *c2s_val, *s2c_val;
   const double *bcF, *bcV, *proj, *D1, *Lsbp;
+  const double *c2sV, *tauVinv;  // fused dense 1-D maps (rows applied by many CTAs)
   double mu, kappa;
 };
 
@@ -68,6 +68,7 @@ CK make_ck(const Params& p, const Tables& t) {
   k.c2s_ptr = t.c2s_ptr; k.c2s_col = t.c2s_col; k.c2s_val = t.c2s_val;
   k.s2c_ptr = t.s2c_ptr; k.s2c_col = t.s2c_col; k.s2c_val = t.s2c_val;
   k.bcF = t.bcF; k.bcV = t.bcV; k.proj = t.proj; k.D1 = t.D1; k.Lsbp = t.Lsbp;
+  k.c2sV = t.c2sV; k.tauVinv = t.tauVinv;
   k.mu = p.eps_sq;
   k.kappa = 1.0 / p.sigma;
   return k;
@@ -97,10 +98,29 @@ __device__ __forceinline__ void tstencil(const CK& k, bool wbasis, C* c, const C
 // transforms carry the state itself and FP32 would be too coarse.  Fields in
 // global memory stay FP64 either way.
 
-// Predictor w and theta to nodal CGL values and to the SBP grid.
+// out[i] = sum_j Mat[i][j] x[j] for the rows i = blockIdx.x, blockIdx.x +
+// gridDim.x, ... < n, one warp per row (lane partial sums over j = lane + 32 q,
+// then a fixed shuffle tree): a dense 1-D map spread over the CTAs of a
+// multi-CTA kernel instead of one SM's FP64 pipe.
+__device__ __forceinline__ void rows_by_ctas(const double* __restrict__ Mat, const double* __restrict__ x,
+                                             double* __restrict__ out, int n) {
+  if (Mat == nullptr || threadIdx.x >= 32) return;
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    const double* row = Mat + (size_t)i * n;
+    double acc = 0.0;
+    for (int j = threadIdx.x; j < n; j += 32) acc = fma(row[j], x[j], acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) out[i] = acc;
+  }
+}
+
+// Predictor w and theta to nodal CGL values and to the SBP grid; the CTAs
+// also form tb_sbp = c2s V tbp (the predictor mean temperature on the SBP grid).
 template <typename C>
 __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const double2* tp,
-                                                 double2* wcgl, double2* wsbp, double2* tsbp) {
+                                                 double2* wcgl, double2* wsbp, double2* tsbp,
+                                                 const double* tbp, double* vec) {
+  rows_by_ctas(k.c2sV, tbp, vec + CV{k.P}.tb_sbp(), k.P);
   extern __shared__ double2 sm_raw[];
   C* sm = reinterpret_cast<C*>(sm_raw);
   const int PT = k.P * TM;
@@ -132,7 +152,10 @@ __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const 
 template <typename C>
 __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const double2* wsbp,
                                                  const double* g_half, double sub_dt, int last,
-                                                 double2* t_out, double2* tcgl) {
+                                                 double2* t_out, double2* tcgl, const double* y_mean,
+                                                 double* tb_out) {
+  // last substep: the corrected mean temperature tb_out = P_tau V^-1 y_mean
+  if (last) rows_by_ctas(k.tauVinv, y_mean, tb_out, k.P);
   using T = typename Prec<C>::T;
   extern __shared__ double2 sm_raw[];
   C* sm = reinterpret_cast<C*>(sm_raw);
@@ -303,10 +326,9 @@ __device__ void d1_matvec(double* out, const double* D1, const double* x, int P)
 // factorisation and the substitutions are serial recurrences, and on this
 // GPU a dependent FP64 operation costs about 14 times a dependent FP32 one
 // (a division about 90 times).  Dynamic shared memory: 10 P doubles.
-__global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt) {
+__device__ __forceinline__ void corr_init_body(const CK& k, double* vec, double sub_dt, double* band_sm) {
   const CV cv{k.P};
   const int P = k.P;
-  extern __shared__ double band_sm[];
   double* w2 = vec + cv.w2();
   double* A = band_sm;
   double* B = band_sm + 5 * P;
@@ -375,11 +397,7 @@ __global__ void k_corr_init(CK k, double* vec, const double* tbp, double sub_dt)
   __syncthreads();
   float* Lg = reinterpret_cast<float*>(vec + cv.lu32());
   for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) Lg[idx] = L[idx];
-  // tb_sbp = c2s (V tbp)
-  double* tmp = vec + cv.tmp();
-  vec_dense(tmp, tbp, k.V, P, P, P);
   __syncthreads();
-  vec_csr(vec + cv.tb_sbp(), tmp, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
 }
 
 // d = (LU)^-1 r with the FP32 factors: rf holds r in FP32 on entry and d on
@@ -449,12 +467,16 @@ __device__ __forceinline__ void lu32_solve(const float* __restrict__ L, float* _
 // 1 / (cond(A) eps_32); kRefine sweeps reach FP64 round-off for the
 // corrector's well-conditioned A = I + (SPD-like) h.  Dynamic shared memory:
 // 5 P doubles (FP64 A band) + 3 P doubles (FP32 factors) + 3 P doubles.
+// With init (the first substep) the kernel first builds and factors the
+// corrector matrices (corr_init_body); its global writes are visible to the
+// rest of the CTA after the barrier that ends the body.
 constexpr int kRefine = 2;
-__global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, double* tb_out) {
+__global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, int init) {
   const CV cv{k.P};
-  const int P = k.P, N = k.N;
+  const int P = k.P;
   __shared__ double red[64];
   extern __shared__ double band_sm[];
+  if (init) corr_init_body(k, vec, sub_dt, band_sm);
   double* flux = vec + cv.flux();
   double* tbs = vec + cv.tb_sbp();
   double* gh = vec + cv.g_half();
@@ -530,21 +552,9 @@ __global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, double*
       rhs[i] = fma(k.bcV[P + i], e1, fma(k.bcV[i], e0, t2[i]));
     __syncthreads();
     vec_csr(tbs, rhs, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
-  } else {
-    vec_dense(rhs, t2, k.Vinv, P, P, P);  // Chebyshev coefficients
-    __syncthreads();
-    // tau projection: keep a_0..a_{N-2}, rewrite a_{N-1}, a_N
-    for (int i = threadIdx.x; i < P; i += blockDim.x) {
-      if (i < N - 1) {
-        tb_out[i] = rhs[i];
-      } else {
-        const double* row = k.proj + (size_t)i * P;
-        double acc = 0.0;
-        for (int j = 0; j < N - 1; ++j) acc = fma(row[j], rhs[j], acc);
-        tb_out[i] = acc;
-      }
-    }
   }
+  // last substep: y = t2 stays in global memory; the last per-mode kernel of
+  // the corrector maps it back to coefficients (k_corr_sub, rows_by_ctas)
 }
 
 // ---- mean-temperature stage update: R = combos; out = solve(R)
@@ -663,18 +673,12 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   }
   Profiler& pf = w.prof;
   pf.begin("corr_pre", st);
-  pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp);
+  pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp, a.tbp, w.vec);
   pf.end(st);
   pf.begin("parseval", st);
-  launch_parseval(p, a.wsbp, a.wsbp, p.d.P, w.vec + cv.w2(), w, st, df);
+  launch_parseval2(p, a.wsbp, a.wsbp, a.tsbp, p.d.P, w.vec + cv.w2(), w.vec + cv.flux(), w, st, df);
   pf.end(st);
-  pf.begin("parseval", st);
-  launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st, df);
-  pf.end(st);
-  pf.begin("corr_init_1d", st);
-  k_corr_init<<<1, NT, 10 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, a.tbp, sub_dt);
-  pf.end(st);
-  int n = 4;
+  int n = 2;
   for (int s = 0; s < nsub; ++s) {
     const int last = (s == nsub - 1);
     if (s > 0) {
@@ -684,7 +688,7 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
       ++n;
     }
     pf.begin("corr_step_1d", st);
-    k_corr_tstep<<<1, NT, 11 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, sub_dt, last, a.tb_out);
+    k_corr_tstep<<<1, NT, 11 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, sub_dt, last, s == 0);
     pf.end(st);
     if (!last && fused_mid) {
       pf.begin("corr_sub_mid", st);
@@ -700,7 +704,7 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
     } else {
       pf.begin(last ? "corr_sub_last" : "corr_sub", st);
       sub<<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt, last, a.t_out,
-                                 a.tcgl);
+                                 a.tcgl, w.vec + cv.tmp2(), a.tb_out);
       pf.end(st);
     }
     n += 2;
@@ -714,7 +718,8 @@ cudaError_t launch_corr_pre(const Params& p, const Tables& t, const double2* w, 
   CK k = make_ck(p, t);
   const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2) + col::dct_smem_bytes(k.dct);
   cudaFuncSetAttribute(k_corr_pre<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  k_corr_pre<double2><<<(p.d.M + TM - 1) / TM, NT, sm2, st>>>(k, w, th, wcgl, wsbp, tsbp);
+  k.c2sV = nullptr;  // no mean-temperature side job here
+  k_corr_pre<double2><<<(p.d.M + TM - 1) / TM, NT, sm2, st>>>(k, w, th, wcgl, wsbp, tsbp, nullptr, nullptr);
   return cudaGetLastError();
 }
 

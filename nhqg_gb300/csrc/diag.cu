@@ -3,7 +3,9 @@
 // |psi|^2, |q|^2, |w|^2, |theta|^2, Re(w theta*) and of the barotropic psi
 // per mode, weighted by the half-plane Parseval weights (1 at ky = 0 and, in
 // the full-band layout of the 3/2 rule, at ky = Nx/2; 2 elsewhere) and normalised by Nx^4.  Spectra: the shell
-// energy spectrum and the vertical mode energies (k_spec_*, k_vspec).
+// energy spectrum, the q / w / theta shell spectra and the vertical mode
+// energies (k_spec_*, k_vspec).  The physical-space maxima come from
+// horizontal.cu (launch_phys_maxima).
 #include "engine.h"
 
 namespace nhqg {
@@ -76,7 +78,8 @@ __global__ void __launch_bounds__(kDiagThreads) k_diag_modes(Dims d, const doubl
 __global__ void k_diag_final(int nblocks, int P, double norm, const double* __restrict__ partials,
                              const double* __restrict__ cc, const double* __restrict__ flux,
                              const double* __restrict__ s2c, bool flux_on_sbp,
-                             const double* __restrict__ th_bar, double* __restrict__ out) {
+                             const double* __restrict__ th_bar,
+                             const unsigned long long* __restrict__ maxima, double* __restrict__ out) {
   __shared__ double tot[kDiagTerms];
   __shared__ double red[32];
   if (threadIdx.x < kDiagTerms) {
@@ -117,52 +120,77 @@ __global__ void k_diag_final(int nblocks, int P, double norm, const double* __re
     out[NHQG_DIAG_W_RMS] = sqrt(w2);
     out[NHQG_DIAG_TH_RMS] = sqrt(t2);
     out[NHQG_DIAG_TH_BAR_MAX] = m;
+    // physical-space maxima (nhqg/diagnostics.py:631-641) and the heat-flux
+    // mismatch between the dealiased and the Parseval volume averages
+    out[NHQG_DIAG_MAX_SPEED] = __longlong_as_double((long long)maxima[0]);
+    out[NHQG_DIAG_MAX_W] = __longlong_as_double((long long)maxima[1]);
+    out[NHQG_DIAG_MAX_THETA] = __longlong_as_double((long long)maxima[2]);
+    out[NHQG_DIAG_MAX_TW] = __longlong_as_double((long long)maxima[3]);
+    out[NHQG_DIAG_HEAT_FLUX_MISMATCH] = voltw_d - wt;
   }
 }
 
-// Shell spectra (nhqg/diagnostics.py:80-101): per compact mode the weighted
+// Shell spectra (nhqg/diagnostics.py:80-111): per compact mode the weighted
 // barotropic and depth-integrated psi energies 0.5 w_k |k|^2 |psi_bt|^2 and
-// 0.5 w_k |k|^2 sum_j cc_j |psi_j|^2 (unnormalised, as the reference sums them)
+// 0.5 w_k |k|^2 sum_j cc_j |psi_j|^2, and the depth-integrated field
+// energies w_k sum_j cc_j |f_j|^2 of q, w, theta at the CGL nodes
+// (unnormalised, as the reference sums them)
 __global__ void __launch_bounds__(kDiagThreads) k_spec_modes(Dims d, const double* __restrict__ cc,
                                                              const double* __restrict__ kx,
                                                              const double* __restrict__ ky,
                                                              const double* __restrict__ inv_denom,
                                                              const double2* __restrict__ qn,
+                                                             const double2* __restrict__ wn,
+                                                             const double2* __restrict__ tn,
                                                              double* __restrict__ per_mode) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= d.M) return;
   const double idn = inv_denom[m];
   double2 pbt = czero();
-  double spsi = 0.0;
+  double spsi = 0.0, sq = 0.0, sw = 0.0, st = 0.0;
   for (int j = 0; j < d.P; ++j) {
-    const double2 psi = cscale(qn[(size_t)j * d.M + m], -idn);
-    pbt = caxpy(cc[j], psi, pbt);
-    spsi = fma(cc[j], fma(psi.x, psi.x, psi.y * psi.y), spsi);
+    const size_t g = (size_t)j * d.M + m;
+    const double2 q = qn[g], w = wn[g], t = tn[g];
+    const double2 psi = cscale(q, -idn);
+    const double c = cc[j];
+    pbt = caxpy(c, psi, pbt);
+    spsi = fma(c, fma(psi.x, psi.x, psi.y * psi.y), spsi);
+    sq = fma(c, fma(q.x, q.x, q.y * q.y), sq);
+    sw = fma(c, fma(w.x, w.x, w.y * w.y), sw);
+    st = fma(c, fma(t.x, t.x, t.y * t.y), st);
   }
   const double wt = hweight(d, m);
   const double ksq = fma(kx[m], kx[m], ky[m] * ky[m]);
   per_mode[m] = 0.5 * wt * ksq * fma(pbt.x, pbt.x, pbt.y * pbt.y);
   per_mode[d.M + m] = 0.5 * wt * ksq * spsi;
+  per_mode[2 * (size_t)d.M + m] = wt * sq;
+  per_mode[3 * (size_t)d.M + m] = wt * sw;
+  per_mode[4 * (size_t)d.M + m] = wt * st;
 }
 
-// one CTA per shell: sum the modes of the shell in a fixed order
+// one CTA per shell: sum the modes of the shell in a fixed order; E_bt, E_bc,
+// E_tot into out[0 .. 3 n_bins), the q, w, theta shell spectra into
+// fout[0 .. 3 n_bins)
 __global__ void k_spec_bins(int M, const int* __restrict__ bin, const double* __restrict__ per_mode,
-                            int n_bins, double* __restrict__ out) {
+                            int n_bins, double* __restrict__ out, double* __restrict__ fout) {
   __shared__ double red[32];
   const int b = blockIdx.x;
-  double eb = 0.0, et = 0.0;
+  double e[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int m = threadIdx.x; m < M; m += blockDim.x)
     if (bin[m] == b) {
-      eb += per_mode[m];
-      et += per_mode[M + m];
+      for (int f = 0; f < 5; ++f) e[f] += per_mode[(size_t)f * M + m];
     }
-  eb = block_sum(eb, red);
-  __syncthreads();
-  et = block_sum(et, red);
+  for (int f = 0; f < 5; ++f) {
+    e[f] = block_sum(e[f], red);
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
-    out[b] = eb;
-    out[n_bins + b] = et - eb;
-    out[2 * n_bins + b] = et;
+    out[b] = e[0];
+    out[n_bins + b] = e[1] - e[0];
+    out[2 * n_bins + b] = e[1];
+    fout[b] = e[2];
+    fout[n_bins + b] = e[3];
+    fout[2 * n_bins + b] = e[4];
   }
 }
 
@@ -198,12 +226,15 @@ __global__ void k_vspec(Dims d, const double2* __restrict__ q, const double2* __
 
 int diag_blocks(const Params& p) { return (p.d.M + kDiagThreads - 1) / kDiagThreads; }
 
-cudaError_t launch_spectra(const Params& p, const Tables& t, const double2* qn, const double2* q,
-                           const double2* w, const double2* th, const int* mode_bin, int n_bins,
-                           double* per_mode, double* out, cudaStream_t st) {
+cudaError_t launch_spectra(const Params& p, const Tables& t, const double2* qn, const double2* wn,
+                           const double2* tn, const double2* q, const double2* w, const double2* th,
+                           const int* mode_bin, int n_bins, double* per_mode, double* out,
+                           cudaStream_t st) {
   if (!t.cc || n_bins <= 0) return cudaErrorInvalidValue;
-  k_spec_modes<<<diag_blocks(p), kDiagThreads, 0, st>>>(p.d, t.cc, t.kx, t.ky, t.inv_denom, qn, per_mode);
-  k_spec_bins<<<n_bins, kDiagThreads, 0, st>>>(p.d.M, mode_bin, per_mode, n_bins, out);
+  k_spec_modes<<<diag_blocks(p), kDiagThreads, 0, st>>>(p.d, t.cc, t.kx, t.ky, t.inv_denom, qn, wn, tn,
+                                                        per_mode);
+  double* fout = out + 3 * (size_t)n_bins + 2 * (size_t)p.d.P + 2 * (size_t)p.d.G;
+  k_spec_bins<<<n_bins, kDiagThreads, 0, st>>>(p.d.M, mode_bin, per_mode, n_bins, out, fout);
   k_vspec<<<dim3(p.d.P, 4), kDiagThreads, 0, st>>>(p.d, q, w, th, t.kx, t.ky, t.inv_denom,
                                                     out + 3 * (size_t)n_bins);
   return cudaGetLastError();
@@ -219,10 +250,10 @@ cudaError_t launch_diag_modes(const Params& p, const Tables& t, const double2* q
 
 cudaError_t launch_diag_final(const Params& p, const Tables& t, const double* partials,
                               const double* flux, bool flux_on_sbp, const double* th_bar,
-                              double* out, cudaStream_t st) {
+                              const unsigned long long* maxima, double* out, cudaStream_t st) {
   const double nx2 = (double)p.d.Nx * (double)p.d.Nx;
   k_diag_final<<<1, 256, 0, st>>>(diag_blocks(p), p.d.P, nx2 * nx2, partials, t.cc, flux, t.s2c_d,
-                                  flux_on_sbp, th_bar, out);
+                                  flux_on_sbp, th_bar, maxima, out);
   return cudaGetLastError();
 }
 

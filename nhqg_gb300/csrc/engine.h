@@ -50,11 +50,19 @@ struct Tables {
   // physical-space fields [Nx*Nx]
   double *sponge = nullptr, *eta_phys = nullptr;
   // FFT over Nx
-  double2* tw = nullptr;  // [Nx]
-  int* perm = nullptr;    // [Nx]
+  double2* tw = nullptr;  // [Nh]
+  int* perm = nullptr;    // [Nh]
+  // FFT over Nx (the physical-space diagnostics; the same tables as tw/perm
+  // unless the 3/2 rule's products run at Npad)
+  double2* tw_nx = nullptr;
+  int* perm_nx = nullptr;
   // FP32 copies for the mixed-precision path (kx_f [Nx], ky_f [Nk] full layout)
   float *kx_f = nullptr, *ky_f = nullptr, *sponge_f = nullptr, *eta_phys_f = nullptr;
   float2 *eta_f = nullptr, *tw_f = nullptr, *tw_v_f = nullptr, *cs_v_f = nullptr;
+  // d eta / dx, d eta / dy on the products' grid (FP32): the mixed path's
+  // products take q itself and add u . grad(eta), which keeps FP32 from
+  // cancelling a small q against the O(1) trap PV
+  float *eta_x_f = nullptr, *eta_y_f = nullptr;
   // FFT over Nz (DCT-I of the vertical columns)
   double2* tw_v = nullptr;  // [Nz]   exp(-2 pi i k / Nz)
   double2* cs_v = nullptr;  // [Nz+1] exp(-i pi j / Nz)
@@ -69,6 +77,8 @@ struct Tables {
   double* s2c_val = nullptr;
   double* bcF = nullptr;    // [2*P] rows N-1, N of (proj_dir - I) V_inv
   double* bcV = nullptr;    // [2*P] columns N-1, N of V
+  double* c2sV = nullptr;     // [P*P] cgl_to_sbp V (th_bar coefficients -> SBP grid)
+  double* tauVinv = nullptr;  // [P*P] P_tau V^-1 (CGL values -> tau-projected coefficients)
   // fused SBP2 substep: R = c2s s2c (rw nonzeros per row, padded), Fs =
   // s2c^T bcF (2 rows), u = c2s bcV (2 columns)
   int* R_col = nullptr;     // [P*rw]
@@ -104,6 +114,7 @@ struct Params {
   Dims d;
   FftPlan plan;
   FftPlan plan_v;  // length Nz (DCT-I); npass <= 0 -> dense vertical transforms
+  FftPlan plan_nx; // length Nx (physical-space diagnostics)
   bool fast_dct;
   int advection, closure, exchange, wbc, substeps;
   double dt, gamma_imex, Ra_sigma, sigma, beta, eps_sq;
@@ -195,6 +206,8 @@ struct HTables {
   const T *sponge, *eta_phys;  // [Nx*Nx] or null
   const C* tw;                 // [Nx]
   const int* perm;             // [Nx]
+  // gradient form of the trap PV (FP32 products): d eta/dx, d eta/dy or null
+  const T *eta_x = nullptr, *eta_y = nullptr;
 };
 
 template <typename C, typename CI>
@@ -334,6 +347,10 @@ cudaError_t launch_finalize(const Params& p, const double2* q, const double2* w,
 cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
                             double* out, Work& w, cudaStream_t st, bool df = false);
 size_t parseval_partials(int levels);
+// <a b> and <a c> per level in one pass over a
+cudaError_t launch_parseval2(const Params& p, const double2* a, const double2* b, const double2* c,
+                             int levels, double* out_ab, double* out_ac, Work& w, cudaStream_t st,
+                             bool df = false);
 cudaError_t launch_hermitian(const Params& p, double2* q, double2* w, double2* th, cudaStream_t st);
 cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStream_t st);
 
@@ -370,16 +387,25 @@ cudaError_t launch_corr_pre(const Params& p, const Tables& t, const double2* w, 
 // diagnostics: per-block partial sums over modes of the depth integrals
 // (kDiagTerms doubles per block), then one CTA for the scalars
 constexpr int kDiagTerms = 7;
+constexpr int kDiagMaxima = 4;  // max |u|, |w|, |theta|, |w theta| over the CGL nodes
 int diag_blocks(const Params& p);
 cudaError_t launch_diag_modes(const Params& p, const Tables& t, const double2* qn, const double2* wn,
                               const double2* tn, double* partials, cudaStream_t st);
 cudaError_t launch_diag_final(const Params& p, const Tables& t, const double* partials,
                               const double* flux, bool flux_on_sbp, const double* th_bar,
-                              double* out, cudaStream_t st);
-// shell energy spectrum (3 n_bins) then vertical spectra (P, G, G, P) into out;
-// qn: FP64 nodal q; per_mode: 2 M doubles of scratch
-cudaError_t launch_spectra(const Params& p, const Tables& t, const double2* qn, const double2* q,
-                           const double2* w, const double2* th, const int* mode_bin, int n_bins,
-                           double* per_mode, double* out, cudaStream_t st);
+                              const unsigned long long* maxima, double* out, cudaStream_t st);
+// physical-space maxima over the Nx grid at every CGL level of the FP64
+// nodal compact fields (q, w, theta): max sqrt(u^2+v^2), |w|, |theta|,
+// |w theta| as bit patterns of non-negative doubles in maxima[0..3]
+cudaError_t launch_phys_maxima(const Params& p, const Tables& t, Work& w, const double2* qn,
+                               const double2* wn, const double2* tn, unsigned long long* maxima,
+                               cudaStream_t st);
+// shell energy spectrum (3 n_bins), vertical spectra (P, G, G, P), then the
+// shell spectra of q, w, theta (3 n_bins) into out; qn, wn, tn: FP64 nodal
+// fields; per_mode: 5 M doubles of scratch
+cudaError_t launch_spectra(const Params& p, const Tables& t, const double2* qn, const double2* wn,
+                           const double2* tn, const double2* q, const double2* w, const double2* th,
+                           const int* mode_bin, int n_bins, double* per_mode, double* out,
+                           cudaStream_t st);
 
 }  // namespace nhqg

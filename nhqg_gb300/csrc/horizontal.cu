@@ -22,6 +22,8 @@
 //       i kx G + H, keep the in-band kx rows.
 // Scaling: numpy's irfft2 carries 1/N^2, folded into H1's input spectra
 // together with the truncation's (N/Nx)^2.
+#include <algorithm>
+
 #include "engine.h"
 
 namespace nhqg {
@@ -40,6 +42,10 @@ struct HK {
   bool full_in, full_out;
   int form, nf1, nprod, ng;
   bool sponge, eta, psi_derived;
+  // FP32 products: q enters without eta and the trap term is u . grad(eta)
+  // from the tables eta_x, eta_y (added to the q sponge slot's product)
+  bool eta_grad;
+  const T *eta_x, *eta_y;
   T scale;  // 1/(N Nx)
   FftPlan plan;
   const CI *psi, *q, *w, *th;
@@ -120,7 +126,7 @@ __global__ void __launch_bounds__(256) k_h1(HK<C, CI> k, int CB) {
     } else {
       psi = to_c<C>(k.psi[off]);
     }
-    if (k.eta) qv = gadd(qv, k.eta_c[r * k.Mc + c]);
+    if (k.eta && !k.eta_grad) qv = gadd(qv, k.eta_c[r * k.Mc + c]);
     const C wv = to_c<C>(k.w[off]), tv = to_c<C>(k.th[off]);
     if (k.form == HF_FLUX) {
       // u = -i ky psi, v = i kx psi
@@ -201,14 +207,20 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
     const int xa = x0 + 2 * p;
     const C* s = in + (size_t)p * k.sx + fft_pad<PS>(y);
     C* o = pr + (size_t)p * k.sx + fft_pad<PS>(y);
-    T sa = 0, sb = 0, ea = 0, eb = 0;
+    T sa = 0, sb = 0, ea = 0, eb = 0, gxa = 0, gxb = 0, gya = 0, gyb = 0;
     if (k.sponge) {
       sa = k.sponge_phys[(size_t)xa * k.N + y];
       sb = k.sponge_phys[(size_t)(xa + 1) * k.N + y];
-      if (k.eta) {
+      if (k.eta && !k.eta_grad) {
         ea = k.eta_phys[(size_t)xa * k.N + y];
         eb = k.eta_phys[(size_t)(xa + 1) * k.N + y];
       }
+    }
+    if (k.eta_grad) {
+      gxa = k.eta_x[(size_t)xa * k.N + y];
+      gxb = k.eta_x[(size_t)(xa + 1) * k.N + y];
+      gya = k.eta_y[(size_t)xa * k.N + y];
+      gyb = k.eta_y[(size_t)(xa + 1) * k.N + y];
     }
     if (k.form == HF_FLUX) {
       const C u = s[0], v = s[fs], Q = s[2 * fs], W = s[3 * fs], Th = s[4 * fs];
@@ -218,8 +230,14 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
       o[3 * fs] = gmk<C>(v.x * W.x, v.y * W.y);
       o[4 * fs] = gmk<C>(u.x * Th.x, u.y * Th.y);
       o[5 * fs] = gmk<C>(v.x * Th.x, v.y * Th.y);
-      if (k.sponge) {
-        o[6 * fs] = gmk<C>(sa * (Q.x - ea), sb * (Q.y - eb));
+      if (k.sponge || k.eta_grad) {
+        // sigma (q - eta), or with the gradient form sigma q + u . grad(eta)
+        T qa = sa * (Q.x - ea), qb = sb * (Q.y - eb);
+        if (k.eta_grad) {
+          qa = fma(u.x, gxa, fma(v.x, gya, qa));
+          qb = fma(u.y, gxb, fma(v.y, gyb, qb));
+        }
+        o[6 * fs] = gmk<C>(qa, qb);
         o[7 * fs] = gmk<C>(sa * W.x, sb * W.y);
         o[8 * fs] = gmk<C>(sa * Th.x, sb * Th.y);
       }
@@ -235,6 +253,10 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
           const T Fb = (f == 0) ? F.y - eb : F.y;
           ja = fma(sa, Fa, ja);
           jb = fma(sb, Fb, jb);
+        }
+        if (f == 0 && k.eta_grad) {  // J[psi, eta] = psi_x eta_y - psi_y eta_x
+          ja = fma(px.x, gya, fma(-py.x, gxa, ja));
+          jb = fma(px.y, gyb, fma(-py.y, gxb, jb));
         }
         o[f * fs] = gmk<C>(ja, jb);
       }
@@ -269,7 +291,7 @@ __global__ void __launch_bounds__(256) k_h2(HK<C, CI> k, int RB) {
         const T ky = k.ky_full[c];
         Ra = gmk<C>(-ky * Va.y, ky * Va.x);
         Rb = gmk<C>(-ky * Vb.y, ky * Vb.x);
-        if (k.sponge) {
+        if (k.sponge || k.eta_grad) {
           C Sa, Sb;
           split(6 + f, Sa, Sb);
           Ra = gadd(Ra, Sa);
@@ -330,6 +352,67 @@ __global__ void __launch_bounds__(256) k_h3(HK<C, CI> k, int CB) {
   }
 }
 
+// ---------------------------------------------------------------- physical maxima
+// Row inverse transforms of H1's u, v, w, theta spectra (fields 0, 1, 3, 4 of
+// the flux form), then per CTA the maxima of sqrt(u^2 + v^2), |w|, |theta|,
+// |w theta| over its rows, merged with atomicMax on the bit patterns (the
+// order of non-negative doubles).  FP64 (the reference's diagnostics).
+__global__ void __launch_bounds__(256) k_hmax(HK<double2, double2> k, int RB,
+                                              unsigned long long* __restrict__ maxima) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2* tw_s = reinterpret_cast<double2*>(smem_raw);
+  int* perm_s = reinterpret_cast<int*>(tw_s + k.N);
+  double2* in = reinterpret_cast<double2*>(perm_s + ((k.N + 3) / 4) * 4);
+  __shared__ double red[4][8];
+  const int NPR = RB / 2;
+  const int lev = blockIdx.y;
+  const int x0 = blockIdx.x * RB;
+  load_tables(k, tw_s, perm_s);
+  for (int i = threadIdx.x; i < 4 * NPR * k.N; i += blockDim.x) in[i] = make_double2(0.0, 0.0);
+  __syncthreads();
+  const int half = k.N / 2;
+  const int src[4] = {0, 1, 3, 4};
+  for (int i = threadIdx.x; i < 4 * NPR * k.cols_in; i += blockDim.x) {
+    const int c = i % k.cols_in;
+    const int rest = i / k.cols_in;
+    const int p = rest % NPR, f = rest / NPR;
+    const int xa = x0 + 2 * p;
+    const size_t base = xidx(k, src[f], lev, xa >> 1, c, k.cols_in);
+    const double2 A = k.x1[base], B = k.x1[base + 1];
+    double2* sq = in + ((size_t)f * NPR + p) * k.N;
+    if (c == 0 || c == half) {
+      sq[perm_s[c]] = make_double2(A.x, B.x);
+    } else {
+      sq[perm_s[c]] = make_double2(A.x - B.y, A.y + B.x);
+      sq[perm_s[k.N - c]] = make_double2(A.x + B.y, B.x - A.y);
+    }
+  }
+  __syncthreads();
+  fft_dit_inv<double2, 0>(in, 4 * NPR, k.N, k.plan, tw_s);
+  double mu = 0.0, mw = 0.0, mt = 0.0, mwt = 0.0;
+  const size_t fs = (size_t)NPR * k.N;
+  for (int i = threadIdx.x; i < NPR * k.N; i += blockDim.x) {
+    const double2 u = in[i], v = in[fs + i], w = in[2 * fs + i], t = in[3 * fs + i];
+    mu = fmax(mu, fmax(sqrt(fma(u.x, u.x, v.x * v.x)), sqrt(fma(u.y, u.y, v.y * v.y))));
+    mw = fmax(mw, fmax(fabs(w.x), fabs(w.y)));
+    mt = fmax(mt, fmax(fabs(t.x), fabs(t.y)));
+    mwt = fmax(mwt, fmax(fabs(w.x * t.x), fabs(w.y * t.y)));
+  }
+  double m4[4] = {mu, mw, mt, mwt};
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int q = 0; q < 4; ++q) {
+    double x = m4[q];
+    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_down_sync(0xffffffffu, x, o));
+    if (lane == 0) red[q][wid] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double x = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) x = fmax(x, red[threadIdx.x][q]);
+    atomicMax(maxima + threadIdx.x, (unsigned long long)__double_as_longlong(x));
+  }
+}
+
 template <typename C>
 size_t table_bytes(int Nx) { return (size_t)Nx * sizeof(C) + (size_t)((Nx + 3) / 4) * 4 * sizeof(int); }
 
@@ -350,8 +433,11 @@ cudaError_t launch_horizontal_t(const Params& p, const HTables<C>& t, Work& w, c
   k.form = a.form;
   k.sponge = a.sponge || a.form == HF_SPONGE;
   k.eta = a.eta;
+  k.eta_grad = a.eta && t.eta_x != nullptr && t.eta_y != nullptr;
+  k.eta_x = t.eta_x;
+  k.eta_y = t.eta_y;
   k.psi_derived = a.psi_derived;
-  if (a.form == HF_FLUX) { k.nf1 = 5; k.nprod = k.sponge ? 9 : 6; k.ng = 6; }
+  if (a.form == HF_FLUX) { k.nf1 = 5; k.nprod = (k.sponge || k.eta_grad) ? 9 : 6; k.ng = 6; }
   else if (a.form == HF_JAC) { k.nf1 = k.sponge ? 11 : 8; k.nprod = 3; k.ng = 3; }
   else { k.nf1 = 1; k.nprod = 1; k.ng = 1; }
   k.scale = (T)(1.0 / ((double)d.Nh * (double)d.Nx));
@@ -421,12 +507,66 @@ cudaError_t launch_horizontal(const Params& p, const Tables& t, Work& w, const H
   return launch_horizontal_t<double2, double2>(p, ht, w, at, st, nlaunch);
 }
 
+cudaError_t launch_phys_maxima(const Params& p0, const Tables& t, Work& w, const double2* qn,
+                               const double2* wn, const double2* tn, unsigned long long* maxima,
+                               cudaStream_t st) {
+  // the context's products may run at Npad (3/2 rule): transforms of length Nx here
+  Params p = p0;
+  p.d.Nh = p.d.Nx;
+  p.plan = p0.plan_nx;
+  if (p.plan.npass <= 0) return cudaErrorInvalidValue;
+  HTables<double2> ht{t.kx_full, t.ky_full, t.inv_denom, nullptr, nullptr, nullptr, t.tw_nx, t.perm_nx};
+  HK<double2, double2> k{};
+  const Dims& d = p.d;
+  k.Nx = d.Nx; k.Nk = d.Nk; k.K = d.K; k.Mr = d.Mr; k.Mc = d.Mc; k.M = d.M;
+  k.N = d.Nx;
+  k.sx = k.N;
+  k.levels = d.P;
+  k.full_in = false;
+  k.full_out = false;
+  k.rows_in = d.Mr;
+  k.cols_in = d.Mc;
+  k.form = HF_FLUX;
+  k.sponge = false; k.eta = false; k.psi_derived = true;
+  k.nf1 = 5; k.nprod = 6; k.ng = 6;
+  k.scale = 1.0 / ((double)d.Nx * (double)d.Nx);
+  k.plan = p.plan;
+  k.psi = nullptr; k.q = qn; k.w = wn; k.th = tn;
+  k.kx_full = ht.kx_full; k.ky_full = ht.ky_full; k.inv_denom = ht.inv_denom;
+  k.eta_c = nullptr; k.sponge_phys = nullptr; k.eta_phys = nullptr;
+  k.tw = ht.tw; k.perm = ht.perm;
+  k.Aq = k.Aw = k.Ath = nullptr;
+  if ((size_t)k.nf1 * d.P * k.cols_in * k.N > w.x1_elems) return cudaErrorInvalidValue;
+  k.x1 = w.x1;
+  k.x2 = nullptr;
+  cudaError_t e = cudaMemsetAsync(maxima, 0, kDiagMaxima * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  const size_t tb = table_bytes<double2>(k.N);
+  const size_t seqb = (size_t)k.N * sizeof(double2);
+  const size_t budget = 200 * 1024;
+  int CB1 = (int)((size_t)96 * 1024 / ((size_t)k.nf1 * seqb));
+  CB1 = std::max(1, std::min(CB1, k.cols_in));
+  const size_t sm1 = tb + (size_t)k.nf1 * CB1 * seqb;
+  int RB = 2;
+  while (RB * 2 <= 16 && k.N % (RB * 2) == 0 && tb + (size_t)4 * (RB * 2 / 2) * seqb <= 96 * 1024) RB *= 2;
+  const size_t sm2 = tb + (size_t)4 * (RB / 2) * seqb;
+  if (sm1 > budget || sm2 > budget) return cudaErrorInvalidConfiguration;
+  cudaFuncSetAttribute(k_h1<double2, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
+  cudaFuncSetAttribute(k_hmax, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget);
+  w.prof.begin("diag_maxima", st);
+  k_h1<double2, double2><<<dim3((k.cols_in + CB1 - 1) / CB1, k.levels), 256, sm1, st>>>(k, CB1);
+  k_hmax<<<dim3(k.N / RB, k.levels), 256, sm2, st>>>(k, RB, maxima);
+  w.prof.end(st);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_horizontal_f32(const Params& p, const Tables& t, Work& w,
                                   const HorizArgsT<float2, float2>& a, cudaStream_t st,
                                   int* nlaunch) {
   if (p.reg_fft && !p.d.pad && horizontal_reg_supported(p.d.Nh))
     return launch_horizontal_f32_reg(p, t, w, a, st, nlaunch);
-  HTables<float2> ht{t.kx_f, t.ky_f, t.inv_denom, t.eta_f, t.sponge_f, t.eta_phys_f, t.tw_f, t.perm};
+  HTables<float2> ht{t.kx_f, t.ky_f, t.inv_denom, t.eta_f, t.sponge_f, t.eta_phys_f, t.tw_f, t.perm,
+                     t.eta_x_f, t.eta_y_f};
   return launch_horizontal_t<float2, float2>(p, ht, w, a, st, nlaunch);
 }
 

@@ -195,13 +195,25 @@ struct HR {
   const double* inv_denom;
   const float2* eta_c;
   const float *sponge_phys, *eta_phys;
+  // gradient form of the trap PV: q enters the products without eta and the
+  // trap term is u . grad(eta) (flux) or J[psi, eta] (Jacobian), from these
+  // tables; FP32 would otherwise cancel a small q against the O(1) eta
+  bool eta_grad;
+  const float *eta_x, *eta_y;
   const float2* tw;  // exp(-2 pi i k / N), k < N
   float2 *x1, *x2;
   float2 *Aq, *Aw, *Ath;
 };
 
+// H1 -> H2 intermediate, pair-major [f][lev][x/2][c][x%2]: H2 reads the row
+// pair of a column as one 16-byte value, contiguous across the columns
 __device__ __forceinline__ size_t xi(const HR& k, int f, int lev, int pair, int c, int cols) {
   return ((((size_t)f * k.levels + lev) * (k.N / 2) + pair) * cols + c) * 2;
+}
+// H2 -> H3 intermediate, column-major [g][lev][c][x]: H3's column loads are
+// contiguous along x; H2 stores a row pair's two values as one 16-byte value
+__device__ __forceinline__ size_t xo(const HR& k, int g, int lev, int c, int x) {
+  return (((size_t)g * k.levels + lev) * k.Mc + c) * k.N + x;
 }
 
 // twiddle table of the lane transforms: tw_s[a S + l] = conj(tw[a l mod N])
@@ -253,80 +265,89 @@ __global__ void __launch_bounds__(128) k_h1r(HR k) {
   const int c0 = blockIdx.x * CB;
   const int ncb = min(CB, k.cols_in - c0);
   load_lane_twiddles<R1, R2>(k, tw_s);
-  // stage the raw fields: 0 psi (read or derived), 1 q (+eta), 2 w, 3 theta
-  const int nraw = (k.form == HF_SPONGE) ? 1 : 4;
+  // raw fields: 0 psi (read or derived), 1 q (+eta), 2 w, 3 theta; staged two
+  // at a time (phase 0: psi, q; phase 1: w, theta) so that the tile stays
+  // small enough for five CTAs per SM
+  const int nphase = (k.form == HF_SPONGE) ? 1 : 2;
   const size_t plane = (size_t)k.rows_in * k.cols_in;
-  for (int i = threadIdx.x; i < k.rows_in * CB; i += blockDim.x) {
-    const int r = i / CB, cc = i - r * CB, c = c0 + cc;
-    float2 v[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-    if (cc < ncb) {
-      const size_t off = (size_t)lev * plane + (size_t)r * k.cols_in + c;
-      if (k.form == HF_SPONGE) {
-        v[0] = k.q[off];
-      } else {
-        const float2 qv = k.q[off];
-        if (k.psi_derived) {
-          const float s = (float)(-k.inv_denom[r * k.Mc + c]);
-          v[0] = make_float2(qv.x * s, qv.y * s);
-        } else {
-          v[0] = k.psi[off];
-        }
-        v[1] = qv;
-        if (k.eta) v[1] = f2add(v[1], k.eta_c[r * k.Mc + c]);
-        v[2] = k.w[off];
-        v[3] = k.th[off];
-      }
-    }
-    for (int f = 0; f < nraw; ++f) tile[((size_t)f * k.rows_in + r) * TS + cc] = v[f];
-  }
-  __syncthreads();
   const int cc = warp * G + g;
   const int c = c0 + cc;
   const bool live = cc < ncb;
   float2* Tg = T + (size_t)(warp * G + g) * F::TILE;
   const float kys = live ? k.ky_full[c] * k.scale : 0.f;
   const float sc = k.scale;
-  for (int f = 0; f < k.nf1; ++f) {
-    // raw field and derivative of output sequence f
-    int raw, der;  // der: 0 none (scaled), 1 d/dx, 2 d/dy, 3 u = -d/dy
-    if (k.form == HF_FLUX) {
-      const int rf[5] = {0, 0, 1, 2, 3}, dv[5] = {3, 1, 0, 0, 0};
-      raw = rf[f]; der = dv[f];
-    } else if (k.form == HF_JAC) {
-      if (f < 8) { raw = f >> 1; der = (f & 1) ? 2 : 1; }
-      else { raw = f - 7; der = 0; }
-    } else {
-      raw = 0; der = 0;
-    }
-    float2 x[R2];
-    sfor<R2>([&](auto jj) {
-      constexpr int j = decltype(jj)::value;
-      const int kpos = l + R1 * j;
-      const int kf = live ? pos_row(k, kpos) : -1;
-      const int r = k.full_in ? kf : kept_row(k, kf);
-      float2 v = make_float2(0.f, 0.f);
-      if (r >= 0) {
-        const float2 a = tile[((size_t)raw * k.rows_in + r) * TS + cc];
-        if (der == 0) {
-          v = make_float2(a.x * sc, a.y * sc);
-        } else if (der == 2) {  // i ky a
-          v = make_float2(-kys * a.y, kys * a.x);
-        } else if (der == 3) {  // -i ky a
-          v = make_float2(kys * a.y, -kys * a.x);
-        } else {  // i kx a
-          const float kxs = k.kx_full[k.full_in ? r : row_full(k, r)] * sc;
-          v = make_float2(-kxs * a.y, kxs * a.x);
+  for (int phase = 0; phase < nphase; ++phase) {
+    if (phase > 0) __syncthreads();  // the previous phase's reads of the tile are done
+    for (int i = threadIdx.x; i < k.rows_in * CB; i += blockDim.x) {
+      const int r = i / CB, cc2 = i - r * CB, c2 = c0 + cc2;
+      float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
+      if (cc2 < ncb) {
+        const size_t off = (size_t)lev * plane + (size_t)r * k.cols_in + c2;
+        if (k.form == HF_SPONGE) {
+          v0 = k.q[off];
+        } else if (phase == 0) {
+          const float2 qv = k.q[off];
+          if (k.psi_derived) {
+            const float s = (float)(-k.inv_denom[r * k.Mc + c2]);
+            v0 = make_float2(qv.x * s, qv.y * s);
+          } else {
+            v0 = k.psi[off];
+          }
+          v1 = qv;
+          if (k.eta && !k.eta_grad) v1 = f2add(v1, k.eta_c[r * k.Mc + c2]);
+        } else {
+          v0 = k.w[off];
+          v1 = k.th[off];
         }
       }
-      x[j] = v;
-    });
-    F::inv(x, Tg, tw_s, l);
-    if (live) {
-      sfor<R2>([&](auto ee) {
-        constexpr int e = decltype(ee)::value;
-        const int xx = (l + R1 * (e / R1)) + R2 * (e % R1);
-        k.x1[xi(k, f, lev, xx >> 1, c, k.cols_in) + (xx & 1)] = x[e];
+      tile[(size_t)r * TS + cc2] = v0;
+      tile[((size_t)k.rows_in + r) * TS + cc2] = v1;
+    }
+    __syncthreads();
+    for (int f = 0; f < k.nf1; ++f) {
+      // raw field and derivative of output sequence f
+      int raw, der;  // der: 0 none (scaled), 1 d/dx, 2 d/dy, 3 u = -d/dy
+      if (k.form == HF_FLUX) {
+        const int rf[5] = {0, 0, 1, 2, 3}, dv[5] = {3, 1, 0, 0, 0};
+        raw = rf[f]; der = dv[f];
+      } else if (k.form == HF_JAC) {
+        if (f < 8) { raw = f >> 1; der = (f & 1) ? 2 : 1; }
+        else { raw = f - 7; der = 0; }
+      } else {
+        raw = 0; der = 0;
+      }
+      if ((raw >> 1) != phase) continue;
+      const int slot = raw & 1;
+      float2 x[R2];
+      sfor<R2>([&](auto jj) {
+        constexpr int j = decltype(jj)::value;
+        const int kpos = l + R1 * j;
+        const int kf = live ? pos_row(k, kpos) : -1;
+        const int r = k.full_in ? kf : kept_row(k, kf);
+        float2 v = make_float2(0.f, 0.f);
+        if (r >= 0) {
+          const float2 a = tile[((size_t)slot * k.rows_in + r) * TS + cc];
+          if (der == 0) {
+            v = make_float2(a.x * sc, a.y * sc);
+          } else if (der == 2) {  // i ky a
+            v = make_float2(-kys * a.y, kys * a.x);
+          } else if (der == 3) {  // -i ky a
+            v = make_float2(kys * a.y, -kys * a.x);
+          } else {  // i kx a
+            const float kxs = k.kx_full[k.full_in ? r : row_full(k, r)] * sc;
+            v = make_float2(-kxs * a.y, kxs * a.x);
+          }
+        }
+        x[j] = v;
       });
+      F::inv(x, Tg, tw_s, l);
+      if (live) {
+        sfor<R2>([&](auto ee) {
+          constexpr int e = decltype(ee)::value;
+          const int xx = (l + R1 * (e / R1)) + R2 * (e % R1);
+          k.x1[xi(k, f, lev, xx >> 1, c, k.cols_in) + (xx & 1)] = x[e];
+        });
+      }
     }
   }
 }
@@ -398,7 +419,7 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
   };
   auto store = [&](int gout, int c, float2 Ra, float2 Rb) {
     if (live)
-      *reinterpret_cast<float4*>(k.x2 + xi(k, gout, lev, pair, c, k.Mc)) = make_float4(Ra.x, Ra.y, Rb.x, Rb.y);
+      *reinterpret_cast<float4*>(k.x2 + xo(k, gout, lev, c, xa)) = make_float4(Ra.x, Ra.y, Rb.x, Rb.y);
   };
   // sponge and eta at this lane's physical points of rows xa, xa + 1
   auto sig = [&](int e, float& sa, float& sb) {
@@ -410,6 +431,14 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
     const int y = (l + R1 * (e / R1)) + R2 * (e % R1);
     ea = k.eta_phys[(size_t)xa * N + y];
     eb = k.eta_phys[(size_t)(xa + 1) * N + y];
+  };
+  // grad(eta) at this lane's physical points of rows xa, xa + 1
+  auto geta = [&](int e, float& gxa, float& gxb, float& gya, float& gyb) {
+    const int y = (l + R1 * (e / R1)) + R2 * (e % R1);
+    gxa = k.eta_x[(size_t)xa * N + y];
+    gxb = k.eta_x[(size_t)(xa + 1) * N + y];
+    gya = k.eta_y[(size_t)xa * N + y];
+    gyb = k.eta_y[(size_t)(xa + 1) * N + y];
   };
 
   float2 x[R2], y[R2], u[R2];
@@ -429,16 +458,28 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
       });
       F::fwd(y, Tg, tw_s, l);
       split(y, [&](int, int c, float2 Ra, float2 Rb) { store(2 * f, c, Ra, Rb); });
-      // sponge spectrum S = F(sigma (f - eta)), kept in y
+      // extra spectrum S = F(sigma (f - eta)) or, in the gradient form,
+      // F(sigma q + u . grad(eta)) for q; kept in y
+      const bool extra = k.sponge || (f == 0 && k.eta_grad);
       if constexpr (SP) {
-        sfor<R2>([&](auto e) {
-          constexpr int ee = decltype(e)::value;
-          float sa, sb, ea = 0.f, eb = 0.f;
-          sig(ee, sa, sb);
-          if (f == 0 && k.eta) eta(ee, ea, eb);
-          y[ee] = make_float2(sa * (x[ee].x - ea), sb * (x[ee].y - eb));
-        });
-        F::fwd(y, Tg, tw_s, l);
+        if (extra) {
+          sfor<R2>([&](auto e) {
+            constexpr int ee = decltype(e)::value;
+            float sa = 0.f, sb = 0.f, ea = 0.f, eb = 0.f;
+            if (k.sponge) sig(ee, sa, sb);
+            if (f == 0 && k.eta && !k.eta_grad) eta(ee, ea, eb);
+            float2 v = make_float2(sa * (x[ee].x - ea), sb * (x[ee].y - eb));
+            if (f == 0 && k.eta_grad) {
+              float gxa, gxb, gya, gyb;
+              geta(ee, gxa, gxb, gya, gyb);
+              const float2 vv = Vg[ee * R1 + l];
+              v.x = fmaf(u[ee].x, gxa, fmaf(vv.x, gya, v.x));
+              v.y = fmaf(u[ee].y, gxb, fmaf(vv.y, gyb, v.y));
+            }
+            y[ee] = v;
+          });
+          F::fwd(y, Tg, tw_s, l);
+        }
       }
       // H = i ky F(v f) (+ S)
       sfor<R2>([&](auto e) {
@@ -447,7 +488,7 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
         x[ee] = make_float2(v.x * x[ee].x, v.y * x[ee].y);
       });
       F::fwd(x, Tg, tw_s, l);
-      if constexpr (SP) {
+      if (SP && extra) {
         // y's split values at the same (j, c) are needed beside x's: split both
         float2 Sa[R2 / 2 + 1], Sb[R2 / 2 + 1];
         split(y, [&](int j, int, float2 Ra, float2 Rb) {
@@ -495,15 +536,27 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
         y[ee] = make_float2(fmaf(u[ee].x, x[ee].x, y[ee].x), fmaf(u[ee].y, x[ee].y, y[ee].y));
       });
       if constexpr (SP) {
-        load(8 + f, x);
-        F::inv(x, Tg, tw_s, l);
-        sfor<R2>([&](auto e) {
-          constexpr int ee = decltype(e)::value;
-          float sa, sb, ea = 0.f, eb = 0.f;
-          sig(ee, sa, sb);
-          if (f == 0 && k.eta) eta(ee, ea, eb);
-          y[ee] = make_float2(fmaf(sa, x[ee].x - ea, y[ee].x), fmaf(sb, x[ee].y - eb, y[ee].y));
-        });
+        if (k.sponge) {
+          load(8 + f, x);
+          F::inv(x, Tg, tw_s, l);
+          sfor<R2>([&](auto e) {
+            constexpr int ee = decltype(e)::value;
+            float sa, sb, ea = 0.f, eb = 0.f;
+            sig(ee, sa, sb);
+            if (f == 0 && k.eta && !k.eta_grad) eta(ee, ea, eb);
+            y[ee] = make_float2(fmaf(sa, x[ee].x - ea, y[ee].x), fmaf(sb, x[ee].y - eb, y[ee].y));
+          });
+        }
+        if (f == 0 && k.eta_grad) {  // J[psi, eta] = psi_x eta_y - psi_y eta_x
+          sfor<R2>([&](auto e) {
+            constexpr int ee = decltype(e)::value;
+            float gxa, gxb, gya, gyb;
+            geta(ee, gxa, gxb, gya, gyb);
+            const float2 py = Vg[ee * R1 + l];
+            y[ee].x = fmaf(u[ee].x, gya, fmaf(-py.x, gxa, y[ee].x));
+            y[ee].y = fmaf(u[ee].y, gyb, fmaf(-py.y, gxb, y[ee].y));
+          });
+        }
       }
       F::fwd(y, Tg, tw_s, l);
       split(y, [&](int, int c, float2 Ra, float2 Rb) { store(f, c, Ra, Rb); });
@@ -532,7 +585,7 @@ __global__ void __launch_bounds__(128) k_h3r(HR k) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* tw_s = reinterpret_cast<float2*>(smem_raw);
   float2* T = tw_s + R2 * (R1 + 1) + 8;
-  float2* tile = T + 4 * G * F::TILE;  // [out field][Mr][TS]
+  float2* tile = T + 4 * G * F::TILE;  // [Mr][TS]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / R1, l = lane - g * R1;
   const int lev = blockIdx.y;
@@ -550,7 +603,7 @@ __global__ void __launch_bounds__(128) k_h3r(HR k) {
     sfor<R2>([&](auto ee) {
       constexpr int e = decltype(ee)::value;
       const int xx = (l + R1 * (e / R1)) + R2 * (e % R1);
-      x[e] = k.x2[xi(k, gi, lev, xx >> 1, cr, k.Mc) + (xx & 1)];
+      x[e] = k.x2[xo(k, gi, lev, cr, xx)];
     });
   };
   for (int f = 0; f < nout; ++f) {
@@ -571,24 +624,24 @@ __global__ void __launch_bounds__(128) k_h3r(HR k) {
       load(f, x);
       F::fwd(x, Tg, tw_s, l);
     }
-    // kept (2/3-band) rows into the staging tile [f][Mr][TS]
+    // kept (2/3-band) rows into the staging tile [Mr][TS], then stored row
+    // by row (coalesced across the CTA's columns)
+    if (f > 0) __syncthreads();  // the previous field's stores have read the tile
     sfor<R2>([&](auto jj) {
       constexpr int j = decltype(jj)::value;
       const int r = kept_row(k, pos_row(k, l + R1 * j));
-      if (r >= 0 && live) tile[((size_t)f * k.Mr + r) * TS + cc] = x[j];
+      if (r >= 0 && live) tile[(size_t)r * TS + cc] = x[j];
     });
-  }
-  __syncthreads();
-  // coalesced stores of the CTA's columns, row by row
-  for (int i = threadIdx.x; i < nout * k.Mr * CB; i += blockDim.x) {
-    const int cc2 = i % CB, rest = i / CB;
-    const int r = rest % k.Mr, f = rest / k.Mr;
-    if (cc2 >= ncb) continue;
-    const int c2 = c0 + cc2;
-    const size_t oidx = k.full_out ? ((size_t)lev * k.Nx + row_full(k, r)) * k.Nk + c2
-                                   : (size_t)lev * k.M + (size_t)r * k.Mc + c2;
+    __syncthreads();
     float2* out = (f == 0) ? k.Aq : (f == 1 ? k.Aw : k.Ath);
-    out[oidx] = tile[((size_t)f * k.Mr + r) * TS + cc2];
+    for (int i = threadIdx.x; i < k.Mr * CB; i += blockDim.x) {
+      const int cc2 = i % CB, r = i / CB;
+      if (cc2 >= ncb) continue;
+      const int c2 = c0 + cc2;
+      const size_t oidx = k.full_out ? ((size_t)lev * k.Nx + row_full(k, r)) * k.Nk + c2
+                                     : (size_t)lev * k.M + (size_t)r * k.Mc + c2;
+      out[oidx] = tile[(size_t)r * TS + cc2];
+    }
   }
 }
 
@@ -599,17 +652,18 @@ cudaError_t launch_reg(const HR& k, cudaStream_t st, Profiler& prof) {
   constexpr int G = 32 / R1;
   constexpr int CB = 4 * G;
   const size_t head = ((size_t)R2 * (R1 + 1) + 8 + (size_t)4 * G * F::TILE) * sizeof(float2);
-  const int nraw = (k.form == HF_SPONGE) ? 1 : 4;
-  const size_t sm1 = head + (size_t)nraw * k.rows_in * (CB + 1) * sizeof(float2);
+  const size_t sm1 = head + (size_t)2 * k.rows_in * (CB + 1) * sizeof(float2);
   const size_t sm2 = head + (size_t)4 * G * (N + 8) * sizeof(float2);
   const int nout = (k.form == HF_SPONGE) ? 1 : 3;
-  const size_t sm3 = head + (size_t)nout * k.Mr * (CB + 1) * sizeof(float2);
+  const size_t sm3 = head + (size_t)k.Mr * (CB + 1) * sizeof(float2);
   const size_t cap = 200 * 1024;
   if (sm1 > cap || sm2 > cap || sm3 > cap) return cudaErrorInvalidConfiguration;
   cudaFuncSetAttribute(k_h1r<R1, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+  // the SP instantiations carry the sponge and the gradient-form eta terms
+  const bool sp = k.sponge || k.eta_grad;
   auto h2 = k_h2r<R1, R2, HF_SPONGE, true>;
-  if (k.form == HF_FLUX) h2 = k.sponge ? k_h2r<R1, R2, HF_FLUX, true> : k_h2r<R1, R2, HF_FLUX, false>;
-  else if (k.form == HF_JAC) h2 = k.sponge ? k_h2r<R1, R2, HF_JAC, true> : k_h2r<R1, R2, HF_JAC, false>;
+  if (k.form == HF_FLUX) h2 = sp ? k_h2r<R1, R2, HF_FLUX, true> : k_h2r<R1, R2, HF_FLUX, false>;
+  else if (k.form == HF_JAC) h2 = sp ? k_h2r<R1, R2, HF_JAC, true> : k_h2r<R1, R2, HF_JAC, false>;
   cudaFuncSetAttribute(h2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
   cudaFuncSetAttribute(k_h3r<R1, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
   prof.begin("h1_col_ifft_f32", st);
@@ -652,6 +706,8 @@ cudaError_t launch_horizontal_f32_reg(const Params& p, const Tables& t, Work& w,
   k.psi = a.psi; k.q = a.q; k.w = a.w; k.th = a.th;
   k.kx_full = t.kx_f; k.ky_full = t.ky_f; k.inv_denom = t.inv_denom;
   k.eta_c = t.eta_f; k.sponge_phys = t.sponge_f; k.eta_phys = t.eta_phys_f;
+  k.eta_x = t.eta_x_f; k.eta_y = t.eta_y_f;
+  k.eta_grad = k.eta && k.eta_x != nullptr && k.eta_y != nullptr;
   k.tw = t.tw_f;
   k.Aq = a.Aq; k.Aw = a.Aw; k.Ath = a.Ath;
   const size_t need1 = (size_t)k.nf1 * a.levels * k.cols_in * d.Nh;

@@ -692,6 +692,81 @@ __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const
   }
 }
 
+// Two horizontal means in one pass over a: out_ab[l] = <a b>, out_ac[l] =
+// <a c> (the corrector's <w^2> and <w theta>), same weights, order and
+// arithmetic as k_parseval; partials hold two sums per (level, segment).
+template <typename C>
+__global__ void __launch_bounds__(NT) k_parseval2(Dims d, const double2* a, const double2* b,
+                                                  const double2* c, double* out_ab, double* out_ac,
+                                                  double scale, double* partials, unsigned* counters) {
+  using T = typename col::Prec<C>::T;
+  __shared__ double scratch[32];
+  __shared__ bool is_last;
+  const int l = blockIdx.y, seg = blockIdx.x;
+  const double2* al = a + (size_t)l * d.M;
+  const double2* bl = b + (size_t)l * d.M;
+  const double2* cl = c + (size_t)l * d.M;
+  const int chunk = (d.M + kParSeg - 1) / kParSeg;
+  const int m0 = seg * chunk, m1 = min(d.M, m0 + chunk);
+  T br = T(0), bi = T(0), cr = T(0), ci = T(0);
+#pragma unroll 4
+  for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+    const C x = col::Prec<C>::in(al[m]), y = col::Prec<C>::in(bl[m]), z = col::Prec<C>::in(cl[m]);
+    br = fma(x.x, y.x, br);
+    bi = fma(x.y, y.y, bi);
+    cr = fma(x.x, z.x, cr);
+    ci = fma(x.y, z.y, ci);
+  }
+  double ab, ac;
+  if constexpr (std::is_same<C, double2>::value) {
+    ab = 2.0 * (br + bi);
+    ac = 2.0 * (cr + ci);
+  } else {
+    ab = 2.0 * df_to_double(br + bi);
+    ac = 2.0 * df_to_double(cr + ci);
+  }
+  for (int r = threadIdx.x; r < d.Mr; r += blockDim.x) {
+    const int m = r * d.Mc;
+    if (m < m0 || m >= m1) continue;
+    const int rm = mirror_row(r, d.Mr);
+    const double2 x = al[m], xm = al[rm * d.Mc];
+    const double2 y = bl[m], ym = bl[rm * d.Mc];
+    const double2 z = cl[m], zm = cl[rm * d.Mc];
+    const double xy = fma(x.x, y.x, x.y * y.y), xz = fma(x.x, z.x, x.y * z.y);
+    if (rm == r && r != 0) {
+      ab += 0.5 * xy - 2.0 * xy;
+      ac += 0.5 * xz - 2.0 * xz;
+      continue;
+    }
+    const double hx_re = 0.5 * (x.x + xm.x), hx_im = 0.5 * (x.y - xm.y);
+    const double hy_re = 0.5 * (y.x + ym.x), hy_im = 0.5 * (y.y - ym.y);
+    const double hz_re = 0.5 * (z.x + zm.x), hz_im = 0.5 * (z.y - zm.y);
+    ab += fma(hx_re, hy_re, hx_im * hy_im) - 2.0 * xy;
+    ac += fma(hx_re, hz_re, hx_im * hz_im) - 2.0 * xz;
+  }
+  const double tab = block_sum(ab, scratch);
+  __syncthreads();
+  const double tac = block_sum(ac, scratch);
+  if (threadIdx.x == 0) {
+    partials[((size_t)l * kParSeg + seg) * 2] = tab;
+    partials[((size_t)l * kParSeg + seg) * 2 + 1] = tac;
+    __threadfence();
+    is_last = atomicAdd(&counters[l], 1u) == kParSeg - 1;
+  }
+  __syncthreads();
+  if (is_last && threadIdx.x == 0) {
+    __threadfence();
+    double s1 = 0.0, s2 = 0.0;
+    for (int q = 0; q < kParSeg; ++q) {
+      s1 += __ldcg(partials + ((size_t)l * kParSeg + q) * 2);
+      s2 += __ldcg(partials + ((size_t)l * kParSeg + q) * 2 + 1);
+    }
+    out_ab[l] = s1 * scale;
+    out_ac[l] = s2 * scale;
+    counters[l] = 0u;
+  }
+}
+
 __global__ void k_zero_mode0(double2* f, int levels, int M) {
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < levels; l += gridDim.x * blockDim.x)
     f[(size_t)l * M] = czero();
@@ -894,7 +969,17 @@ cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStrea
   return cudaGetLastError();
 }
 
-size_t parseval_partials(int levels) { return (size_t)levels * kParSeg; }
+size_t parseval_partials(int levels) { return 2 * (size_t)levels * kParSeg; }
+
+cudaError_t launch_parseval2(const Params& p, const double2* a, const double2* b, const double2* c,
+                             int levels, double* out_ab, double* out_ac, Work& w, cudaStream_t st,
+                             bool df) {
+  const double n2 = (double)p.d.Nx * (double)p.d.Nx;
+  auto kern = df ? k_parseval2<cdfl> : k_parseval2<double2>;
+  kern<<<dim3(kParSeg, levels), NT, 0, st>>>(p.d, a, b, c, out_ab, out_ac, 1.0 / (n2 * n2), w.partials,
+                                             w.counters);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
                             double* out, Work& w, cudaStream_t st, bool df) {

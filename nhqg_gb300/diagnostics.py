@@ -4,14 +4,17 @@
 rms values and Nusselt numbers of the reference's ``compute_diagnostics``
 (nhqg/diagnostics.py:597-690) under the same keys: KE_bt, KE_bc, KE_tot,
 enstrophy, Nusselt, Nusselt_dealiased, vol_avg_tw, vol_avg_tw_dealiased,
-q_rms, w_rms, th_rms, th_bar_max.  The reference's budget terms are not
-computed.  The reduction runs on the device (``nhqg_diagnostics``); the call
-synchronises to return host floats.
+q_rms, w_rms, th_rms, th_bar_max, the physical-space maxima over the Nx grid
+at every CGL node max_speed, max_w, max_theta, max_tw (:631-641) and
+heat_flux_mismatch.  The reference's budget terms are not computed.  The
+reductions and the transforms to physical space run on the device
+(``nhqg_diagnostics``); the call synchronises to return host floats.
 
 ``spectra(state, grid)`` returns the reference's ``energy_spectrum`` of psi
-(nhqg/diagnostics.py:80-101) and ``vertical_mode_energy`` (:583-585) of q, w
-and theta, plus the psi kinetic energy per Chebyshev index; the sums run on
-the device (``nhqg_spectra``).  ``high_mode_fraction`` (:588-594) and
+(nhqg/diagnostics.py:80-101), the q, w, theta horizontal shell spectra of
+``compute_diagnostics`` (:104-111, 667-669) and ``vertical_mode_energy``
+(:583-585) of q, w and theta, plus the psi kinetic energy per Chebyshev
+index; the sums run on the device (``nhqg_spectra``).  ``high_mode_fraction`` (:588-594) and
 ``tail_fraction`` read a vertical spectrum.
 """
 
@@ -67,10 +70,11 @@ def shell_table(grid: Grid, n_bins: int | None = None):
 
 
 def spectra(state, grid: Grid, n_bins: int | None = None) -> dict:
-    """Shell energy spectrum of psi (k_bins, E_bt, E_bc, E_tot) and vertical
+    """Shell energy spectrum of psi (k_bins, E_bt, E_bc, E_tot), vertical
     spectra (q, w, th: sum of |f_n|^2 over the modes; psi_ke: sum of
-    w_k |k|^2 |psi_n|^2), as host float64 arrays; unnormalised like the
-    reference."""
+    w_k |k|^2 |psi_n|^2) and the horizontal shell spectra of q, w, theta at
+    the CGL nodes (q_shell, w_shell, th_shell), as host float64 arrays;
+    unnormalised like the reference."""
     s = to_device(state)
     k_bins, compact = shell_table(grid, n_bins)
     nb = len(k_bins)
@@ -78,9 +82,11 @@ def spectra(state, grid: Grid, n_bins: int | None = None) -> dict:
     out = engine_for(grid).spectra(*s, bins, nb).cpu().numpy()
     P, G = grid.Nz + 1, grid.Nz - 1
     o = 3 * nb
+    f = o + 2 * P + 2 * G
     return dict(k_bins=k_bins, E_bt=out[:nb], E_bc=out[nb:2 * nb], E_tot=out[2 * nb:o],
                 q=out[o:o + P], w=out[o + P:o + P + G], th=out[o + P + G:o + P + 2 * G],
-                psi_ke=out[o + P + 2 * G:o + 2 * P + 2 * G])
+                psi_ke=out[o + P + 2 * G:f], q_shell=out[f:f + nb], w_shell=out[f + nb:f + 2 * nb],
+                th_shell=out[f + 2 * nb:f + 3 * nb])
 
 
 def high_mode_fraction(spec, frac: float = 0.25) -> float:

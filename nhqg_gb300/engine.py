@@ -82,11 +82,15 @@ class Engine:
             d.eta_hat = ctypes.cast(e.ctypes.data, nat.c_double_p)
             # physical eta on the products' grid, derived from eta_hat so that a
             # replaced eta_hat cannot disagree with it
-            if self.pad32:
-                eta_phys = np.fft.irfft2(_zero_pad(e, g.Nx, g.Npad), s=(g.Npad, g.Npad))
-            else:
-                eta_phys = np.fft.irfft2(e, s=(g.Nx, g.Nx))
-            d.eta_phys = arr("eta_phys", eta_phys)
+            kx = np.asarray(g.kx, dtype=np.float64).reshape(-1)[:, None]
+            ky = np.asarray(g.ky, dtype=np.float64).reshape(-1)[None, :g.Nk]
+            parts = {"eta_phys": e, "eta_x_phys": 1j * kx * e, "eta_y_phys": 1j * ky * e}
+            for name, spec in parts.items():
+                if self.pad32:
+                    phys = np.fft.irfft2(_zero_pad(spec, g.Nx, g.Npad), s=(g.Npad, g.Npad))
+                else:
+                    phys = np.fft.irfft2(spec, s=(g.Nx, g.Nx))
+                setattr(d, name, arr(name, phys))
         sponge = g.sponge_phys_pad if self.pad32 else g.sponge_phys
         if g.sponge_phys is not None and sponge is None:
             raise ValueError("a 3/2-rule grid with a sponge needs sponge_phys_pad")
@@ -233,11 +237,12 @@ class Engine:
         return out
 
     def spectra(self, q, w, th, tb, mode_bin: torch.Tensor, n_bins: int) -> torch.Tensor:
-        """3 n_bins shell energies then the vertical spectra of q, w, theta and
-        the psi kinetic energy, on the device (layout of nhqg_spectra)."""
+        """3 n_bins shell energies, the vertical spectra of q, w, theta and
+        the psi kinetic energy, then the q, w, theta shell spectra (3 n_bins),
+        on the device (layout of nhqg_spectra)."""
         s = self.state_desc(q, w, th, tb)
         P, G = int(q.shape[0]), int(w.shape[0])
-        out = torch.empty(3 * n_bins + 2 * P + 2 * G, dtype=torch.float64, device=q.device)
+        out = torch.empty(6 * n_bins + 2 * P + 2 * G, dtype=torch.float64, device=q.device)
         nat.check(self.lib.nhqg_spectra(self.handle, ctypes.byref(s), ctypes.c_void_p(mode_bin.data_ptr()),
                                         int(n_bins), ctypes.c_void_p(out.data_ptr()), _stream_handle()),
                   "nhqg_spectra")

@@ -247,3 +247,38 @@ def run(grid: Grid, state, n_steps: int, save_interval: int, use_imex: bool = Tr
     if rem:
         step_inplace(s, grid, rem, check=(n_outer == 0), precision=precision)
     return s, snaps
+
+
+def prolong_state(state, grid_from: Grid, grid_to: Grid) -> State:
+    """Spectral prolongation of a state onto a finer grid of the same box
+    (no reference counterpart; used to start a fine run from a state spun up
+    on a coarse grid).  Horizontal modes keep their wavenumbers (fftfreq rows,
+    rfft columns) and are scaled by (Nx_to/Nx_from)^2, the ratio of the
+    unnormalised rfft2 sums; Chebyshev (q', Theta_bar) and Dirichlet-Galerkin
+    (w, theta) coefficients are zero-padded, an exact embedding of the
+    coarse polynomials.  Both grids must have the Dirichlet w basis, the same
+    L, Nx_to >= Nx_from and Nz_to >= Nz_from; the result is sanitized on
+    ``grid_to``."""
+    if grid_to.Nx < grid_from.Nx or grid_to.Nz < grid_from.Nz:
+        raise ValueError("prolong_state: the target grid must be at least as fine")
+    if abs(float(grid_to.L) - float(grid_from.L)) > 1e-12 * float(grid_from.L):
+        raise ValueError("prolong_state: both grids must have the same box size L")
+    if grid_from.w_bc_top != "dirichlet" or grid_to.w_bc_top != "dirichlet":
+        raise ValueError("prolong_state: needs the Dirichlet w basis on both grids")
+    s = to_device(state)
+    n0, n1 = grid_from.Nx, grid_to.Nx
+    h0 = n0 // 2  # coarse rows 0..h0-1 are kx >= 0, rows h0.. negative (Nyquist row kept in place)
+    scale = (n1 / n0) ** 2
+
+    def horiz(f: torch.Tensor, levels: int) -> torch.Tensor:
+        out = torch.zeros((levels, n1, n1 // 2 + 1), dtype=torch.complex128, device="cuda")
+        lv, nk0 = f.shape[0], f.shape[2]
+        out[:lv, :h0, :nk0] = f[:, :h0] * scale
+        out[:lv, n1 - (n0 - h0):, :nk0] = f[:, h0:] * scale
+        return out
+
+    P1, G1 = grid_to.Nz + 1, grid_to.Nz - 1
+    tb = torch.zeros(P1, dtype=torch.float64, device="cuda")
+    tb[:s.th_bar.shape[0]] = s.th_bar
+    fine = State(horiz(s.q_hat, P1), horiz(s.w_hat, G1), horiz(s.th_hat, G1), tb)
+    return sanitize_state(fine, grid_to)

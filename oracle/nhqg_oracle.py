@@ -523,15 +523,26 @@ def sanitize_state(state: OracleState, grid: OracleGrid) -> OracleState:
 # Horizontal products under the 2/3 rule -- nhqg/spectral.py:53-60, 281-358
 # ---------------------------------------------------------------------------
 
+# Test hook, None in every parity check: a function applied to the
+# physical-space factors of the 2/3-rule products before they are multiplied.
+# A test sets it (e.g. to a BF16 rounding) to show that a precision gate on
+# the mixed path would catch products computed at a lower precision.
+PRODUCT_ROUNDING = None
+
+
+def _factor(a):
+    return a if PRODUCT_ROUNDING is None else PRODUCT_ROUNDING(a)
+
+
 def triple_conservative_flux_divergence_23(psi, q, w, th, kx, ky, mask, Nx):
     """div(u f, v f), u=-psi_y, v=psi_x, for f in (q, w, th), every level
     (nhqg/spectral.py:307-328, 346-358)."""
     kx3, ky3 = kx[None], ky[None]
-    u = _irfft2(-1j * ky3 * psi, Nx)
-    v = _irfft2(1j * kx3 * psi, Nx)
+    u = _factor(_irfft2(-1j * ky3 * psi, Nx))
+    v = _factor(_irfft2(1j * kx3 * psi, Nx))
     outs = []
     for f_hat in (q, w, th):
-        f = _irfft2(f_hat, Nx)
+        f = _factor(_irfft2(f_hat, Nx))
         div = 1j * kx3 * _rfft2(u * f) + 1j * ky3 * _rfft2(v * f)
         outs.append(div * mask[None])
     return tuple(outs)

@@ -70,3 +70,24 @@ def test_dominant_roofline_entry():
     assert 0.0 < dom["hbm_view"]["frac"] < 1.0 and dom["frac"] > 0
     other = bench.dominant_roofline(prof, roof, (128, 256, "23_rule"), peaks)
     assert other["traffic"] is None and "hbm_view" not in other
+
+
+def test_reference_arm_polar_json():
+    """The reference arm of the polar-trap configuration: whole oracle steps
+    at 256^2 x 32 with the trap, the sponge and the open top."""
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--config", "polar",
+                          "--steps", "1", "--warmup", "0"],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["metric"] == bench.POLAR_METRIC and "polar" in line["config"]["workload"]
+    assert line["config"]["Nx"] == 256 and line["config"]["Nz"] == 32
+    assert "whole steps" in line["cpu_baseline"]["sample"]
+
+
+def test_polar_workload_passes_resolution_guards():
+    """The production-scaled trap and sponge pass the eta and sponge
+    resolution guards of make_grid at 256^2 x 32."""
+    g = make_grid(NHQGConfig(**bench.polar_workload()))
+    assert g.eta_hat is not None and g.sponge_phys is not None and g.w_bc_top == "neumann"

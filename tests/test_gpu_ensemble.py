@@ -92,3 +92,44 @@ def test_ensemble_recaptures_on_precision_change():
     for a, b in zip(s0, _host(s)):
         assert np.array_equal(a, b)
     ens.close()
+
+
+def test_ensemble_config4_size_classes():
+    """One member per size class of the 48-instance benchmark ensemble
+    (64^2x32, 96^2x48 with radix-3 transforms, 128^2x64; L = 10 L_c,
+    dt = 5e-5, Ra ~ U(40, 120), production recipe), each in FP64 and mixed
+    precision: 20 ensemble steps equal every member's own single-context
+    run bitwise, and the FP64 members match the oracle to 1e-11 after 5
+    steps."""
+    import sys
+    from pathlib import Path
+
+    import oracle
+    from oracle.nhqg_oracle import OracleConfig, OracleState
+    from nhqg_gb300 import theta_perturbation_state
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+    import bench
+
+    cfgs = bench.ensemble_configs()
+    picks = [cfgs[0], cfgs[16], cfgs[32]]  # first member of each class
+    grids = [make_grid(NHQGConfig(**c)) for c in picks]
+    members = [(i, p) for i in range(3) for p in ("fp64", "mixed")]
+    ens = Ensemble([grids[i] for i, _ in members], precision=[p for _, p in members],
+                   steps_per_launch=10, autotune=False)
+    starts = [theta_perturbation_state(grids[i], seed=7 + i, amplitude=0.1) for i in range(3)]
+    for j, (i, _) in enumerate(members):
+        ens.load(j, starts[i])
+    ens.step(20)
+    for j, (i, prec) in enumerate(members):
+        got = _host(ens.store(j))
+        ref = _single(grids[i], starts[i], 20, prec)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b), (picks[i]["Nx"], prec)
+    ens.close()
+    for i, c in enumerate(picks):
+        o = oracle.make_grid(OracleConfig(**c))
+        os_ = OracleState(*starts[i])
+        for _ in range(5):
+            os_ = oracle.imex_step(os_, o)
+        assert_state_close(_single(grids[i], starts[i], 5, "fp64"), os_, 1e-11, th_bar_abs=1e-18)

@@ -173,3 +173,48 @@ def test_explicit_rhs_fp32_row_products_sizes(nx):
     E64 = _host(S.explicit_rhs(s, g))
     E32 = _host(S.explicit_rhs(s, g, precision="mixed"))
     assert_state_close(E32, E64, 2e-5, th_bar_abs=1e-14)
+
+
+def _bf16(a):
+    """Round float64 values to bfloat16 (round to nearest even on the top 16
+    bits of the float32 pattern)."""
+    f = np.asarray(a, dtype=np.float32)
+    b = f.view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def test_config1_convecting_state_100_steps(monkeypatch):
+    """64^2 x 32 production recipe from a convecting state (seeded theta'
+    of amplitude 1, 4000 mixed steps: t = 0.2, Nu - 1 ~ 4), where the
+    advection term is O(1) of the tendency: 100 mixed steps within 1e-6 of
+    the oracle's FP64 trajectory, 100 plain steps within 1e-9.  The same 100
+    oracle steps with the product factors rounded to BF16 leave the 1e-6
+    band, so the gate sees the precision of the products."""
+    from nhqg_gb300.diagnostics import compute_diagnostics
+    g = make_grid(NHQGConfig(**CFG1))
+    s0 = S.to_device(theta_perturbation_state(g, seed=0, amplitude=1.0))
+    S.step_inplace(s0, g, 4000, check=True, precision="mixed")
+    d = compute_diagnostics(s0, g)
+    assert d["Nusselt"] - 1.0 >= 0.1, d["Nusselt"]
+    E = S.explicit_rhs(s0, g)
+    I = S.implicit_tendency(s0, g)  # noqa: E741
+    share = float(torch.linalg.norm(E.th_hat) / torch.linalg.norm(I.th_hat))
+    assert share > 0.05, share  # the nonlinear term is a visible part of the theta tendency
+    host = S.to_host(s0)
+    o = oracle.make_grid(OracleConfig(**CFG1))
+    ref = OracleState(*host)
+    for _ in range(100):
+        ref = oracle.imex_step(ref, o)
+    mix = S.State(*(t.clone() for t in s0))
+    S.step_inplace(mix, g, 100, check=True, precision="mixed")
+    assert_state_close(_host(mix), ref, 1e-6, th_bar_abs=1e-18)
+    plain = S.State(*(t.clone() for t in s0))
+    S.step_inplace(plain, g, 100, check=True)
+    assert_state_close(_host(plain), ref, 1e-9, th_bar_abs=1e-18)
+    monkeypatch.setattr(oracle.nhqg_oracle, "PRODUCT_ROUNDING", _bf16)
+    bad = OracleState(*host)
+    for _ in range(100):
+        bad = oracle.imex_step(bad, o)
+    worst = max(rel_l2(b, r) for b, r in zip(bad[:3], ref[:3]))
+    assert worst > 1e-6, worst

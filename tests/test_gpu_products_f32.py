@@ -67,3 +67,24 @@ def test_fp32_products_vs_fp64(nx, form, extras):
     E64 = _host(S.explicit_rhs(s, g))
     E32 = _host(S.explicit_rhs(s, g, precision="mixed"))
     assert_state_close(E32, E64, 2e-5, th_bar_abs=1e-14)
+
+
+@pytest.mark.parametrize("nx", [48, 256])
+@pytest.mark.parametrize("form", ["flux", "jacobian"])
+def test_fp32_products_small_q_large_eta(nx, form):
+    """q five orders below an O(1) trap PV with a sponge (the polar
+    configuration's start): the FP32 products take q itself and add the trap
+    term in gradient form, so sigma q and the advection of eta keep their
+    FP32 accuracy instead of cancelling q + eta against eta (Nx = 48 runs the
+    shared-memory FFT kernels, 256 the register ones)."""
+    cfg = dict(Nx=nx, Nz=16, L=10 * L_C, Ra_tilde=100.0, dt=5e-5, nonlinear_advection=form,
+               horizontal_dealiasing="23_rule", float_dtype="float64", thermal_closure="fixed_conduction")
+    g = make_grid(NHQGConfig(**cfg))
+    eta, sigma = _smooth_eta_sponge(g)
+    eta = eta * 1000.0
+    g = g._replace(eta_hat=eta, sponge_phys=sigma, eta_phys=np.fft.irfft2(eta, s=(nx, nx)))
+    s = _state(g, nx + 3)
+    s = S.State(s.q_hat * 1e-5, s.w_hat, s.th_hat, s.th_bar)
+    E64 = _host(S.explicit_rhs(s, g))
+    E32 = _host(S.explicit_rhs(s, g, precision="mixed"))
+    assert_state_close(E32, E64, 2e-5, th_bar_abs=1e-14)

@@ -163,3 +163,32 @@ def test_oracle_spectra_golden(case):
             scale = max(float(np.max(np.abs(ref))), 1e-300)
             assert float(np.max(np.abs(got[key] - ref))) <= 1e-12 * scale, (case, label, key)
         assert 0.0 <= oracle.high_mode_fraction(got["q"]) <= 1.0
+
+
+def test_product_rounding_hook_changes_products():
+    """The oracle's product-rounding test hook is off by default and, set to a
+    BF16 rounding, moves the flux products by far more than 1e-6."""
+    import oracle.nhqg_oracle as O
+    assert O.PRODUCT_ROUNDING is None
+    rng = np.random.default_rng(5)
+    Nx = 16
+    kx = 2 * np.pi * np.fft.fftfreq(Nx, d=1.0 / Nx) / 10.0
+    ky = 2 * np.pi * np.arange(Nx // 2 + 1) / 10.0
+    KX, KY = np.meshgrid(kx, ky, indexing="ij")
+    mask = ((np.abs(np.round(KX * 10 / (2 * np.pi))) <= Nx // 3) &
+            (np.round(KY * 10 / (2 * np.pi)) <= Nx // 3)).astype(float)
+    f = [rng.standard_normal((2, Nx, Nx // 2 + 1)) * mask + 0j for _ in range(4)]
+    ref = O.triple_conservative_flux_divergence_23(*f, KX, KY, mask, Nx)
+
+    def bf16(a):
+        b = np.asarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+        b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+        return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+    try:
+        O.PRODUCT_ROUNDING = bf16
+        bad = O.triple_conservative_flux_divergence_23(*f, KX, KY, mask, Nx)
+    finally:
+        O.PRODUCT_ROUNDING = None
+    for a, b in zip(bad, ref):
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) > 1e-4
