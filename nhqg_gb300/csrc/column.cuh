@@ -235,19 +235,79 @@ __device__ __forceinline__ void warp_parity_scan(int len, bool reverse, Get get,
   }
 }
 
+// Inclusive sums along the two parity classes of every (mode, re/im) column
+// of a tile, run by the whole CTA (blockDim.x == NT, called by every thread;
+// callers synchronise before and after).  Element n < len of mode mm is
+// get(n, mm) (a complex C); put(n, mm, v) receives
+//   v = sum of get(m, mm) over m = n (mod 2), m <= n      (reverse = false)
+//   v = sum of get(m, mm) over m = n (mod 2), m >= n      (reverse = true).
+// Thread t takes level t + NT r of round r and all TM modes, so the tile is
+// read and written row by row (no shared-memory bank conflicts, where a
+// level-strided walk down one column hits one bank); the class scan of a
+// warp runs on shuffles at even offsets, warp totals and the running carry
+// go through shared memory.
+template <typename C, typename Get, typename Put>
+__device__ __forceinline__ void tscan(int len, bool reverse, Get get, Put put) {
+  constexpr int NW = NT / 32;
+  __shared__ double2 red_raw[NW][2][TM];   // warp totals per position class
+  __shared__ double2 pref_raw[NW][2][TM];  // exclusive prefix of the warp totals (+ carry)
+  __shared__ double2 carry_raw[2][TM];     // totals of the previous rounds
+  C (*red)[2][TM] = reinterpret_cast<C (*)[2][TM]>(red_raw);
+  C (*pref)[2][TM] = reinterpret_cast<C (*)[2][TM]>(pref_raw);
+  C (*carry)[TM] = reinterpret_cast<C (*)[TM]>(carry_raw);
+  static_assert(sizeof(C) == sizeof(double2), "16-byte complex tiles");
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t < 2 * TM) carry[t / TM][t % TM] = gzero<C>();
+  for (int r0 = 0; r0 < len; r0 += NT) {
+    const int pos = r0 + t;                        // position along the scan
+    const int n = reverse ? len - 1 - pos : pos;   // level
+    const bool in = pos < len;
+    C v[TM];
+#pragma unroll
+    for (int mm = 0; mm < TM; ++mm) v[mm] = in ? get(n, mm) : gzero<C>();
+    // class scan within the warp: positions of one class are 2 apart
+#pragma unroll
+    for (int o = 2; o < 32; o <<= 1) {
+#pragma unroll
+      for (int mm = 0; mm < TM; ++mm) {
+        C u;
+        u.x = __shfl_up_sync(0xffffffffu, v[mm].x, o);
+        u.y = __shfl_up_sync(0xffffffffu, v[mm].y, o);
+        if (lane >= o) v[mm] = gadd(v[mm], u);
+      }
+    }
+    // lanes 30 and 31 hold the warp's totals of the two position classes
+    if (lane >= 30) {
+#pragma unroll
+      for (int mm = 0; mm < TM; ++mm) red[warp][lane & 1][mm] = v[mm];
+    }
+    __syncthreads();
+    if (t < 2 * TM) {  // exclusive prefix over the warps, and the carry into the next round
+      const int c = t / TM, mm = t % TM;
+      C acc = carry[c][mm];
+      for (int w = 0; w < NW; ++w) {
+        pref[w][c][mm] = acc;
+        acc = gadd(acc, red[w][c][mm]);
+      }
+      carry[c][mm] = acc;
+    }
+    __syncthreads();
+    // position class of this thread (pos parity; r0 is a multiple of NT, even)
+    const int pc = pos & 1;
+    if (in) {
+#pragma unroll
+      for (int mm = 0; mm < TM; ++mm) put(n, mm, gadd(pref[warp][pc][mm], v[mm]));
+    }
+    if (r0 + NT < len) __syncthreads();  // red / pref are rewritten by the next round
+  }
+}
+
 // exact left inverse of the Dirichlet stencil: x_n = x_{n-2} - c_n, i.e.
-// x_n = -(sum of c_i over i <= n, i = n mod 2), n < G.  Needs 2*TM warps.
+// x_n = -(sum of c_i over i <= n, i = n mod 2), n < G.  All threads.
 template <typename C>
 __device__ __forceinline__ void tpinv_dir(C* x, const C* c, int G) {
-  using T = typename Prec<C>::T;
-  const int w = threadIdx.x >> 5;
-  if (w < 2 * TM) {
-    const int mm = w >> 1;
-    const bool im = w & 1;
-    warp_parity_scan(G, false,
-        [&](int n) -> T { return im ? -c[n * TM + mm].y : -c[n * TM + mm].x; },
-        [&](int n, T v) { if (im) x[n * TM + mm].y = v; else x[n * TM + mm].x = v; });
-  }
+  tscan<C>(G, false, [&](int n, int mm) { return gneg(c[n * TM + mm]); },
+           [&](int n, int mm, C v) { x[n * TM + mm] = v; });
 }
 
 // exact left inverse of the open-top stencil: x_n = c_n - a_{n-1} x_{n-1} - b_{n-2} x_{n-2}
@@ -273,34 +333,21 @@ __device__ __forceinline__ void tpinv_mixed(C* x, const C* c, int G,
 }
 // d/dZ on Chebyshev coefficients, G_Z = 2 G_xi (nhqg/grid.py:148-169):
 // b_k = sum_{j > k, j - k odd} 4 j a_j for 1 <= k <= N-1, b_N = 0,
-// b_0 = b_2 / 2 + 2 a_1 -- suffix sums over a parity class.  Needs 2*TM warps.
+// b_0 = b_2 / 2 + 2 a_1 -- suffix sums over a parity class.  All threads.
 template <typename C>
 __device__ __forceinline__ void tgz(C* b, const C* a, int N) {
   using T = typename Prec<C>::T;
-  const int w = threadIdx.x >> 5;
-  if (w < 2 * TM) {
-    const int mm = w >> 1;
-    const bool im = w & 1;
-    // t_j = 4 j a_j for j = 1..N, scanned from the top: U_j = sum_{i>=j, i=j mod 2} t_i
-    // stored as b_{j-1} = U_j (j = 2..N), b_0 fixed up below
-    warp_parity_scan(N, true,
-        [&](int n) -> T {  // n = j - 1 in [0, N-1]
-          const T av = im ? a[(n + 1) * TM + mm].y : a[(n + 1) * TM + mm].x;
-          return Prec<C>::i(4 * (n + 1)) * av;
-        },
-        [&](int n, T v) { if (n >= 1) { if (im) b[n * TM + mm].y = v; else b[n * TM + mm].x = v; } });
-    if ((threadIdx.x & 31) == 0) {
-      if (im) b[N * TM + mm].y = T(0); else b[N * TM + mm].x = T(0);
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < 2 * TM) {
-    const int mm = threadIdx.x >> 1;
-    const bool im = threadIdx.x & 1;
-    const T b2 = N >= 2 ? (im ? b[2 * TM + mm].y : b[2 * TM + mm].x) : T(0);
-    const T a1 = im ? a[TM + mm].y : a[TM + mm].x;
-    const T b0 = fma(T(0.5), b2, T(2.0) * a1);
-    if (im) b[mm].y = b0; else b[mm].x = b0;
+  // t_j = 4 j a_j for j = 1..N, summed from the top over j's class:
+  // U_j = sum_{i >= j, i = j mod 2} t_i, stored as b_{j-1} (n = j - 1 in [1, N-1])
+  tscan<C>(N, true, [&](int n, int mm) { return gscale(a[(n + 1) * TM + mm], Prec<C>::i(4 * (n + 1))); },
+           [&](int n, int mm, C v) { if (n >= 1) b[n * TM + mm] = v; });
+  __syncthreads();  // b_2 comes from another thread
+  if (threadIdx.x < TM) {
+    const int mm = threadIdx.x;
+    b[N * TM + mm] = gzero<C>();
+    const C b2 = N >= 2 ? b[2 * TM + mm] : gzero<C>();
+    const C a1 = a[TM + mm];
+    b[mm] = gmk<C>(fma(T(0.5), b2.x, T(2.0) * a1.x), fma(T(0.5), b2.y, T(2.0) * a1.y));
   }
 }
 
@@ -369,23 +416,26 @@ __device__ __forceinline__ void tdct(C* out, const C* in, const Dct& d, const Dc
     if (inverse && (n == 0 || n == N)) v = gscale(v, half);
     return v;
   };
+  constexpr int PS = 0;
+  const int SX = N;
+  auto W = [&](int mm, int pos) -> C& { return s.work[mm * SX + fft_pad<PS>(pos)]; };
   for (int idx = threadIdx.x; idx < TM * N; idx += blockDim.x) {
     const int mm = idx / N, j = idx - mm * N;
     const C cj = cin(j, mm), cr = cin(N - j, mm);
     const T sn = -s.cs[j].y;  // sin(pi j / N)
     const C sum = gadd(cj, cr), dif = gsub(cj, cr);
-    s.work[idx] = gmk<C>(fma(half, sum.x, -sn * dif.x), fma(half, sum.y, -sn * dif.y));
+    W(mm, j) = gmk<C>(fma(half, sum.x, -sn * dif.x), fma(half, sum.y, -sn * dif.y));
   }
   __syncthreads();
-  fft_dif_fwd(s.work, TM, N, d.plan, s.tw);
+  fft_dif_fwd<C, PS>(s.work, TM, SX, d.plan, s.tw);
   const T sc = inverse ? T(2.0 / N) : T(1);
   // even outputs j = 2k
   for (int idx = threadIdx.x; idx < TM * (N / 2 + 1); idx += blockDim.x) {
     const int k = idx / TM, mm = idx - k * TM;
     const int j = 2 * k;
     if (j >= nout) continue;
-    const C Zk = s.work[mm * N + s.perm[k % N]];
-    const C Zm = s.work[mm * N + s.perm[(N - k) % N]];
+    const C Zk = W(mm, s.perm[k % N]);
+    const C Zm = W(mm, s.perm[(N - k) % N]);
     const C c0 = cin(0, mm), cN = cin(N, mm);
     C y = gscale(gadd(gadd(Zk, Zm), gadd(c0, cN)), half);
     T f = sc;
@@ -406,7 +456,7 @@ __device__ __forceinline__ void tdct(C* out, const C* in, const Dct& d, const Dc
     f1 = fma(half, c0 - cN, f1);
     // D_m (m = 1 .. N/2-1), re part = Im(Z_m - Z_{N-m})/2, im part = -Re(Z_m - Z_{N-m})/2
     auto dm = [&](int m) {
-      const C a = s.work[mm * N + s.perm[m]], b = s.work[mm * N + s.perm[N - m]];
+      const C a = W(mm, s.perm[m]), b = W(mm, s.perm[N - m]);
       return im ? half * (b.x - a.x) : half * (a.y - b.y);
     };
     const int len = N / 2 - 1;

@@ -364,6 +364,10 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
   float2* tw_s = reinterpret_cast<float2*>(smem_raw);
   float2* T = tw_s + R2 * (R1 + 1) + 8;
   float2* Vs = T + 4 * G * F::TILE;
+  // output staging: the CTA's 4 G row pairs = 8 G consecutive x of every kept
+  // column, stored as one contiguous run per column
+  constexpr int OS = 8 * G + 2;  // row stride (complex values) of the staging tile
+  float2* Os = Vs + (size_t)4 * G * (N + 8);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / R1, l = lane - g * R1;
   const int lev = blockIdx.y;
@@ -417,9 +421,20 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
       }
     });
   };
-  auto store = [&](int gout, int c, float2 Ra, float2 Rb) {
-    if (live)
-      *reinterpret_cast<float4*>(k.x2 + xo(k, gout, lev, c, xa)) = make_float4(Ra.x, Ra.y, Rb.x, Rb.y);
+  const int gi = warp * G + g;  // row pair within the CTA
+  const int x0 = 2 * blockIdx.x * 4 * G;
+  const int nx = min(8 * G, N - x0);
+  auto store = [&](int, int c, float2 Ra, float2 Rb) {
+    *reinterpret_cast<float4*>(Os + (size_t)c * OS + 2 * gi) = make_float4(Ra.x, Ra.y, Rb.x, Rb.y);
+  };
+  // after every group has staged output gout: contiguous stores per column
+  auto flush = [&](int gout) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < k.Mc * nx; i += blockDim.x) {
+      const int c = i / nx, xx = i - c * nx;
+      k.x2[xo(k, gout, lev, c, x0 + xx)] = Os[(size_t)c * OS + xx];
+    }
+    __syncthreads();
   };
   // sponge and eta at this lane's physical points of rows xa, xa + 1
   auto sig = [&](int e, float& sa, float& sb) {
@@ -458,6 +473,7 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
       });
       F::fwd(y, Tg, tw_s, l);
       split(y, [&](int, int c, float2 Ra, float2 Rb) { store(2 * f, c, Ra, Rb); });
+      flush(2 * f);
       // extra spectrum S = F(sigma (f - eta)) or, in the gradient form,
       // F(sigma q + u . grad(eta)) for q; kept in y
       const bool extra = k.sponge || (f == 0 && k.eta_grad);
@@ -513,6 +529,7 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
           store(2 * f + 1, c, make_float2(-ky * Va.y, ky * Va.x), make_float2(-ky * Vb.y, ky * Vb.x));
         });
       }
+      flush(2 * f + 1);
     }
   } else if constexpr (FORM == HF_JAC) {
     // J_f = psi_x f_y - psi_y f_x (+ sigma (f - eta)): psi_x in registers, psi_y stored
@@ -560,6 +577,7 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
       }
       F::fwd(y, Tg, tw_s, l);
       split(y, [&](int, int c, float2 Ra, float2 Rb) { store(f, c, Ra, Rb); });
+      flush(f);
     }
   } else {  // sponge-only product
     load(0, x);
@@ -572,6 +590,7 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
     });
     F::fwd(x, Tg, tw_s, l);
     split(x, [&](int, int c, float2 Ra, float2 Rb) { store(0, c, Ra, Rb); });
+    flush(0);
   }
 }
 
@@ -653,7 +672,7 @@ cudaError_t launch_reg(const HR& k, cudaStream_t st, Profiler& prof) {
   constexpr int CB = 4 * G;
   const size_t head = ((size_t)R2 * (R1 + 1) + 8 + (size_t)4 * G * F::TILE) * sizeof(float2);
   const size_t sm1 = head + (size_t)2 * k.rows_in * (CB + 1) * sizeof(float2);
-  const size_t sm2 = head + (size_t)4 * G * (N + 8) * sizeof(float2);
+  const size_t sm2 = head + ((size_t)4 * G * (N + 8) + (size_t)k.Mc * (8 * G + 2)) * sizeof(float2);
   const int nout = (k.form == HF_SPONGE) ? 1 : 3;
   const size_t sm3 = head + (size_t)k.Mr * (CB + 1) * sizeof(float2);
   const size_t cap = 200 * 1024;
