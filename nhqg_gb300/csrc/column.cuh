@@ -44,17 +44,33 @@ struct Dct {
   const double *V, *Vinv;     // dense fallback [P*P]
 };
 
+// FFT sequences of the DCT work area carry one padding element every 2^PS
+// (fft_pad) where the transform is bound by its shared-memory passes: the
+// double-float and FP32 tiles (PS = 2 and 3 for 16- and 8-byte values spread
+// the short-span radix-4 passes over the banks); the FP64 tiles, bound by the
+// FP64 pipe, stay dense.
+template <typename C> __host__ __device__ constexpr int dct_ps() {
+  return sizeof(C) == sizeof(float2) ? 3 : (std::is_same<C, double2>::value ? 0 : 2);
+}
+// stride of one work sequence
+template <typename C> __host__ __device__ inline int dct_sx(int N) {
+  return dct_ps<C>() > 0 ? N + (N >> dct_ps<C>()) + 1 : N;
+}
+
 // shared memory of the fast DCT in units of the complex type C: work
-// [TM][N], FFT twiddles [N], cos/sin table [N+1], permutation [N] ints
+// [TM][sx], FFT twiddles [N], cos/sin table [N+1], permutation [N] ints
 template <typename C>
 __host__ __device__ inline size_t dct_smem_bytes_t(const Dct& d) {
   if (!d.fast) return 0;
-  const size_t n = (size_t)TM * d.N + d.N + d.N + 1;
+  const size_t n = (size_t)TM * dct_sx<C>(d.N) + d.N + d.N + 1;
   const size_t c = (n * sizeof(C) + 15) / 16 * 16;
   return c + ((size_t)d.N * sizeof(int) + 15) / 16 * 16;
 }
+// bytes for the FP32 tiles (f32) or the larger of the FP64 and double-float ones
 __host__ __device__ inline size_t dct_smem_bytes(const Dct& d, bool f32 = false) {
-  return f32 ? dct_smem_bytes_t<float2>(d) : dct_smem_bytes_t<double2>(d);
+  if (f32) return dct_smem_bytes_t<float2>(d);
+  const size_t a = dct_smem_bytes_t<double2>(d), b = dct_smem_bytes_t<cdfl>(d);
+  return a > b ? a : b;
 }
 
 // Arithmetic of a tile type: double2 (FP64) or cdfl (double-float, the
@@ -376,9 +392,9 @@ template <typename C = double2>
 __device__ __forceinline__ DctSharedT<C> dct_shared(const Dct& d, void* base) {
   DctSharedT<C> s;
   s.work = reinterpret_cast<C*>(base);
-  s.tw = s.work + TM * d.N;
+  s.tw = s.work + TM * dct_sx<C>(d.N);
   s.cs = s.tw + d.N;
-  const size_t cbytes = ((size_t)(TM * d.N + d.N + d.N + 1) * sizeof(C) + 15) / 16 * 16;
+  const size_t cbytes = ((size_t)(TM * dct_sx<C>(d.N) + d.N + d.N + 1) * sizeof(C) + 15) / 16 * 16;
   s.perm = reinterpret_cast<int*>(reinterpret_cast<char*>(base) + cbytes);
   if (d.fast) {
     const C* tw = dct_tw<C>(d);
@@ -416,8 +432,8 @@ __device__ __forceinline__ void tdct(C* out, const C* in, const Dct& d, const Dc
     if (inverse && (n == 0 || n == N)) v = gscale(v, half);
     return v;
   };
-  constexpr int PS = 0;
-  const int SX = N;
+  constexpr int PS = dct_ps<C>();
+  const int SX = dct_sx<C>(N);
   auto W = [&](int mm, int pos) -> C& { return s.work[mm * SX + fft_pad<PS>(pos)]; };
   for (int idx = threadIdx.x; idx < TM * N; idx += blockDim.x) {
     const int mm = idx / N, j = idx - mm * N;
