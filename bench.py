@@ -209,7 +209,11 @@ def kernel_work(name: str, g, launches_per_step: int, tc: bool = False) -> tuple
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
 # dominant kernel class of the mixed step at 256^2 x 256 (2/3 rule), from one
 # single-pass ncu capture of a timed mixed step at that size
-NCU_TRAFFIC_256 = {"h2_row_products_f32": 452866048}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# main kernel classes of the mixed step at 256^2 x 256 (2/3 rule), each from
+# a one-launch ncu capture of a mixed step at that size (profiles/)
+NCU_TRAFFIC_256 = {"corr_pre": 258424320, "vback_stage2": 880997888, "h2_row_products_f32": 451207424,
+                   "tau_solve": 225772800, "corr_sub_mid": 136062976, "vpost": 272108032}
 NCU_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, full size"
 
 
@@ -374,25 +378,35 @@ def _roofline(prof, grid, steps, peaks):
 
 
 def dominant_roofline(prof, roof, workload_key, peaks) -> dict:
-    """The roofline entry of the kernel class with the largest time share,
-    with its DRAM traffic per launch (ncu, where measured for this workload)
-    and the HBM view of that traffic beside its limiting-pipe figure."""
+    """The roofline block of the kernel class with the largest time share.
+
+    Every kernel of the step is bounded by HBM or by a CUDA-core pipe (no
+    kernel with a large share is a contraction), so the block states the HBM
+    view: achieved = the class's algorithmic bytes per launch (kernel_work)
+    over its average launch time, against the measured copy bandwidth
+    (MEASURED_PEAKS.json); traffic = the ncu DRAM bytes of one launch where
+    measured for this workload.  ``pipe_view`` keeps the limiting-pipe
+    figures (FP64: the DGEMM rate measured in this run; FP32: SGEMM; double-
+    float kernels count FP64-equivalent flops against DGEMM, so that figure can
+    exceed 1 and only says the FP64 pipe is not the limit)."""
     dname = max(prof.items(), key=lambda kv: kv[1][1])[0]
-    dom = dict(roof[dname])
-    dom["kernel"] = dname
-    dom["bound"] = dom.pop("pipe")
-    dom["traffic"] = None
-    dom["peak_source"] = {"fp64": "cuBLAS DGEMM 8192^3 measured in this run",
-                          "df64": "cuBLAS DGEMM 8192^3 measured in this run (FP64-equivalent flops)",
-                          "fp32": "cuBLAS SGEMM 8192^3 (TF32 off) measured in this run",
-                          "hbm": "MEASURED_PEAKS.json hbm_gbs"}[dom["bound"]]
+    r = roof[dname]
+    ms = r["avg_launch_ms"]
+    bytes_ = r["bytes_per_launch"]
+    hbm = peaks.get("hbm")
+    ach = bytes_ / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    dom = {"kernel": dname, "bound": "hbm", "achieved": round(ach, 1), "unit": "GB/s",
+           "peak": hbm, "frac": round(ach / hbm, 4) if hbm else None, "traffic": None,
+           "launches": r["launches"], "avg_launch_ms": ms, "bytes_per_launch": bytes_,
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)",
+           "pipe_view": {k: r[k] for k in ("pipe", "achieved", "unit", "peak", "frac", "flops_per_launch", "note")
+                         if k in r}}
     if workload_key == (256, 256, "23_rule") and dname in NCU_TRAFFIC_256:
         dom["traffic"] = NCU_TRAFFIC_256[dname]
         dom["traffic_source"] = NCU_TRAFFIC_SOURCE
-        if peaks.get("hbm"):
-            gbs = dom["traffic"] / (dom["avg_launch_ms"] * 1e-3) / 1e9
-            dom["hbm_view"] = {"achieved_gbs": round(gbs, 1), "peak_gbs": peaks["hbm"],
-                               "frac": round(gbs / peaks["hbm"], 4)}
+        if hbm:
+            gbs = dom["traffic"] / (ms * 1e-3) / 1e9
+            dom["traffic_view"] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm, 4)}
     return dom
 
 

@@ -58,18 +58,20 @@ def test_kernel_work_padded_products():
 
 def test_dominant_roofline_entry():
     """The JSON roofline block of the dominant kernel, from a synthetic
-    profile: largest-share class, bound and peak source, the ncu traffic of
-    the headline workload and its HBM view."""
+    profile: largest-share class, the HBM view against the measured copy
+    bandwidth, the ncu traffic of the headline workload, the pipe view."""
     g = make_grid(NHQGConfig(**bench.workload(48, 16)))
     prof = {"h2_row_products_f32": (20, 13.0), "corr_pre": (20, 8.0), "corr_sub_mid": (60, 5.0)}
     peaks = {"fp64": 1.1, "fp32": 70.0, "hbm": 6500.0}
     roof = bench._roofline(prof, g, 10, peaks)
     dom = bench.dominant_roofline(prof, roof, (256, 256, "23_rule"), peaks)
-    assert dom["kernel"] == "h2_row_products_f32" and dom["bound"] == "fp32"
+    assert dom["kernel"] == "h2_row_products_f32" and dom["bound"] == "hbm" and dom["unit"] == "GB/s"
+    assert dom["peak"] == 6500.0 and 0.0 < dom["frac"] == round(dom["achieved"] / 6500.0, 4)
     assert dom["traffic"] == bench.NCU_TRAFFIC_256["h2_row_products_f32"]
-    assert 0.0 < dom["hbm_view"]["frac"] < 1.0 and dom["frac"] > 0
+    assert dom["pipe_view"]["pipe"] == "fp32" and dom["pipe_view"]["frac"] > 0
     other = bench.dominant_roofline(prof, roof, (128, 256, "23_rule"), peaks)
-    assert other["traffic"] is None and "hbm_view" not in other
+    assert other["traffic"] is None and "traffic_view" not in other
+
 
 
 def test_reference_arm_polar_json():
