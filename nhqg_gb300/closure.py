@@ -168,8 +168,9 @@ def truncate(state, coarse: Grid) -> State:
     Galerkin basis functions of the kept indices are the same functions)."""
     P, G = coarse.Nz + 1, coarse.Nz - 1
     s = to_device(state)
-    return State(s.q_hat[:P].contiguous(), s.w_hat[:G].contiguous(), s.th_hat[:G].contiguous(),
-                 s.th_bar[:P].contiguous())
+    # copies: a leading slice of a contiguous field is itself contiguous, and
+    # a view would share memory with the fine state
+    return State(s.q_hat[:P].clone(), s.w_hat[:G].clone(), s.th_hat[:G].clone(), s.th_bar[:P].clone())
 
 
 def _base(g: Grid) -> Grid:
