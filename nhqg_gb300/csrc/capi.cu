@@ -350,6 +350,21 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   UP(t.proj, g->proj_dirichlet, (size_t)P * P);
   UP(t.D1, g->sbp_D1, (size_t)P * P);
   UP(t.Lsbp, g->sbp_L, (size_t)P * P);
+  {  // diagonals of D1 and of the SBP Laplacian (the corrector's 1-D kernels)
+    std::vector<double> d1b(3 * (size_t)P, 0.0), lb(5 * (size_t)P, 0.0);
+    for (int i = 0; i < P; ++i) {
+      for (int d = 0; d < 3; ++d) {
+        const int j = i - 1 + d;
+        if (j >= 0 && j < P) d1b[(size_t)d * P + i] = g->sbp_D1[(size_t)i * P + j];
+      }
+      for (int d = 0; d < 5; ++d) {
+        const int j = i - 2 + d;
+        if (j >= 0 && j < P) lb[(size_t)d * P + i] = g->sbp_L[(size_t)i * P + j];
+      }
+    }
+    UP(t.D1b, d1b.data(), d1b.size());
+    UP(t.Lb, lb.data(), lb.size());
+  }
   UP(t.GZ, g->G_Z, (size_t)P * P);
   {
     std::vector<double> gz2((size_t)P * P, 0.0);
@@ -375,6 +390,23 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     UP(t.c2s_val, a.val.data(), a.val.size());
     UP(t.s2c_ptr, b.ptr.data(), b.ptr.size()); UP(t.s2c_col, b.col.data(), b.col.size());
     UP(t.s2c_val, b.val.data(), b.val.size());
+    int w = 1;
+    for (int i = 0; i < P; ++i)
+      w = std::max(w, std::max(a.ptr[i + 1] - a.ptr[i], b.ptr[i + 1] - b.ptr[i]));
+    std::vector<int> ac((size_t)w * P), bc((size_t)w * P);
+    std::vector<double> av((size_t)w * P, 0.0), bvv((size_t)w * P, 0.0);
+    for (int i = 0; i < P; ++i)
+      for (int q = 0; q < w; ++q) {
+        const int qa = a.ptr[i] + q, qb = b.ptr[i] + q;
+        const bool ina = qa < a.ptr[i + 1], inb = qb < b.ptr[i + 1];
+        ac[(size_t)q * P + i] = ina ? a.col[qa] : i;
+        av[(size_t)q * P + i] = ina ? a.val[qa] : 0.0;
+        bc[(size_t)q * P + i] = inb ? b.col[qb] : i;
+        bvv[(size_t)q * P + i] = inb ? b.val[qb] : 0.0;
+      }
+    t.ell_w = w;
+    UP(t.c2s_ecol, ac.data(), ac.size()); UP(t.c2s_eval, av.data(), av.size());
+    UP(t.s2c_ecol, bc.data(), bc.size()); UP(t.s2c_eval, bvv.data(), bvv.size());
     UP(t.c2s_d, g->cgl_to_sbp, (size_t)P * P);
     UP(t.s2c_d, g->sbp_to_cgl, (size_t)P * P);
   }

@@ -93,6 +93,21 @@ template <> struct Prec<cdfl> {
   static __device__ __forceinline__ cdfl in(float2 v) { return cdfl{dfl(v.x, 0.f), dfl(v.y, 0.f)}; }
   static __device__ __forceinline__ double2 out(cdfl v) { return cdf_to(v); }
 };
+// FP32 tiles (the mixed-precision corrector's w, which enters it only
+// through the sub_dt-scaled exchange increment and the FP32 products).  The
+// FP64 <-> FP32 conversions go through the integer split of df64.cuh (the
+// two-float sum rounded once in FP32) instead of the FP64 pipe.
+template <> struct Prec<float2> {
+  using T = float;
+  static __device__ __forceinline__ float s(double v) {
+    const dfl d = df_from_double(v);
+    return __fadd_rn(d.hi, d.lo);
+  }
+  static __device__ __forceinline__ float i(int v) { return (float)v; }
+  static __device__ __forceinline__ float2 in(double2 v) { return make_float2(s(v.x), s(v.y)); }
+  static __device__ __forceinline__ float2 in(float2 v) { return v; }
+  static __device__ __forceinline__ double2 out(float2 v) { return make_double2(f2d_bits(v.x), f2d_bits(v.y)); }
+};
 template <typename C> __device__ __forceinline__ C gzero() {
   using T = typename Prec<C>::T;
   return gmk<C>(T(0), T(0));

@@ -12,6 +12,9 @@
 // The 1-D system A = I - half (pentadiagonal: D1 diag(<w^2>) D1 and the SBP
 // Laplacian) is factored once per corrector without pivoting: it is the
 // identity plus a weakly diagonally dominant M-matrix-like term.
+#include <algorithm>
+#include <cmath>
+
 #include "column.cuh"
 #include "engine.h"
 
@@ -42,7 +45,16 @@ struct CV {
   __host__ __device__ int Aband() const { return 6 * P; }   // 5P: diag offsets -2..2
   __host__ __device__ int Bband() const { return 11 * P; }  // 5P
   __host__ __device__ int lu32() const { return 16 * P; }   // 3P doubles = 6P floats: FP32 LU band
-  __host__ __device__ int total() const { return 19 * P; }
+  __host__ __device__ int lu_ok() const { return 19 * P; }  // 1: lu32 holds the factors of this A
+  __host__ __device__ int win() const { return 19 * P + 2; }  // window factors
+  __host__ __device__ int total() const { return 19 * P + 2 + win_doubles(P); }
+  // overlapping windows of the 1-D solve: kWinCore core rows, up to
+  // kWinOvMax rows of overlap on each side, 5 FP32 band rows each (+1 float
+  // of padding per window so that the windows' threads hit distinct banks)
+  static constexpr int kWinCore = 32, kWinOvMax = 24, kWinLen = kWinCore + 2 * kWinOvMax;
+  static constexpr int kWinStride = 5 * kWinLen + 1;  // floats per window
+  __host__ __device__ static constexpr int n_win(int P) { return (P + kWinCore - 1) / kWinCore; }
+  __host__ __device__ static constexpr int win_doubles(int P) { return (n_win(P) * kWinStride + 1) / 2; }
 };
 
 struct CK {
@@ -56,6 +68,11 @@ struct CK {
   const double *bcF, *bcV, *proj, *D1, *Lsbp;
   const double *c2sV, *tauVinv;  // fused dense 1-D maps (rows applied by many CTAs)
   double mu, kappa;
+  const double *D1b, *Lb;  // D1 (3 diagonals) and the SBP Laplacian (5), [d][P]
+  int ell_w;               // c2s / s2c as fixed-width rows, [q][P]
+  const int *c2s_ecol, *s2c_ecol;
+  const double *c2s_eval, *s2c_eval;
+  int win_ov;              // overlap of the windowed 1-D solve; 0: one serial LU
 };
 
 CK make_ck(const Params& p, const Tables& t) {
@@ -71,6 +88,10 @@ CK make_ck(const Params& p, const Tables& t) {
   k.c2sV = t.c2sV; k.tauVinv = t.tauVinv;
   k.mu = p.eps_sq;
   k.kappa = 1.0 / p.sigma;
+  k.D1b = t.D1b; k.Lb = t.Lb;
+  k.ell_w = t.ell_w;
+  k.c2s_ecol = t.c2s_ecol; k.s2c_ecol = t.s2c_ecol; k.c2s_eval = t.c2s_eval; k.s2c_eval = t.s2c_eval;
+  k.win_ov = 0;
   return k;
 }
 
@@ -116,28 +137,41 @@ __device__ __forceinline__ void rows_by_ctas(const double* __restrict__ Mat, con
 
 // Predictor w and theta to nodal CGL values and to the SBP grid; the CTAs
 // also form tb_sbp = c2s V tbp (the predictor mean temperature on the SBP grid).
+// In the double-float path w runs on FP32 tiles: it enters the corrector only
+// through the exchange increment sub_dt g_half w (about 1e-5 of theta, so an
+// FP32 w changes theta by ~1e-12 relative), the means <w^2>, <w theta> (an
+// FP32-relative error there is again scaled by sub_dt) and the nodal w of the
+// next explicit RHS, whose products are FP32.  theta, the state the corrector
+// carries, stays double-float.
 template <typename C>
 __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const double2* tp,
                                                  double2* wcgl, double2* wsbp, double2* tsbp,
                                                  const double* tbp, double* vec) {
   rows_by_ctas(k.c2sV, tbp, vec + CV{k.P}.tb_sbp(), k.P);
+  using CW = typename std::conditional<std::is_same<C, cdfl>::value, float2, C>::type;
   extern __shared__ double2 sm_raw[];
-  C* sm = reinterpret_cast<C*>(sm_raw);
   const int PT = k.P * TM;
-  C *b0 = sm, *b1 = sm + PT;
-  const col::DctSharedT<C> ds = col::dct_shared<C>(k.dct, sm + 2 * PT);
+  void* dct_base = sm_raw + 2 * PT;  // after two tiles of the widest type
   const int m0 = blockIdx.x * TM;
-  tloadp(b0, wp, k.G, m0, k.M);
-  __syncthreads();
-  tstencil(k, true, b1, b0);
-  __syncthreads();
-  tdct(b0, b1, k.dct, ds, false, k.P);
-  __syncthreads();
-  tstorep(b0, wcgl, k.P, m0, k.M);
-  tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
-  __syncthreads();
-  tstorep(b1, wsbp, k.P, m0, k.M);
-  __syncthreads();
+  {
+    CW* sw = reinterpret_cast<CW*>(sm_raw);
+    CW *b0 = sw, *b1 = sw + PT;
+    const col::DctSharedT<CW> ds = col::dct_shared<CW>(k.dct, dct_base);
+    tloadp(b0, wp, k.G, m0, k.M);
+    __syncthreads();
+    tstencil(k, true, b1, b0);
+    __syncthreads();
+    tdct(b0, b1, k.dct, ds, false, k.P);
+    __syncthreads();
+    tstorep(b0, wcgl, k.P, m0, k.M);
+    tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
+    __syncthreads();
+    tstorep(b1, wsbp, k.P, m0, k.M);
+    __syncthreads();
+  }
+  C* sm = reinterpret_cast<C*>(sm_raw);
+  C *b0 = sm, *b1 = sm + PT;
+  const col::DctSharedT<C> ds = col::dct_shared<C>(k.dct, dct_base);
   tloadp(b0, tp, k.G, m0, k.M);
   __syncthreads();
   tstencil(k, false, b1, b0);
@@ -287,271 +321,415 @@ __device__ void vec_dense(double* out, const double* in, const double* Mat, int 
     out[i] = acc;
   }
 }
-__device__ void vec_csr(double* out, const double* in, const int* ptr, const int* col,
-                        const double* val, int n) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double acc = 0.0;
-    for (int q = ptr[i]; q < ptr[i + 1]; ++q) acc = fma(val[q], in[col[q]], acc);
-    out[i] = acc;
-  }
-}
-// pentadiagonal matrix stored as band[d*P + i] = A[i, i+d-2]
-__device__ void band_matvec(double* out, const double* band, const double* x, int P) {
-  for (int i = threadIdx.x; i < P; i += blockDim.x) {
-    double acc = 0.0;
-    for (int d = 0; d < 5; ++d) {
-      const int j = i + d - 2;
-      if (j >= 0 && j < P) acc = fma(band[d * P + i], x[j], acc);
-    }
-    out[i] = acc;
-  }
-}
-// D1 (tridiagonal) product
-__device__ void d1_matvec(double* out, const double* D1, const double* x, int P) {
-  for (int i = threadIdx.x; i < P; i += blockDim.x) {
-    double acc = 0.0;
-    for (int j = max(0, i - 1); j <= min(P - 1, i + 1); ++j) acc = fma(D1[(size_t)i * P + j], x[j], acc);
-    out[i] = acc;
+// ---- 1-D corrector solve
+// A = I - h (boundary rows identity) and B = I + h with the pentadiagonal
+// h = (mu kappa sub_dt / 2) L_sbp + (mu sub_dt^2 / 4) D1 diag(<w^2>) D1, per
+// corrector.  A = I + (an M-matrix-like term) is diagonally dominant with a
+// condition number near 1 (1.7 at 256 levels, dt = 2e-5), and its inverse
+// decays geometrically away from the diagonal, like r^|i-j| with r the small
+// root of a r^2 - (1 + 2a) r + a = 0, a = mu kappa sub_dt / (2 dz^2)
+// (r = 0.125 there).
+//
+// Solve: FP64 iterative refinement (Wilkinson's mixed-precision scheme)
+// around an FP32 approximate inverse, x_0 = M b, x_{k+1} = x_k + M (b - A x_k)
+// with the residual in FP64.  M is the restricted additive Schwarz inverse
+// over overlapping windows: window w owns the kWinCore core rows
+// [32 w, 32 w + 32) and solves the window's own block of A over the core
+// widened by win_ov rows on each side (FP32 banded LU, factored per window
+// in parallel), keeping its core rows.  The truncated coupling changes the
+// core rows by about r^win_ov relative, which the host sets to 1e-7 or
+// below, so each sweep divides the error by about 1e7 -- as a global FP32 LU
+// would -- while the serial chains are one window long instead of P.  If
+// the last correction is not below 1e-10 of the solution (the windows did
+// not converge: a far larger <w^2> than the host's estimate assumed), the
+// kernel factors the whole band once (one thread) and redoes the solve with
+// it.
+
+// Banded LU without pivoting of rows [e0, e0 + n) of the pentadiagonal A
+// (band[d P + i] = A[i, i + d - 2]; couplings outside the block dropped):
+// F[0][ii], F[1][ii] the multipliers of rows ii-2, ii-1; F[2][ii] = 1 /
+// pivot; F[3][ii], F[4][ii] the two superdiagonals of U times 1 / pivot.
+// Serial (one thread per block), FP32.
+__device__ __forceinline__ void lu32_factor(const float* __restrict__ A, int P, int e0, int n,
+                                            float* __restrict__ F, int ld) {
+  float d1 = 0.f, d2 = 0.f;    // 1/pivot of rows ii-1, ii-2
+  float u11 = 0.f, u21 = 0.f;  // U(ii-1, ii), U(ii-1, ii+1)
+  float u12 = 0.f, u22 = 0.f;  // U(ii-2, ii-1), U(ii-2, ii)
+  for (int ii = 0; ii < n; ++ii) {
+    const int i = e0 + ii;
+    const float a0 = ii >= 2 ? A[0 * P + i] : 0.f;
+    const float a1 = ii >= 1 ? A[1 * P + i] : 0.f;
+    const float a2 = A[2 * P + i];
+    const float a3 = ii + 1 < n ? A[3 * P + i] : 0.f;
+    const float a4 = ii + 2 < n ? A[4 * P + i] : 0.f;
+    const float l2 = a0 * d2;                    // row ii-2 multiplier
+    const float l1 = fmaf(-l2, u12, a1) * d1;    // row ii-1 multiplier
+    const float piv = fmaf(-l1, u11, fmaf(-l2, u22, a2));
+    const float dv = __frcp_rn(piv);
+    const float s1 = fmaf(-l1, u21, a3);         // U(ii, ii+1)
+    F[0 * ld + ii] = l2;
+    F[1 * ld + ii] = l1;
+    F[2 * ld + ii] = dv;
+    F[3 * ld + ii] = s1 * dv;
+    F[4 * ld + ii] = a4 * dv;
+    u12 = u11; u22 = u21;
+    u11 = s1; u21 = a4;
+    d2 = d1; d1 = dv;
   }
 }
 
-// The band is built and factored in shared memory: the factorisation is a
-// serial recurrence, and shared-memory operands keep each step at on-chip
-// latency.  Dynamic shared memory: 10 P doubles.
-// Builds the pentadiagonal corrector matrices A = I - h (boundary rows
-// identity) and B = I + h in FP64, and factors A in FP32 (LU without
-// pivoting: A is the identity plus an M-matrix-like term, diagonally
-// dominant, so the factors stay bounded).  The substitutions of
-// k_corr_tstep use the FP32 factors inside an FP64 iterative refinement: the
-// factorisation and the substitutions are serial recurrences, and on this
-// GPU a dependent FP64 operation costs about 14 times a dependent FP32 one
-// (a division about 90 times).  Dynamic shared memory: 10 P doubles.
-__device__ __forceinline__ void corr_init_body(const CK& k, double* vec, double sub_dt, double* band_sm) {
-  const CV cv{k.P};
-  const int P = k.P;
-  double* w2 = vec + cv.w2();
-  double* A = band_sm;
-  double* B = band_sm + 5 * P;
-  const double c1 = 0.5 * k.mu * k.kappa * sub_dt;
-  const double c2 = 0.25 * k.mu * (sub_dt * sub_dt);
-  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) {
-    const int d = idx / P, i = idx - d * P;
-    const int j = i + d - 2;
-    double h = 0.0, a = 0.0, b = 0.0;
-    if (j >= 0 && j < P) {
-      double dmd = 0.0;  // (D1 diag(w2) D1)[i, j]
-      for (int kk = max(0, i - 1); kk <= min(P - 1, i + 1); ++kk) {
-        if (abs(kk - j) <= 1) dmd = fma(k.D1[(size_t)i * P + kk] * w2[kk], k.D1[(size_t)kk * P + j], dmd);
-      }
-      h = fma(c1, k.Lsbp[(size_t)i * P + j], c2 * dmd);
-      const double id = (i == j) ? 1.0 : 0.0;
-      a = id - h;
-      b = id + h;
-      if (i == 0 || i == P - 1) a = id;
-    }
-    A[idx] = a;
-    B[idx] = b;
-    vec[cv.Aband() + idx] = a;
-    vec[cv.Bband() + idx] = b;
-  }
-  __syncthreads();
-  float* L = reinterpret_cast<float*>(band_sm + 5 * P);  // FP32 factors over the B copy
-  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) L[idx] = (float)A[idx];
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    // banded LU: multipliers below the diagonal, 1/pivot in the diagonal
-    // slot.  Row i of the band is A[i, i-2 .. i+2]; the running values of
-    // the two rows below the current pivot stay in registers.
-    float r1_0 = P > 1 ? L[1 * P + 1] : 0.f, r1_1 = P > 1 ? L[2 * P + 1] : 0.f;
-    float r1_2 = P > 1 ? L[3 * P + 1] : 0.f;
-    float piv = L[2 * P + 0], u1 = L[3 * P + 0], u2 = L[4 * P + 0];
-    for (int col = 0; col < P; ++col) {
-      const float rp = 1.0f / piv;
-      L[2 * P + col] = rp;
-      float r2_0 = 0.f, r2_1 = 0.f, r2_2 = 0.f, r2_3 = 0.f;
-      if (col + 2 < P) {
-        r2_0 = L[0 * P + col + 2];
-        r2_1 = L[1 * P + col + 2];
-        r2_2 = L[2 * P + col + 2];
-        r2_3 = L[3 * P + col + 2];
-      }
-      float n_piv = 0.f, n_u1 = 0.f, n_u2 = 0.f;
-      if (col + 1 < P) {
-        const float l = r1_0 * rp;
-        L[1 * P + col + 1] = l;
-        n_piv = fmaf(-l, u1, r1_1);
-        n_u1 = fmaf(-l, u2, r1_2);
-        n_u2 = (col + 3 < P) ? L[4 * P + col + 1] : 0.f;
-        L[3 * P + col + 1] = n_u1;
-      }
-      if (col + 2 < P) {
-        const float l = r2_0 * rp;
-        L[0 * P + col + 2] = l;
-        r1_0 = fmaf(-l, u1, r2_1);
-        r1_1 = fmaf(-l, u2, r2_2);
-        r1_2 = r2_3;
-      }
-      piv = n_piv; u1 = n_u1; u2 = n_u2;
-    }
-  }
-  __syncthreads();
-  float* Lg = reinterpret_cast<float*>(vec + cv.lu32());
-  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) Lg[idx] = L[idx];
-  __syncthreads();
-}
-
-// d = (LU)^-1 r with the FP32 factors: rf holds r in FP32 on entry and d on
-// exit.  Serial, thread 0; FP32 only, so each step costs FP32 latency.
-__device__ __forceinline__ void lu32_solve(const float* __restrict__ L, float* __restrict__ rf, int P) {
-  // operands are fetched 8 rows ahead of the dependent chain so that the
-  // shared-memory latency overlaps the FMAs
+// x = (LU)^-1 r on a block of n rows with factors F (row stride ld): r is
+// read through ridx(ii), x written through xout(ii, v); tmp takes the
+// forward sweep (n rounded up to 8 floats).  The sweeps run over whole
+// blocks of 8 rows with every operand index clamped into [0, n): the loads
+// of a block are unconditional and issue together ahead of its dependent
+// chain, rows past n carry zeros into the backward sweep, and each row adds
+// the term two rows back first, so the chain through the previous row is
+// one FMA in both sweeps.
+template <typename RI, typename XO>
+__device__ __forceinline__ void lu32_solve(const float* __restrict__ F, int ld, int n, RI ridx,
+                                           float* __restrict__ tmp, XO xout) {
   constexpr int U = 8;
-  float v1 = rf[0], v2 = 0.f;
-  int i = 1;
-  for (; i + U <= P; i += U) {
+  const int npad = (n + U - 1) & ~(U - 1);
+  float v1 = 0.f, v2 = 0.f;
+  for (int i0 = 0; i0 < npad; i0 += U) {
     float a0[U], a1[U], r[U];
 #pragma unroll
-    for (int q = 0; q < U; ++q) { a0[q] = L[0 * P + i + q]; a1[q] = L[1 * P + i + q]; r[q] = rf[i + q]; }
+    for (int q = 0; q < U; ++q) {
+      const int i = min(i0 + q, n - 1);
+      a0[q] = F[0 * ld + i];
+      a1[q] = F[1 * ld + i];
+      r[q] = ridx(i);
+    }
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      float v = fmaf(-a1[q], v1, r[q]);
-      if (i + q >= 2) v = fmaf(-a0[q], v2, v);
-      rf[i + q] = v;
+      const float v = fmaf(-a1[q], v1, fmaf(-a0[q], v2, r[q]));
+      tmp[i0 + q] = (i0 + q < n) ? v : 0.f;
       v2 = v1;
       v1 = v;
     }
   }
-  for (; i < P; ++i) {
-    float v = fmaf(-L[1 * P + i], v1, rf[i]);
-    if (i >= 2) v = fmaf(-L[0 * P + i], v2, v);
-    rf[i] = v;
-    v2 = v1;
-    v1 = v;
-  }
   float x1 = 0.f, x2 = 0.f;
-  int j = P - 1;
-  for (; j - U + 1 >= 0; j -= U) {
-    float d[U], u1[U], u2[U], r[U];
+  for (int j0 = npad - 1; j0 >= 0; j0 -= U) {
+    float t[U], u1[U], u2[U];
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      const int ii = j - q;
-      d[q] = L[2 * P + ii]; u1[q] = L[3 * P + ii]; u2[q] = L[4 * P + ii]; r[q] = rf[ii];
+      const int jc = min(j0 - q, n - 1);
+      t[q] = tmp[j0 - q] * F[2 * ld + jc];
+      u1[q] = F[3 * ld + jc];
+      u2[q] = F[4 * ld + jc];
     }
 #pragma unroll
     for (int q = 0; q < U; ++q) {
-      const int ii = j - q;
-      float v = r[q];
-      if (ii + 1 < P) v = fmaf(-u1[q], x1, v);
-      if (ii + 2 < P) v = fmaf(-u2[q], x2, v);
-      v *= d[q];
-      rf[ii] = v;
+      const float v = fmaf(-u1[q], x1, fmaf(-u2[q], x2, t[q]));
+      if (j0 - q < n) xout(j0 - q, v);
       x2 = x1;
       x1 = v;
     }
   }
-  for (; j >= 0; --j) {
-    float v = rf[j];
-    if (j + 1 < P) v = fmaf(-L[3 * P + j], x1, v);
-    if (j + 2 < P) v = fmaf(-L[4 * P + j], x2, v);
-    v *= L[2 * P + j];
-    rf[j] = v;
-    x2 = x1;
-    x1 = v;
+}
+
+// shared-memory index of level i in the FP32 vectors of the windowed solve:
+// one float of padding per 32, so that windows 32 levels apart use distinct
+// banks
+__device__ __forceinline__ int pz(int i) { return i + (i >> 5); }
+
+// dst[i] = src[i], i < n, eight independent loads in flight per thread
+template <typename T>
+__device__ __forceinline__ void copy_block(T* __restrict__ dst, const T* __restrict__ src, int n) {
+  constexpr int U = 8;
+  const int step = blockDim.x * U;
+  for (int i0 = threadIdx.x; i0 < n; i0 += step) {
+    T v[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const int i = i0 + q * blockDim.x;
+      v[q] = i < n ? src[i] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < U; ++q) {
+      const int i = i0 + q * blockDim.x;
+      if (i < n) dst[i] = v[q];
+    }
   }
 }
 
-// Solves A tb_new = B tb_sbp - mu sub_dt D1 flux by FP64 iterative
-// refinement around the FP32 factors (Wilkinson's mixed-precision iterative
-// refinement): x_0 = (LU)^-1 b, x_{k+1} = x_k + (LU)^-1 (b - A x_k) with the
-// residual in FP64.  Each sweep divides the error by about
-// 1 / (cond(A) eps_32); kRefine sweeps reach FP64 round-off for the
-// corrector's well-conditioned A = I + (SPD-like) h.  Dynamic shared memory:
-// 5 P doubles (FP64 A band) + 3 P doubles (FP32 factors) + 3 P doubles.
-// With init (the first substep) the kernel first builds and factors the
-// corrector matrices (corr_init_body); its global writes are visible to the
-// rest of the CTA after the barrier that ends the body.
 constexpr int kRefine = 2;
-__global__ void k_corr_tstep(CK k, double* vec, double sub_dt, int last, int init) {
+// dynamic shared memory of k_corr_tstep, doubles
+__host__ __device__ constexpr int kTstepSmem(int P) { return 15 * P + 64 + CV::win_doubles(P); }
+
+// One substep of the 1-D mean-temperature update: solves
+//   A tb_new = B tb_sbp - mu sub_dt D1 flux,
+// then g_half = D1 (tb_sbp + tb_new) / 2 and, except after the last
+// substep, the round trip of tb_new through coefficients to the SBP grid
+// (y = s2c tb_new, tb_sbp = c2s (y + V[:,N-1] F_0.y + V[:,N] F_1.y)).
+// With init (the first substep of a corrector) the kernel first builds A and
+// B and factors the windows.  Every phase issues its global loads together
+// (the band tables, the fixed-width c2s / s2c rows), so each costs one
+// memory latency.
+__global__ void __launch_bounds__(NT) k_corr_tstep(CK k, double* vec, double sub_dt, int last, int init) {
   const CV cv{k.P};
   const int P = k.P;
+  const int nw = CV::n_win(P);
   __shared__ double red[64];
-  extern __shared__ double band_sm[];
-  if (init) corr_init_body(k, vec, sub_dt, band_sm);
-  double* flux = vec + cv.flux();
+  __shared__ float wmax[2][NT / 32];
+  __shared__ int fail;
+  extern __shared__ double smem[];
+  double* A = smem;               // 5P FP64 band
+  double* xs = smem + 5 * P;      // tb_sbp
+  double* b = smem + 6 * P;
+  double* sol = smem + 7 * P;
+  double* res = smem + 8 * P;
+  double* y = smem + 9 * P;       // s2c tb_new
+  double* u = smem + 10 * P;      // tb_sbp + tb_new, then the rank-2 update
+  float* rin = reinterpret_cast<float*>(smem + 11 * P);  // FP32 residual (pz index)
+  float* xo = reinterpret_cast<float*>(smem + 12 * P);   // FP32 correction (pz index)
+  float* fw = reinterpret_cast<float*>(smem + 13 * P);   // forward sweeps, kWinLen + 1 per window
+  float* W = reinterpret_cast<float*>(smem + 15 * P + 64);  // window factors, or the global ones
+  float* Wg = reinterpret_cast<float*>(vec + cv.win());
+  float* Lg = reinterpret_cast<float*>(vec + cv.lu32());
   double* tbs = vec + cv.tb_sbp();
+  const double* flux = vec + cv.flux();
   double* gh = vec + cv.g_half();
-  double* A = band_sm;                                  // 5P FP64
-  float* L = reinterpret_cast<float*>(band_sm + 5 * P); // 5P FP32 (3P doubles)
-  double* b = band_sm + 8 * P;
-  double* rhs = band_sm + 9 * P;  // the solution
-  double* res = band_sm + 10 * P;
   double* t2 = vec + cv.tmp2();
-  const double* B = vec + cv.Bband();
-  const float* Lg = reinterpret_cast<const float*>(vec + cv.lu32());
-  for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) {
-    A[idx] = vec[cv.Aband() + idx];
-    L[idx] = Lg[idx];
-  }
-  // b = B tb_sbp - mu sub_dt D1 flux
-  band_matvec(b, B, tbs, P);
-  d1_matvec(t2, k.D1, flux, P);
-  __syncthreads();
-  const double cf = k.mu * sub_dt;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) {
-    b[i] = (i == 0 || i == P - 1) ? 0.0 : fma(-cf, t2[i], b[i]);
-    res[i] = b[i];
-    rhs[i] = 0.0;
-  }
-  __syncthreads();
-  float* rf = reinterpret_cast<float*>(res);  // FP32 view of the residual slot
-  for (int it = 0; it <= kRefine; ++it) {
-    double rv[4];
-    for (int q = 0, i = threadIdx.x; i < P; i += blockDim.x, ++q) rv[q] = res[i];
-    __syncthreads();
-    for (int q = 0, i = threadIdx.x; i < P; i += blockDim.x, ++q) rf[i] = (float)rv[q];
-    __syncthreads();
-    if (threadIdx.x == 0) lu32_solve(L, rf, P);
-    __syncthreads();
-    for (int i = threadIdx.x; i < P; i += blockDim.x) rhs[i] += (double)rf[i];
-    __syncthreads();
-    if (it == kRefine) break;
-    for (int i = threadIdx.x; i < P; i += blockDim.x) {  // res = b - A x in FP64
-      double acc = b[i];
+  const int ov = k.win_ov;
+  auto d1at = [&](int d, int i) { return __ldg(k.D1b + d * P + i); };
+  if (init) {
+    // A = I - h (identity boundary rows), B = I + h; the FP32 copy of A for
+    // the factorisations sits in the not yet used b / sol / res rows
+    float* Af = reinterpret_cast<float*>(b);
+    const double* w2 = vec + cv.w2();
+    const double c1 = 0.5 * k.mu * k.kappa * sub_dt;
+    const double c2 = 0.25 * k.mu * (sub_dt * sub_dt);
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      double dl[3][3], wv[3], lb[5];  // D1 rows i-1 .. i+1, <w^2> there, L row i
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int row = i - 1 + c;
+        const bool in = row >= 0 && row < P;
+        wv[c] = in ? w2[row] : 0.0;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) dl[c][e] = in ? d1at(e, row) : 0.0;
+      }
+#pragma unroll
+      for (int d = 0; d < 5; ++d) lb[d] = __ldg(k.Lb + d * P + i);
+#pragma unroll
       for (int d = 0; d < 5; ++d) {
         const int j = i + d - 2;
-        if (j >= 0 && j < P) acc = fma(-A[d * P + i], rhs[j], acc);
+        double a = 0.0, bb = 0.0;
+        if (j >= 0 && j < P) {
+          double dmd = 0.0;  // (D1 diag(w2) D1)[i, j]
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const int kk = i - 1 + c;
+            if (kk >= 0 && kk < P && abs(kk - j) <= 1) dmd = fma(dl[1][c] * wv[c], dl[c][j - kk + 1], dmd);
+          }
+          const double h = fma(c1, lb[d], c2 * dmd);
+          const double id = (i == j) ? 1.0 : 0.0;
+          a = (i == 0 || i == P - 1) ? id : id - h;
+          bb = id + h;
+        }
+        A[d * P + i] = a;
+        Af[d * P + i] = (float)a;
+        vec[cv.Aband() + d * P + i] = a;
+        vec[cv.Bband() + d * P + i] = bb;
       }
-      res[i] = acc;
+    }
+    if (threadIdx.x == 0) vec[cv.lu_ok()] = 0.0;
+    __syncthreads();
+    if (ov > 0 && threadIdx.x < nw) {  // window factors, one thread each
+      const int w = threadIdx.x;
+      const int e0 = max(0, w * CV::kWinCore - ov), e1 = min(P, (w + 1) * CV::kWinCore + ov);
+      lu32_factor(Af, P, e0, e1 - e0, W + w * CV::kWinStride, CV::kWinLen);
     }
     __syncthreads();
+    if (ov > 0) copy_block(Wg, W, nw * CV::kWinStride);
+  } else {
+    copy_block(A, vec + cv.Aband(), 5 * P);
+    if (ov > 0) copy_block(W, Wg, nw * CV::kWinStride);
   }
-  // rhs = tb_new
-  for (int i = threadIdx.x; i < P; i += blockDim.x) t2[i] = tbs[i] + rhs[i];
+  copy_block(xs, tbs, P);
+  if (threadIdx.x == 0) fail = (ov == 0);
   __syncthreads();
-  d1_matvec(gh, k.D1, t2, P);
-  __syncthreads();
+  // b = B tb_sbp - mu sub_dt D1 flux
+  const double cf = k.mu * sub_dt;
+  const double* Bg = vec + cv.Bband();
   for (int i = threadIdx.x; i < P; i += blockDim.x) {
-    gh[i] *= 0.5;
-    if (i == 0 || i == P - 1) rhs[i] = 0.0;
+    double bv[5], dv[3], fv[3];
+#pragma unroll
+    for (int d = 0; d < 5; ++d) bv[d] = Bg[d * P + i];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const int c = min(max(i - 1 + e, 0), P - 1);
+      dv[e] = d1at(e, i);
+      fv[e] = flux[c];
+    }
+    double acc = 0.0;
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+      const int j = i + d - 2;
+      if (j >= 0 && j < P) acc = fma(bv[d], xs[j], acc);
+    }
+    double df = 0.0;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const int c = i - 1 + e;
+      if (c >= 0 && c < P) df = fma(dv[e], fv[e], df);
+    }
+    b[i] = (i == 0 || i == P - 1) ? 0.0 : fma(-cf, df, acc);
   }
   __syncthreads();
-  vec_csr(t2, rhs, k.s2c_ptr, k.s2c_col, k.s2c_val, P);  // y = s2c tb_new
-  __syncthreads();
-  if (!last) {
-    double a0 = 0.0, a1 = 0.0;
-    for (int i = threadIdx.x; i < P; i += blockDim.x) {
-      a0 = fma(k.bcF[i], t2[i], a0);
-      a1 = fma(k.bcF[P + i], t2[i], a1);
+  // refinement; M = the windows (or, after a failed check, the global LU)
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1) {
+      if (!fail) break;
+      // global factors: factor once per A (lu_ok), else reuse
+      if (vec[cv.lu_ok()] == 0.0) {
+        float* Af = reinterpret_cast<float*>(res);  // free until the sweeps start
+        for (int idx = threadIdx.x; idx < 5 * P; idx += blockDim.x) Af[idx] = (float)A[idx];
+        __syncthreads();
+        if (threadIdx.x == 0) lu32_factor(Af, P, 0, P, W, P);
+        __syncthreads();
+        copy_block(Lg, W, 5 * P);
+        __syncthreads();
+        if (threadIdx.x == 0) vec[cv.lu_ok()] = 1.0;
+      } else {
+        copy_block(W, Lg, 5 * P);
+      }
+      __syncthreads();
+    } else if (fail) {
+      continue;
     }
-    const double d0 = block_sum(a0, red);
-    const double d1 = block_sum(a1, red + 32);
-    if (threadIdx.x == 0) { red[0] = d0; red[1] = d1; }
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+      sol[i] = 0.0;
+      res[i] = b[i];
+    }
+    __syncthreads();
+    for (int it = 0; it <= kRefine; ++it) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) rin[pz(i)] = (float)res[i];
+      __syncthreads();
+      if (pass == 0) {
+        if (threadIdx.x < nw) {
+          const int w = threadIdx.x;
+          const int c0 = w * CV::kWinCore, c1 = min(P, c0 + CV::kWinCore);
+          const int e0 = max(0, c0 - ov), e1 = min(P, c1 + ov);
+          lu32_solve(W + w * CV::kWinStride, CV::kWinLen, e1 - e0,
+                     [&](int ii) { return rin[pz(e0 + ii)]; }, fw + w * (CV::kWinLen + 1),
+                     [&](int ii, float v) {
+                       const int i = e0 + ii;
+                       if (i >= c0 && i < c1) xo[pz(i)] = v;
+                     });
+        }
+      } else if (threadIdx.x == 0) {
+        lu32_solve(W, P, P, [&](int ii) { return rin[pz(ii)]; }, fw,
+                   [&](int ii, float v) { xo[pz(ii)] = v; });
+      }
+      __syncthreads();
+      const bool check = pass == 0 && it == kRefine;
+      float cmax = 0.f, smax = 0.f;
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        const float c = xo[pz(i)];
+        const double v = sol[i] + (double)c;
+        sol[i] = v;
+        if (check) {
+          cmax = fmaxf(cmax, fabsf(c));
+          smax = fmaxf(smax, fabsf((float)v));
+        }
+      }
+      if (check) {  // the windows converged: last correction <= 1e-10 max |sol|
+        for (int o = 16; o > 0; o >>= 1) {
+          cmax = fmaxf(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+          smax = fmaxf(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+          wmax[0][threadIdx.x >> 5] = cmax;
+          wmax[1][threadIdx.x >> 5] = smax;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          float c = 0.f, sm = 0.f;
+          for (int q = 0; q < NT / 32; ++q) { c = fmaxf(c, wmax[0][q]); sm = fmaxf(sm, wmax[1][q]); }
+          if (!(c <= 1e-10f * sm)) fail = 1;
+        }
+      }
+      __syncthreads();
+      if (it == kRefine) break;
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {  // res = b - A sol in FP64
+        double acc = b[i];
+#pragma unroll
+        for (int d = 0; d < 5; ++d) {
+          const int j = i + d - 2;
+          if (j >= 0 && j < P) acc = fma(-A[d * P + i], sol[j], acc);
+        }
+        res[i] = acc;
+      }
+      __syncthreads();
+    }
+  }
+  // sol = tb_new.  u = tb_sbp + tb_new (for g_half) and y = s2c tb_new with
+  // the two end values of tb_new taken as zero
+  const int ew = k.ell_w;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    u[i] = xs[i] + sol[i];
+    double acc = 0.0;
+    for (int q = 0; q < ew; ++q) {
+      const int c = __ldg(k.s2c_ecol + q * P + i);
+      const double v = (c == 0 || c == P - 1) ? 0.0 : sol[c];
+      acc = fma(__ldg(k.s2c_eval + q * P + i), v, acc);
+    }
+    y[i] = acc;
+    t2[i] = acc;
+  }
+  __syncthreads();
+  // g_half = D1 u / 2 and the rank-2 dot products F_j . y
+  double a0 = 0.0, a1 = 0.0;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    double dv[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) dv[e] = d1at(e, i);
+    const double f0 = __ldg(k.bcF + i), f1 = __ldg(k.bcF + P + i);
+    double acc = 0.0;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const int c = i - 1 + e;
+      if (c >= 0 && c < P) acc = fma(dv[e], u[c], acc);
+    }
+    gh[i] = 0.5 * acc;
+    a0 = fma(f0, y[i], a0);
+    a1 = fma(f1, y[i], a1);
+  }
+  if (!last) {
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_down_sync(0xffffffffu, a0, o);
+      a1 += __shfl_down_sync(0xffffffffu, a1, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[threadIdx.x >> 5] = a0;
+      red[32 + (threadIdx.x >> 5)] = a1;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const int nwp = blockDim.x >> 5;
+      double s0 = threadIdx.x < nwp ? red[threadIdx.x] : 0.0;
+      double s1 = threadIdx.x < nwp ? red[32 + threadIdx.x] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+      }
+      __syncwarp();
+      if (threadIdx.x == 0) { red[0] = s0; red[1] = s1; }
+    }
     __syncthreads();
     const double e0 = red[0], e1 = red[1];
     for (int i = threadIdx.x; i < P; i += blockDim.x)
-      rhs[i] = fma(k.bcV[P + i], e1, fma(k.bcV[i], e0, t2[i]));
+      u[i] = fma(__ldg(k.bcV + P + i), e1, fma(__ldg(k.bcV + i), e0, y[i]));
     __syncthreads();
-    vec_csr(tbs, rhs, k.c2s_ptr, k.c2s_col, k.c2s_val, P);
+    for (int i = threadIdx.x; i < P; i += blockDim.x) {  // tb_sbp = c2s u
+      double acc = 0.0;
+      for (int q = 0; q < ew; ++q)
+        acc = fma(__ldg(k.c2s_eval + q * P + i), u[__ldg(k.c2s_ecol + q * P + i)], acc);
+      tbs[i] = acc;
+    }
   }
   // last substep: y = t2 stays in global memory; the last per-mode kernel of
   // the corrector maps it back to coefficients (k_corr_sub, rows_by_ctas)
@@ -671,6 +849,17 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
     cudaFuncSetAttribute(k_corr_sub_mid<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
     cudaFuncSetAttribute(k_corr_sub_mid<cdfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
   }
+  {  // window overlap: r^ov <= 1e-7 for the decay rate r of A^-1 (two rows of margin)
+    const double aa = 0.5 * k.mu * k.kappa * sub_dt * (double)p.d.Nz * (double)p.d.Nz;
+    int ov = 2;
+    if (aa > 0.0) {
+      const double r = 2.0 * aa / ((1.0 + 2.0 * aa) + std::sqrt(1.0 + 4.0 * aa));
+      ov = std::max(2, (int)std::ceil(std::log(1e-7) / std::log(r)) + 2);
+    }
+    k.win_ov = ov <= CV::kWinOvMax ? ov : 0;
+  }
+  const size_t tsm = (size_t)kTstepSmem(p.d.P) * sizeof(double);
+  cudaFuncSetAttribute(k_corr_tstep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
   Profiler& pf = w.prof;
   pf.begin("corr_pre", st);
   pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp, a.tbp, w.vec);
@@ -688,7 +877,7 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
       ++n;
     }
     pf.begin("corr_step_1d", st);
-    k_corr_tstep<<<1, NT, 11 * (size_t)p.d.P * sizeof(double), st>>>(k, w.vec, sub_dt, last, s == 0);
+    k_corr_tstep<<<1, NT, tsm, st>>>(k, w.vec, sub_dt, last, s == 0);
     pf.end(st);
     if (!last && fused_mid) {
       pf.begin("corr_sub_mid", st);

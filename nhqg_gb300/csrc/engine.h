@@ -75,6 +75,11 @@ struct Tables {
   double* c2s_val = nullptr;
   int *s2c_ptr = nullptr, *s2c_col = nullptr;
   double* s2c_val = nullptr;
+  // the same two maps as fixed-width rows (ELL, [q][P], zero-padded, in the
+  // CSR order) for the 1-D kernels: every entry's position is known up front
+  int ell_w = 0;
+  int *c2s_ecol = nullptr, *s2c_ecol = nullptr;
+  double *c2s_eval = nullptr, *s2c_eval = nullptr;
   double* bcF = nullptr;    // [2*P] rows N-1, N of (proj_dir - I) V_inv
   double* bcV = nullptr;    // [2*P] columns N-1, N of V
   double* c2sV = nullptr;     // [P*P] cgl_to_sbp V (th_bar coefficients -> SBP grid)
@@ -90,6 +95,8 @@ struct Tables {
   double* proj = nullptr;   // [P*P] proj_dirichlet
   double* D1 = nullptr;     // [P*P] SBP first derivative
   double* Lsbp = nullptr;   // [P*P] SBP Laplacian
+  double* D1b = nullptr;    // [3*P] D1[i][i-1+d] at d*P + i
+  double* Lb = nullptr;     // [5*P] Lsbp[i][i-2+d] at d*P + i
   double* GZ = nullptr;     // [P*P]
   double* GZ2 = nullptr;    // [P*P]
   double* mean_solve = nullptr;  // [P*P] or null

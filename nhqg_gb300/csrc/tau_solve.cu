@@ -121,7 +121,8 @@ void build_tau_tables(int N, bool open_top, int n_shells, const double* coef,
 
 namespace {
 
-constexpr int kTauThreads = 256;  // 64 modes per CTA, 4 chains (re/im x parity) per mode
+constexpr int kTauThreads = 64;  // 16 modes per CTA, 4 chains (re/im x parity) per mode: small CTAs
+                                  // spread the chains evenly over the SMs
 constexpr int kPF = 8;            // rows per operand prefetch block
 
 struct TK {

@@ -635,7 +635,7 @@ __global__ void k_hermitian(Dims d, double2* q, double2* w, double2* th) {
 // order (deterministic) and resets the level's counter for the next launch.
 // C = cdfl accumulates the per-thread sums in double-float (the mixed path;
 // the FP64 pipe bounds the FP64 form on GB300); CTA totals are FP64.
-constexpr int kParSeg = 8;
+constexpr int kParSeg = 4;  // 4 P CTAs: one wave on 152 SMs for P <= 257
 template <typename C>
 __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const double2* b,
                                                  double* out, double scale, double* partials,
@@ -651,7 +651,7 @@ __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const
   // two FMAs per element on two accumulators; the half-plane weight 2 is
   // applied once
   T accr = T(0), acci = T(0);
-#pragma unroll 4
+#pragma unroll 8
   for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
     const C x = col::Prec<C>::in(al[m]), y = col::Prec<C>::in(bl[m]);
     accr = fma(x.x, y.x, accr);
@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(NT) k_parseval2(Dims d, const double2* a, cons
   const int chunk = (d.M + kParSeg - 1) / kParSeg;
   const int m0 = seg * chunk, m1 = min(d.M, m0 + chunk);
   T br = T(0), bi = T(0), cr = T(0), ci = T(0);
-#pragma unroll 4
+#pragma unroll 8
   for (int m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
     const C x = col::Prec<C>::in(al[m]), y = col::Prec<C>::in(bl[m]), z = col::Prec<C>::in(cl[m]);
     br = fma(x.x, y.x, br);
