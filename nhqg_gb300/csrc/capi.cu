@@ -350,6 +350,21 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   UP(t.proj, g->proj_dirichlet, (size_t)P * P);
   UP(t.D1, g->sbp_D1, (size_t)P * P);
   UP(t.Lsbp, g->sbp_L, (size_t)P * P);
+  {  // Parseval weights of the compact modes
+    std::vector<double2> wt(d.M);
+    for (int m = 0; m < d.M; ++m) {
+      const int r = m / d.Mc, col = m - r * d.Mc;
+      double wr = 2.0, wi = 2.0;
+      if (col == 0) {
+        const int rm = mirror_row(r, d.Mr);
+        if (r == 0) { wr = 1.0; wi = 0.0; }
+        else if (rm == r) { wr = wi = 0.5; }
+        else { wr = wi = 1.0; }
+      }
+      wt[m] = make_double2(wr, wi);
+    }
+    UP(t.pwt, wt.data(), wt.size());
+  }
   {  // diagonals of D1 and of the SBP Laplacian (the corrector's 1-D kernels)
     std::vector<double> d1b(3 * (size_t)P, 0.0), lb(5 * (size_t)P, 0.0);
     for (int i = 0; i < P; ++i) {
@@ -608,8 +623,9 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
   if (dalloc(c, &w.vec, corrector_vec_doubles(P)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
   cudaMemset(w.vec, 0, corrector_vec_doubles(P) * sizeof(double));
   if (dalloc(c, &w.partials, parseval_partials(P)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
-  if (dalloc(c, &w.counters, (size_t)P) != cudaSuccess) return fail(NHQG_ERR_CUDA);
-  if (cudaMemset(w.counters, 0, (size_t)P * sizeof(unsigned)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  if (dalloc(c, &w.counters, (size_t)P + 1) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  if (cudaMemset(w.counters, 0, ((size_t)P + 1) * sizeof(unsigned)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
+  if (dalloc(c, &w.mid_part, (size_t)P * corr_mid_ctas(p.d.M)) != cudaSuccess) return fail(NHQG_ERR_CUDA);
   if (dalloc(c, &w.status, 4) != cudaSuccess) return fail(NHQG_ERR_CUDA);
   cudaMemset(w.status, 0, 4 * sizeof(int));
   {
@@ -1034,6 +1050,7 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
     ca.wcgl = c->Wcgl; ca.wsbp = c->Wsbp; ca.tsbp = c->Tsbp; ca.tcgl = c->Tcgl;
     ca.total_dt = alpha;
     ca.df = mixed(c);
+    ca.wcgl_f = mixed(c) ? c->Wf : nullptr;  // nodal w of state1 straight to the FP32 products
     CK(run_corrector(p, c->t, c->w, ca, st, &c->launches));
     t1 = c->T1;
     tb1 = c->tb1;
@@ -1045,7 +1062,7 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
     // nodal w and theta of state1 come out of the corrector
     if (mixed(c)) {
       if ((rc = to_nodal_f32(c, c->Q1, nullptr, nullptr, st))) return rc;
-      PCK("to_f32", launch_to_f32(p, c->Wcgl, c->Tcgl, c->Wf, c->Tf, st));
+      PCK("to_f32", launch_to_f32(p, nullptr, c->Tcgl, nullptr, c->Tf, st));
       c->launches += 1;
       if ((rc = horizontal_step_f32(c, c->Qf, c->Wf, c->Tf, st))) return rc;
     } else {

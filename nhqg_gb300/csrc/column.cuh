@@ -139,6 +139,14 @@ __device__ __forceinline__ void tstorep(const C* b, double2* __restrict__ dst, i
   }
 }
 
+// FP32 tiles straight to an FP32 field
+__device__ __forceinline__ void tstorep(const float2* b, float2* __restrict__ dst, int nlev, int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    if (m < M) dst[(size_t)l * M + m] = b[i];
+  }
+}
+
 __device__ __forceinline__ void tload(double2* b, const double2* __restrict__ src, int nlev,
                                       int m0, int M) {
   for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {

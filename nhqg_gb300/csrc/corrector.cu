@@ -143,10 +143,13 @@ __device__ __forceinline__ void rows_by_ctas(const double* __restrict__ Mat, con
 // FP32-relative error there is again scaled by sub_dt) and the nodal w of the
 // next explicit RHS, whose products are FP32.  theta, the state the corrector
 // carries, stays double-float.
+// The double-float instantiation writes w as FP32 (wcgl_f, wsbp_f; a null
+// wcgl_f skips the nodal w), the FP64 one as FP64 (wcgl, wsbp).
 template <typename C>
 __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const double2* tp,
-                                                 double2* wcgl, double2* wsbp, double2* tsbp,
-                                                 const double* tbp, double* vec) {
+                                                 double2* wcgl, double2* wsbp, float2* wcgl_f,
+                                                 float2* wsbp_f, double2* tsbp, const double* tbp,
+                                                 double* vec) {
   rows_by_ctas(k.c2sV, tbp, vec + CV{k.P}.tb_sbp(), k.P);
   using CW = typename std::conditional<std::is_same<C, cdfl>::value, float2, C>::type;
   extern __shared__ double2 sm_raw[];
@@ -163,10 +166,15 @@ __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const 
     __syncthreads();
     tdct(b0, b1, k.dct, ds, false, k.P);
     __syncthreads();
-    tstorep(b0, wcgl, k.P, m0, k.M);
+    if constexpr (std::is_same<CW, float2>::value) {
+      if (wcgl_f != nullptr) tstorep(b0, wcgl_f, k.P, m0, k.M);
+    } else {
+      tstorep(b0, wcgl, k.P, m0, k.M);
+    }
     tcsr(b1, b0, k.c2s_ptr, k.c2s_col, k.c2s_val, k.P);
     __syncthreads();
-    tstorep(b1, wsbp, k.P, m0, k.M);
+    if constexpr (std::is_same<CW, float2>::value) tstorep(b1, wsbp_f, k.P, m0, k.M);
+    else tstorep(b1, wsbp, k.P, m0, k.M);
     __syncthreads();
   }
   C* sm = reinterpret_cast<C*>(sm_raw);
@@ -183,8 +191,8 @@ __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const 
   tstorep(b1, tsbp, k.P, m0, k.M);
 }
 
-template <typename C>
-__global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const double2* wsbp,
+template <typename C, typename WT>
+__global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const WT* wsbp,
                                                  const double* g_half, double sub_dt, int last,
                                                  double2* t_out, double2* tcgl, const double* y_mean,
                                                  double* tb_out) {
@@ -259,6 +267,8 @@ constexpr int kSM = 8;
 constexpr int kSubThreads = 256;
 constexpr int kLG = kSubThreads / kSM;  // level groups
 
+__device__ __forceinline__ float as_float(dfl v) { return __fadd_rn(v.hi, v.lo); }
+
 template <typename V>
 struct SubK {
   int P, M, rw;
@@ -268,14 +278,24 @@ struct SubK {
   V sub_dt;
 };
 
-template <typename C>
+// With part != nullptr the CTA also forms the per-level sums of
+// wt Re(w conj(theta_sbp')) over its kSM modes (the Parseval weights of the
+// compact modes, pwt), the next substep's flux <w theta> before its scale;
+// part[l * gridDim.x + blockIdx.x] holds them, summed over CTAs in a fixed
+// order by k_corr_tstep.  The weights take the ky = 0 column once instead of
+// through its Hermitian projection: the corrector's per-mode maps have real
+// coefficients, so Hermitian inputs stay Hermitian and the two agree to
+// rounding.
+template <typename C, typename WT>
 __global__ void __launch_bounds__(kSubThreads) k_corr_sub_mid(SubK<typename Prec<C>::T> k,
                                                               double2* __restrict__ tsbp,
-                                                              const double2* __restrict__ wsbp) {
+                                                              const WT* __restrict__ wsbp,
+                                                              double* __restrict__ part,
+                                                              const double2* __restrict__ pwt) {
   using T = typename Prec<C>::T;
   extern __shared__ double2 xs_raw[];      // [P][kSM]
   C* xs = reinterpret_cast<C*>(xs_raw);
-  __shared__ C part[2][kLG][kSM];          // partial dot products
+  __shared__ C sum2[2][kLG][kSM];          // partial dot products
   const int P = k.P, M = k.M;
   const int mm = threadIdx.x % kSM, lg = threadIdx.x / kSM;
   const int m = blockIdx.x * kSM + mm;
@@ -291,24 +311,46 @@ __global__ void __launch_bounds__(kSubThreads) k_corr_sub_mid(SubK<typename Prec
     d0 = col::gaxpy(k.Fs[l], x, d0);
     d1 = col::gaxpy(k.Fs[P + l], x, d1);
   }
-  part[0][lg][mm] = d0;
-  part[1][lg][mm] = d1;
+  sum2[0][lg][mm] = d0;
+  sum2[1][lg][mm] = d1;
   __syncthreads();
   if (lg < 2) {  // 2 kSM threads: (j, mm) totals, summed in a fixed order
     C acc = col::gzero<C>();
-    for (int q = 0; q < kLG; ++q) acc = gadd(acc, part[lg][q][mm]);
-    part[lg][0][mm] = acc;
+    for (int q = 0; q < kLG; ++q) acc = gadd(acc, sum2[lg][q][mm]);
+    sum2[lg][0][mm] = acc;
   }
   __syncthreads();
-  d0 = part[0][0][mm];
-  d1 = part[1][0][mm];
-  if (!ok) return;
+  d0 = sum2[0][0][mm];
+  d1 = sum2[1][0][mm];
+  float wr = 0.f, wi = 0.f;
+  if (part != nullptr && ok) {
+    const double2 wt = pwt[m];  // 2, 1, 1/2 or 0: exact in FP32
+    wr = (float)wt.x;
+    wi = (float)wt.y;
+  }
+  // the kSM lanes of a level group run the same levels
+  const unsigned gmask = 0xFFu << (threadIdx.x & 24);
   for (int l = lg; l < P; l += kLG) {
     C v = col::gaxpy(k.Us[P + l], d1, gscale(d0, k.Us[l]));
     const int* rc = k.Rcol + (size_t)l * k.rw;
     const T* rv = k.Rval + (size_t)l * k.rw;
     for (int q = 0; q < k.rw; ++q) v = col::gaxpy(rv[q], xs[rc[q] * kSM + mm], v);
-    tsbp[(size_t)l * M + m] = Prec<C>::out(v);
+    const size_t g = (size_t)l * M + m;
+    if (ok) tsbp[g] = Prec<C>::out(v);
+    if constexpr (std::is_same<WT, float2>::value) {
+      // the flux enters th_bar scaled by mu sub_dt D1: FP32 products of the
+      // FP32 w with theta rounded to FP32, summed over the kSM modes in FP32,
+      // then in FP64 across CTAs
+      if (part != nullptr) {
+        float f = 0.f;
+        if (ok) {
+          const float2 w = wsbp[g];
+          f = fmaf(wr * w.x, as_float(v.x), (wi * w.y) * as_float(v.y));
+        }
+        for (int o = 1; o < kSM; o <<= 1) f += __shfl_xor_sync(gmask, f, o);
+        if (mm == 0) part[(size_t)l * gridDim.x + blockIdx.x] = f2d_bits(f);
+      }
+    }
   }
 }
 
@@ -467,13 +509,36 @@ __host__ __device__ constexpr int kTstepSmem(int P) { return 15 * P + 64 + CV::w
 // B and factors the windows.  Every phase issues its global loads together
 // (the band tables, the fixed-width c2s / s2c rows), so each costs one
 // memory latency.
-__global__ void __launch_bounds__(NT) k_corr_tstep(CK k, double* vec, double sub_dt, int last, int init) {
+//
+// With part != nullptr (a substep after a fused k_corr_sub_mid) the kernel
+// runs on P CTAs: CTA l first sums the nsum per-CTA sums of level l in a
+// fixed order into the flux, and the last CTA to finish (arrival counter,
+// reset for the next launch) goes on with the 1-D update; the others exit.
+__global__ void __launch_bounds__(NT) k_corr_tstep(CK k, double* vec, double sub_dt, int last, int init,
+                                                   const double* __restrict__ part, int nsum,
+                                                   double scale, unsigned* counter) {
   const CV cv{k.P};
   const int P = k.P;
   const int nw = CV::n_win(P);
   __shared__ double red[64];
   __shared__ float wmax[2][NT / 32];
   __shared__ int fail;
+  if (part != nullptr) {
+    __shared__ bool is_last;
+    const int l = blockIdx.x;
+    double acc = 0.0;
+    for (int j = threadIdx.x; j < nsum; j += blockDim.x) acc += part[(size_t)l * nsum + j];
+    const double tot = block_sum(acc, red);
+    if (threadIdx.x == 0) {
+      vec[cv.flux() + l] = tot * scale;
+      __threadfence();
+      is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    if (threadIdx.x == 0) *counter = 0u;
+  }
   extern __shared__ double smem[];
   double* A = smem;               // 5P FP64 band
   double* xs = smem + 5 * P;      // tb_sbp
@@ -562,7 +627,7 @@ __global__ void __launch_bounds__(NT) k_corr_tstep(CK k, double* vec, double sub
     for (int e = 0; e < 3; ++e) {
       const int c = min(max(i - 1 + e, 0), P - 1);
       dv[e] = d1at(e, i);
-      fv[e] = flux[c];
+      fv[e] = __ldcg(flux + c);  // written by other CTAs of this launch
     }
     double acc = 0.0;
 #pragma unroll
@@ -826,6 +891,7 @@ __global__ void k_mean_legacy(LK k, const double* tb, const double* flux, double
 }  // namespace
 
 size_t corrector_vec_doubles(int P) { return (size_t)CV{P}.total(); }
+int corr_mid_ctas(int M) { return (M + kSM - 1) / kSM; }
 
 cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrArgs& a,
                           cudaStream_t st, int* nlaunch) {
@@ -840,14 +906,17 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   // double-float tiles (same 16-byte complex size) need the fast DCT's tables
   const bool df = a.df && k.dct.fast && k.dct.tw_df != nullptr;
   auto pre = df ? k_corr_pre<cdfl> : k_corr_pre<double2>;
-  auto sub = df ? k_corr_sub<cdfl> : k_corr_sub<double2>;
   cudaFuncSetAttribute(pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  cudaFuncSetAttribute(sub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+  cudaFuncSetAttribute(k_corr_sub<cdfl, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+  cudaFuncSetAttribute(k_corr_sub<double2, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+  // the double-float path keeps w in FP32 in the wsbp buffer
+  float2* wsbp_f = reinterpret_cast<float2*>(a.wsbp);
   const size_t smid = (size_t)p.d.P * kSM * sizeof(double2);
   const bool fused_mid = smid <= 200 * 1024 && t.R_col != nullptr;
   if (fused_mid) {
-    cudaFuncSetAttribute(k_corr_sub_mid<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
-    cudaFuncSetAttribute(k_corr_sub_mid<cdfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
+    cudaFuncSetAttribute(k_corr_sub_mid<double2, double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smid);
+    cudaFuncSetAttribute(k_corr_sub_mid<cdfl, float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smid);
   }
   {  // window overlap: r^ov <= 1e-7 for the decay rate r of A^-1 (two rows of margin)
     const double aa = 0.5 * k.mu * k.kappa * sub_dt * (double)p.d.Nz * (double)p.d.Nz;
@@ -862,38 +931,57 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
   cudaFuncSetAttribute(k_corr_tstep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
   Profiler& pf = w.prof;
   pf.begin("corr_pre", st);
-  pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.tsbp, a.tbp, w.vec);
+  pre<<<grid, NT, sm2, st>>>(k, a.wp, a.tp, a.wcgl, a.wsbp, a.wcgl_f, wsbp_f, a.tsbp, a.tbp, w.vec);
   pf.end(st);
   pf.begin("parseval", st);
-  launch_parseval2(p, a.wsbp, a.wsbp, a.tsbp, p.d.P, w.vec + cv.w2(), w.vec + cv.flux(), w, st, df);
+  if (df)
+    launch_parseval2(p, wsbp_f, wsbp_f, a.tsbp, p.d.P, w.vec + cv.w2(), w.vec + cv.flux(), w, st, true);
+  else
+    launch_parseval2(p, a.wsbp, a.wsbp, a.tsbp, p.d.P, w.vec + cv.w2(), w.vec + cv.flux(), w, st, false);
   pf.end(st);
   int n = 2;
+  // the double-float path takes the next substep's flux from the fused
+  // substep's per-CTA sums instead of a separate Parseval pass
+  const bool mid_flux = df && fused_mid && t.R_val_df && t.pwt && w.mid_part;
+  const int nmid = corr_mid_ctas(p.d.M);
+  const double n2 = (double)p.d.Nx * (double)p.d.Nx;
   for (int s = 0; s < nsub; ++s) {
     const int last = (s == nsub - 1);
-    if (s > 0) {
+    const bool from_mid = s > 0 && mid_flux;
+    if (s > 0 && !from_mid) {
       pf.begin("parseval", st);
-      launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st, df);
+      if (df) launch_parseval(p, wsbp_f, a.tsbp, p.d.P, w.vec + cv.flux(), w, st, true);
+      else launch_parseval(p, a.wsbp, a.tsbp, p.d.P, w.vec + cv.flux(), w, st, false);
       pf.end(st);
       ++n;
     }
     pf.begin("corr_step_1d", st);
-    k_corr_tstep<<<1, NT, tsm, st>>>(k, w.vec, sub_dt, last, s == 0);
+    if (from_mid)
+      k_corr_tstep<<<p.d.P, NT, tsm, st>>>(k, w.vec, sub_dt, last, 0, w.mid_part, nmid, 1.0 / (n2 * n2),
+                                             w.counters + p.d.P);
+    else
+      k_corr_tstep<<<1, NT, tsm, st>>>(k, w.vec, sub_dt, last, s == 0, nullptr, 0, 0.0, nullptr);
     pf.end(st);
-    if (!last && fused_mid) {
+    if (!last && fused_mid && (!df || t.R_val_df)) {
       pf.begin("corr_sub_mid", st);
-      if (df && t.R_val_df) {
+      if (df) {
         SubK<dfl> sk{p.d.P, p.d.M, t.R_w, t.R_col, t.R_val_df, t.Fs_df, t.Us_df, w.vec + cv.g_half(),
                      dfl(sub_dt)};
-        k_corr_sub_mid<cdfl><<<(p.d.M + kSM - 1) / kSM, kSubThreads, smid, st>>>(sk, a.tsbp, a.wsbp);
+        k_corr_sub_mid<cdfl, float2><<<nmid, kSubThreads, smid, st>>>(sk, a.tsbp, wsbp_f,
+                                                                      mid_flux ? w.mid_part : nullptr, t.pwt);
       } else {
         SubK<double> sk{p.d.P, p.d.M, t.R_w, t.R_col, t.R_val, t.Fs, t.Us, w.vec + cv.g_half(), sub_dt};
-        k_corr_sub_mid<double2><<<(p.d.M + kSM - 1) / kSM, kSubThreads, smid, st>>>(sk, a.tsbp, a.wsbp);
+        k_corr_sub_mid<double2, double2><<<nmid, kSubThreads, smid, st>>>(sk, a.tsbp, a.wsbp, nullptr, nullptr);
       }
       pf.end(st);
     } else {
       pf.begin(last ? "corr_sub_last" : "corr_sub", st);
-      sub<<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt, last, a.t_out,
-                                 a.tcgl, w.vec + cv.tmp2(), a.tb_out);
+      if (df)
+        k_corr_sub<cdfl, float2><<<grid, NT, sm4, st>>>(k, a.tsbp, wsbp_f, w.vec + cv.g_half(), sub_dt, last,
+                                                        a.t_out, a.tcgl, w.vec + cv.tmp2(), a.tb_out);
+      else
+        k_corr_sub<double2, double2><<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt,
+                                                            last, a.t_out, a.tcgl, w.vec + cv.tmp2(), a.tb_out);
       pf.end(st);
     }
     n += 2;
@@ -908,7 +996,8 @@ cudaError_t launch_corr_pre(const Params& p, const Tables& t, const double2* w, 
   const size_t sm2 = 2 * (size_t)p.d.P * TM * sizeof(double2) + col::dct_smem_bytes(k.dct);
   cudaFuncSetAttribute(k_corr_pre<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
   k.c2sV = nullptr;  // no mean-temperature side job here
-  k_corr_pre<double2><<<(p.d.M + TM - 1) / TM, NT, sm2, st>>>(k, w, th, wcgl, wsbp, tsbp, nullptr, nullptr);
+  k_corr_pre<double2><<<(p.d.M + TM - 1) / TM, NT, sm2, st>>>(k, w, th, wcgl, wsbp, nullptr, nullptr, tsbp,
+                                                               nullptr, nullptr);
   return cudaGetLastError();
 }
 

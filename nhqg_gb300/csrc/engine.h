@@ -97,6 +97,10 @@ struct Tables {
   double* Lsbp = nullptr;   // [P*P] SBP Laplacian
   double* D1b = nullptr;    // [3*P] D1[i][i-1+d] at d*P + i
   double* Lb = nullptr;     // [5*P] Lsbp[i][i-2+d] at d*P + i
+  // Parseval weights of the compact modes for a horizontal mean (re, im
+  // parts): 2 for ky > 0, 1 on the ky = 0 column (its Hermitian projection
+  // for Hermitian fields), 1/2 at the padded kx Nyquist, (1, 0) at k = 0
+  double2* pwt = nullptr;   // [M]
   double* GZ = nullptr;     // [P*P]
   double* GZ2 = nullptr;    // [P*P]
   double* mean_solve = nullptr;  // [P*P] or null
@@ -236,7 +240,10 @@ struct Work {
   // small vectors
   double* vec = nullptr;       // assorted 1-D vectors (see corrector.cu)
   double* partials = nullptr;    // per-segment reduction sums [P * parseval segments]
-  unsigned* counters = nullptr;  // per-level arrival counters of the reductions [P], kept at 0
+  unsigned* counters = nullptr;  // arrival counters of the reductions [P + 1], kept at 0
+  // per-CTA level sums of <w theta> from the fused corrector substeps
+  // [P * corr_mid_ctas(M)]
+  double* mid_part = nullptr;
   int* status = nullptr;       // device status word
 };
 
@@ -353,9 +360,16 @@ cudaError_t launch_finalize(const Params& p, const double2* q, const double2* w,
                             double2* qo, double2* wo, double2* to, cudaStream_t st);
 cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
                             double* out, Work& w, cudaStream_t st, bool df = false);
+cudaError_t launch_parseval(const Params& p, const float2* a, const double2* b, int levels,
+                            double* out, Work& w, cudaStream_t st, bool df = false);
 size_t parseval_partials(int levels);
+// CTAs of the fused corrector substep (one level sum each per level)
+int corr_mid_ctas(int M);
 // <a b> and <a c> per level in one pass over a
 cudaError_t launch_parseval2(const Params& p, const double2* a, const double2* b, const double2* c,
+                             int levels, double* out_ab, double* out_ac, Work& w, cudaStream_t st,
+                             bool df = false);
+cudaError_t launch_parseval2(const Params& p, const float2* a, const float2* b, const double2* c,
                              int levels, double* out_ab, double* out_ac, Work& w, cudaStream_t st,
                              bool df = false);
 cudaError_t launch_hermitian(const Params& p, double2* q, double2* w, double2* th, cudaStream_t st);
@@ -384,6 +398,11 @@ struct CorrArgs {
   double2 *wcgl, *wsbp, *tsbp, *tcgl;  // work; tcgl may be null
   double total_dt;
   bool df;  // double-float column tiles (the mixed-precision path)
+  // double-float path: w stays FP32 (it enters the corrector only through the
+  // sub_dt-scaled exchange increment, the means and the FP32 products); the
+  // SBP-grid w lives in the wsbp buffer as float2, the nodal w goes to
+  // wcgl_f (the FP32 products' input) or nowhere (null)
+  float2* wcgl_f = nullptr;
 };
 cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrArgs& a,
                           cudaStream_t st, int* nlaunch);

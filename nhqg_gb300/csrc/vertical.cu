@@ -636,15 +636,18 @@ __global__ void k_hermitian(Dims d, double2* q, double2* w, double2* th) {
 // C = cdfl accumulates the per-thread sums in double-float (the mixed path;
 // the FP64 pipe bounds the FP64 form on GB300); CTA totals are FP64.
 constexpr int kParSeg = 4;  // 4 P CTAs: one wave on 152 SMs for P <= 257
-template <typename C>
-__global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const double2* b,
+__device__ __forceinline__ double2 as_d2(double2 v) { return v; }
+__device__ __forceinline__ double2 as_d2(float2 v) { return make_double2(f2d_bits(v.x), f2d_bits(v.y)); }
+
+template <typename C, typename TA>
+__global__ void __launch_bounds__(NT) k_parseval(Dims d, const TA* a, const double2* b,
                                                  double* out, double scale, double* partials,
                                                  unsigned* counters) {
   using T = typename col::Prec<C>::T;
   __shared__ double scratch[32];
   __shared__ bool is_last;
   const int l = blockIdx.y, seg = blockIdx.x;
-  const double2* al = a + (size_t)l * d.M;
+  const TA* al = a + (size_t)l * d.M;
   const double2* bl = b + (size_t)l * d.M;
   const int chunk = (d.M + kParSeg - 1) / kParSeg;
   const int m0 = seg * chunk, m1 = min(d.M, m0 + chunk);
@@ -665,7 +668,7 @@ __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const
     const int m = r * d.Mc;
     if (m < m0 || m >= m1) continue;
     const int rm = mirror_row(r, d.Mr);
-    const double2 x = al[m], xm = al[rm * d.Mc];
+    const double2 x = as_d2(al[m]), xm = as_d2(al[rm * d.Mc]);
     const double2 y = bl[m], ym = bl[rm * d.Mc];
     const double xy = fma(x.x, y.x, x.y * y.y);
     if (rm == r && r != 0) {  // padded kx Nyquist (full-band layout only)
@@ -695,16 +698,16 @@ __global__ void __launch_bounds__(NT) k_parseval(Dims d, const double2* a, const
 // Two horizontal means in one pass over a: out_ab[l] = <a b>, out_ac[l] =
 // <a c> (the corrector's <w^2> and <w theta>), same weights, order and
 // arithmetic as k_parseval; partials hold two sums per (level, segment).
-template <typename C>
-__global__ void __launch_bounds__(NT) k_parseval2(Dims d, const double2* a, const double2* b,
+template <typename C, typename TA>
+__global__ void __launch_bounds__(NT) k_parseval2(Dims d, const TA* a, const TA* b,
                                                   const double2* c, double* out_ab, double* out_ac,
                                                   double scale, double* partials, unsigned* counters) {
   using T = typename col::Prec<C>::T;
   __shared__ double scratch[32];
   __shared__ bool is_last;
   const int l = blockIdx.y, seg = blockIdx.x;
-  const double2* al = a + (size_t)l * d.M;
-  const double2* bl = b + (size_t)l * d.M;
+  const TA* al = a + (size_t)l * d.M;
+  const TA* bl = b + (size_t)l * d.M;
   const double2* cl = c + (size_t)l * d.M;
   const int chunk = (d.M + kParSeg - 1) / kParSeg;
   const int m0 = seg * chunk, m1 = min(d.M, m0 + chunk);
@@ -729,8 +732,8 @@ __global__ void __launch_bounds__(NT) k_parseval2(Dims d, const double2* a, cons
     const int m = r * d.Mc;
     if (m < m0 || m >= m1) continue;
     const int rm = mirror_row(r, d.Mr);
-    const double2 x = al[m], xm = al[rm * d.Mc];
-    const double2 y = bl[m], ym = bl[rm * d.Mc];
+    const double2 x = as_d2(al[m]), xm = as_d2(al[rm * d.Mc]);
+    const double2 y = as_d2(bl[m]), ym = as_d2(bl[rm * d.Mc]);
     const double2 z = cl[m], zm = cl[rm * d.Mc];
     const double xy = fma(x.x, y.x, x.y * y.y), xz = fma(x.x, z.x, x.y * z.y);
     if (rm == r && r != 0) {
@@ -971,23 +974,44 @@ cudaError_t launch_zero_mode0(const Params& p, double2* f, int levels, cudaStrea
 
 size_t parseval_partials(int levels) { return 2 * (size_t)levels * kParSeg; }
 
-cudaError_t launch_parseval2(const Params& p, const double2* a, const double2* b, const double2* c,
-                             int levels, double* out_ab, double* out_ac, Work& w, cudaStream_t st,
-                             bool df) {
+template <typename TA>
+cudaError_t parseval2_t(const Params& p, const TA* a, const TA* b, const double2* c,
+                        int levels, double* out_ab, double* out_ac, Work& w, cudaStream_t st,
+                        bool df) {
   const double n2 = (double)p.d.Nx * (double)p.d.Nx;
-  auto kern = df ? k_parseval2<cdfl> : k_parseval2<double2>;
+  auto kern = df ? k_parseval2<cdfl, TA> : k_parseval2<double2, TA>;
   kern<<<dim3(kParSeg, levels), NT, 0, st>>>(p.d, a, b, c, out_ab, out_ac, 1.0 / (n2 * n2), w.partials,
+                                             w.counters);
+  return cudaGetLastError();
+}
+
+template <typename TA>
+cudaError_t parseval_t(const Params& p, const TA* a, const double2* b, int levels,
+                       double* out, Work& w, cudaStream_t st, bool df) {
+  const double n2 = (double)p.d.Nx * (double)p.d.Nx;
+  auto kern = df ? k_parseval<cdfl, TA> : k_parseval<double2, TA>;
+  kern<<<dim3(kParSeg, levels), NT, 0, st>>>(p.d, a, b, out, 1.0 / (n2 * n2), w.partials,
                                              w.counters);
   return cudaGetLastError();
 }
 
 cudaError_t launch_parseval(const Params& p, const double2* a, const double2* b, int levels,
                             double* out, Work& w, cudaStream_t st, bool df) {
-  const double n2 = (double)p.d.Nx * (double)p.d.Nx;
-  auto kern = df ? k_parseval<cdfl> : k_parseval<double2>;
-  kern<<<dim3(kParSeg, levels), NT, 0, st>>>(p.d, a, b, out, 1.0 / (n2 * n2), w.partials,
-                                             w.counters);
-  return cudaGetLastError();
+  return parseval_t(p, a, b, levels, out, w, st, df);
+}
+cudaError_t launch_parseval(const Params& p, const float2* a, const double2* b, int levels,
+                            double* out, Work& w, cudaStream_t st, bool df) {
+  return parseval_t(p, a, b, levels, out, w, st, df);
+}
+cudaError_t launch_parseval2(const Params& p, const double2* a, const double2* b, const double2* c,
+                             int levels, double* out_ab, double* out_ac, Work& w, cudaStream_t st,
+                             bool df) {
+  return parseval2_t(p, a, b, c, levels, out_ab, out_ac, w, st, df);
+}
+cudaError_t launch_parseval2(const Params& p, const float2* a, const float2* b, const double2* c,
+                             int levels, double* out_ab, double* out_ac, Work& w, cudaStream_t st,
+                             bool df) {
+  return parseval2_t(p, a, b, c, levels, out_ab, out_ac, w, st, df);
 }
 
 }  // namespace nhqg
