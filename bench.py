@@ -182,18 +182,18 @@ def kernel_work(name: str, g, launches_per_step: int, tc: bool = False) -> tuple
         return 4.0 * G * G * M, 2 * G * M * 16.0 + n_in * G * G * 8.0, "fp64"
     if name == "tau_solve":
         return 2 * 12.0 * Nz * M, 2 * G * M * 16.0, "fp64"
-    if name == "corr_pre":
-        return 2 * dct * M, 5 * field64, col
+    # the mixed step keeps the corrector's w in FP32 (8 B per complex value)
+    wbytes = P * M * (8.0 if tc else 16.0)
+    if name == "corr_pre":  # w, theta in; nodal w, SBP w, SBP theta out
+        return 2 * dct * M, 3 * field64 + 2 * wbytes, col
     if name == "corr_sub":
-        return 2 * 8.0 * P * M, 4 * field64, col
+        return 2 * 8.0 * P * M, 3 * field64 + wbytes, col
     if name == "corr_sub_mid":  # x = t - dt g w, two dots, R x + rank 2: memory-bound
-        return 2 * 16.0 * P * M, 3 * field64, "hbm"
+        return 2 * 16.0 * P * M, 2 * field64 + wbytes, "hbm"
     if name == "corr_sub_last":  # + inverse DCT of y and the Dirichlet pseudo-inverse
-        return dct * M + 2 * 16.0 * P * M, 4 * field64, col
+        return dct * M + 2 * 16.0 * P * M, 2 * field64 + 2 * wbytes, col
     if name == "vpost":  # stencil, G_Z scan, two stage updates per mode and level
         return 12.0 * P * M, 5 * field64, col
-    if name == "to_f32":
-        return 0.0, 2 * P * M * (16.0 + 8.0), "hbm"
     # tensor-core vertical transforms: two parity-folded GEMMs of Nz/2 rows
     # per field, three TF32 split products each (12 (Nz/2) K M flops);
     # designed HBM-bound: FP64 coefficients in / FP32 nodal out, or FP32 in

@@ -1050,7 +1050,9 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
     ca.wcgl = c->Wcgl; ca.wsbp = c->Wsbp; ca.tsbp = c->Tsbp; ca.tcgl = c->Tcgl;
     ca.total_dt = alpha;
     ca.df = mixed(c);
-    ca.wcgl_f = mixed(c) ? c->Wf : nullptr;  // nodal w of state1 straight to the FP32 products
+    // nodal w and theta of state1 straight to the FP32 products
+    ca.wcgl_f = mixed(c) ? c->Wf : nullptr;
+    ca.tcgl_f = mixed(c) ? c->Tf : nullptr;
     CK(run_corrector(p, c->t, c->w, ca, st, &c->launches));
     t1 = c->T1;
     tb1 = c->tb1;
@@ -1062,8 +1064,6 @@ int one_step(nhqg_ctx* c, cudaStream_t st) {
     // nodal w and theta of state1 come out of the corrector
     if (mixed(c)) {
       if ((rc = to_nodal_f32(c, c->Q1, nullptr, nullptr, st))) return rc;
-      PCK("to_f32", launch_to_f32(p, nullptr, c->Tcgl, nullptr, c->Tf, st));
-      c->launches += 1;
       if ((rc = horizontal_step_f32(c, c->Qf, c->Wf, c->Tf, st))) return rc;
     } else {
       PCK("vfwd", launch_vfwd(p, c->t, c->Q1, nullptr, nullptr, c->Qn, nullptr, nullptr, st));

@@ -139,6 +139,13 @@ __device__ __forceinline__ void tstorep(const C* b, double2* __restrict__ dst, i
   }
 }
 
+// double-float tiles rounded to an FP32 field
+__device__ __forceinline__ void tstorep(const cdfl* b, float2* __restrict__ dst, int nlev, int m0, int M) {
+  for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {
+    const int l = i / TM, mm = i - l * TM, m = m0 + mm;
+    if (m < M) dst[(size_t)l * M + m] = make_float2(__fadd_rn(b[i].x.hi, b[i].x.lo), __fadd_rn(b[i].y.hi, b[i].y.lo));
+  }
+}
 // FP32 tiles straight to an FP32 field
 __device__ __forceinline__ void tstorep(const float2* b, float2* __restrict__ dst, int nlev, int m0, int M) {
   for (int i = threadIdx.x; i < nlev * TM; i += blockDim.x) {

@@ -194,7 +194,10 @@ __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const 
 template <typename C, typename WT>
 __global__ void __launch_bounds__(NT) k_corr_sub(CK k, double2* tsbp, const WT* wsbp,
                                                  const double* g_half, double sub_dt, int last,
-                                                 double2* t_out, double2* tcgl, const double* y_mean,
+                                                 double2* t_out,
+                                                 typename std::conditional<std::is_same<WT, float2>::value,
+                                                                           float2, double2>::type* tcgl,
+                                                 const double* y_mean,
                                                  double* tb_out) {
   // last substep: the corrected mean temperature tb_out = P_tau V^-1 y_mean
   if (last) rows_by_ctas(k.tauVinv, y_mean, tb_out, k.P);
@@ -978,7 +981,7 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
       pf.begin(last ? "corr_sub_last" : "corr_sub", st);
       if (df)
         k_corr_sub<cdfl, float2><<<grid, NT, sm4, st>>>(k, a.tsbp, wsbp_f, w.vec + cv.g_half(), sub_dt, last,
-                                                        a.t_out, a.tcgl, w.vec + cv.tmp2(), a.tb_out);
+                                                        a.t_out, a.tcgl_f, w.vec + cv.tmp2(), a.tb_out);
       else
         k_corr_sub<double2, double2><<<grid, NT, sm4, st>>>(k, a.tsbp, a.wsbp, w.vec + cv.g_half(), sub_dt,
                                                             last, a.t_out, a.tcgl, w.vec + cv.tmp2(), a.tb_out);

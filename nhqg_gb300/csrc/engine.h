@@ -334,9 +334,6 @@ cudaError_t launch_tc_to_nodal(const Params& p, const Tables& t, const Work& w, 
 // E_w, E_theta (Galerkin, G rows) of nodal A_q, A_w, A_theta (TC_E_Q, TC_E_G)
 cudaError_t launch_tc_to_coef(const Params& p, const Tables& t, const Work& w, float2* aq,
                               float2* aw, float2* at, bool explicit_form, cudaStream_t st);
-// FP64 nodal fields (the corrector's w and theta) -> FP32, P*M elements each
-cudaError_t launch_to_f32(const Params& p, const double2* a, const double2* b, float2* fa,
-                          float2* fb, cudaStream_t st);  // a/fa may be null
 // O(N) tau solve of the per-shell w system (the mixed-precision path's
 // replacement for the dense shell inverses)
 cudaError_t launch_tau_solve(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
@@ -403,6 +400,7 @@ struct CorrArgs {
   // SBP-grid w lives in the wsbp buffer as float2, the nodal w goes to
   // wcgl_f (the FP32 products' input) or nowhere (null)
   float2* wcgl_f = nullptr;
+  float2* tcgl_f = nullptr;  // double-float path: nodal theta rounded to FP32 (or null)
 };
 cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrArgs& a,
                           cudaStream_t st, int* nlaunch);

@@ -886,35 +886,6 @@ cudaError_t launch_sub_diss(const Params& p, double2* K, const double2* Y, const
   return cudaGetLastError();
 }
 
-namespace {
-
-__global__ void k_to_f32(const double2* __restrict__ a, const double2* __restrict__ b,
-                         float2* __restrict__ fa, float2* __restrict__ fb, size_t n) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    if (a) {
-      const double2 x = a[i];
-      fa[i] = make_float2((float)x.x, (float)x.y);
-    }
-    const double2 y = b[i];
-    fb[i] = make_float2((float)y.x, (float)y.y);
-  }
-}
-
-}  // namespace
-
-cudaError_t launch_to_f32(const Params& p, const double2* a, const double2* b, float2* fa,
-                          float2* fb, cudaStream_t st) {
-  const size_t n = (size_t)p.d.P * p.d.M;
-  int sms = 0, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t want = (n + 255) / 256;
-  const int grid = (int)std::min<size_t>(want, (size_t)(sms > 0 ? sms : 1) * 8);
-  k_to_f32<<<grid, 256, 0, st>>>(a, b, fa, fb, n);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_shell(const Params& p, const Tables& t, const double2* rhs_w, double2* w_out,
                          cudaStream_t st) {
   const size_t sm = (size_t)p.d.G * SHELL_NC * sizeof(double2);

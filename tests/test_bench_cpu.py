@@ -37,7 +37,7 @@ def test_kernel_work_model(rule):
     g = make_grid(NHQGConfig(**bench.workload(48, 16, rule)))
     names = ["h1_col_ifft", "h2_row_products", "h3_col_fft", "h2_row_products_f32", "vfwd",
              "vback_stage1", "vback_stage2", "shell_solve", "tau_solve", "corr_pre", "corr_sub_mid",
-             "corr_sub_last", "vpost", "to_f32", "tc_to_nodal", "tc_to_coef"]
+             "corr_sub_last", "vpost", "tc_to_nodal", "tc_to_coef"]
     for tc in (False, True):
         for n in names:
             flops, bytes_, pipe = bench.kernel_work(n, g, 1, tc)
