@@ -185,14 +185,32 @@ __global__ void __launch_bounds__(kTauThreads) k_tau_solve(TK k, const double* _
     const int cnt = (N - 2 - p) / 2;  // rows n = p+2, p+4, .., last
     const int last = p + 2 * cnt;
     double d = 0.0;
+    double rprev = rv(p);  // Dirichlet f_n = r_{n-2} - r_n: r_{n-2} carried from the row before
     for (int r0 = 0; r0 < cnt; r0 += kPF) {
       double lr[kPF], ty[kPF];
+      if (!k.open_top) {
+        double rr[kPF], rmv[kPF];
 #pragma unroll
-      for (int q = 0; q < kPF; ++q) {
-        const int n = p + 2 + 2 * (r0 + q);
-        const bool in = r0 + q < cnt;
-        lr[q] = in ? __ldg(Lrm + n) : 0.0;
-        ty[q] = in ? f(n) * __ldg(rm + n) : 0.0;
+        for (int q = 0; q < kPF; ++q) {
+          const int n = p + 2 + 2 * (r0 + q);
+          const bool in = r0 + q < cnt;
+          lr[q] = in ? __ldg(Lrm + n) : 0.0;
+          rmv[q] = in ? __ldg(rm + n) : 0.0;
+          rr[q] = in ? rv(n) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < kPF; ++q) {
+          ty[q] = (rprev - rr[q]) * rmv[q];
+          rprev = rr[q];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < kPF; ++q) {
+          const int n = p + 2 + 2 * (r0 + q);
+          const bool in = r0 + q < cnt;
+          lr[q] = in ? __ldg(Lrm + n) : 0.0;
+          ty[q] = in ? f(n) * __ldg(rm + n) : 0.0;
+        }
       }
 #pragma unroll
       for (int q = 0; q < kPF; ++q) {
@@ -229,10 +247,22 @@ __global__ void __launch_bounds__(kTauThreads) k_tau_solve(TK k, const double* _
   }
   b0 += __shfl_xor_sync(0xffffffffu, b0, 1);  // partner lane: same column, other parity
   b1 += __shfl_xor_sync(0xffffffffu, b1, 1);
+  // Dirichlet w basis: the pseudo-inverse w_n = -sum_{j <= n} c_j (same
+  // parity, n < G = N-1) runs inside the pass that forms c; the open top's
+  // w recurrence couples the two classes and reads c back from y
+  const bool fold = !k.open_top;
+  double acc = 0.0;
   if (s_zero) {
     // A' = a I: c_n = f_n / a for n <= N-2 (the rows the pseudo-inverse reads)
-    for (int n = p; n <= N - 2; n += 2)
-      if (live) y[at(n)] = f(n) * ra;
+    for (int n = p; n <= N - 2; n += 2) {
+      const double cv = f(n) * ra;
+      if (fold) {
+        acc -= cv;
+        if (live) wout[at(n)] = acc;
+      } else if (live) {
+        y[at(n)] = cv;
+      }
+    }
   } else {
     b0 = fma(ra, fma(k.g1_0, f0, k.g1_1 * f1), b0);
     b1 = fma(ra, f0 - f1, b1);
@@ -248,33 +278,21 @@ __global__ void __launch_bounds__(kTauThreads) k_tau_solve(TK k, const double* _
       double c;
       if (n < 2) c = fma(s4ra, e0, fp * ra);
       else c = fma(__ldg(uA + n), em2, fma(__ldg(uB + n), e0, __ldg(uC + n) * ep2));
-      if (live) y[at(n)] = c;
+      if (fold) {
+        acc -= c;
+        if (live) wout[at(n)] = acc;
+      } else if (live) {
+        y[at(n)] = c;
+      }
       em2 = e0;
       e0 = ep2;
     }
   }
+  if (fold) return;
   __syncwarp();
-  // w = pinv_w c over n < G (the pseudo-inverse reads c_0 .. c_{N-2})
+  // open top: w = pinv_w c over n < G (the pseudo-inverse reads c_0 .. c_{N-2})
   if (!live) return;
-  if (!k.open_top) {
-    double acc = 0.0;
-    for (int r0 = p; r0 < G; r0 += 2 * kPF) {
-      double cv[kPF];
-#pragma unroll
-      for (int q = 0; q < kPF; ++q) {
-        const int n = r0 + 2 * q;
-        cv[q] = n < G ? y[at(n)] : 0.0;
-      }
-#pragma unroll
-      for (int q = 0; q < kPF; ++q) {
-        const int n = r0 + 2 * q;
-        if (n < G) {
-          acc -= cv[q];
-          wout[at(n)] = acc;
-        }
-      }
-    }
-  } else if (p == 0) {
+  if (p == 0) {
     double w1 = 0.0, w2 = 0.0;
     for (int n = 0; n < G; ++n) {
       double w = y[at(n)];
