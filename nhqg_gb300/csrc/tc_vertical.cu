@@ -25,14 +25,14 @@
 // Work decomposition.  One CTA owns 128 real columns (64 complex modes; the
 // matrices are real, so real and imaginary parts are independent columns)
 // and every level.  The fold index (K) runs in chunks of 8 (one MMA k-step)
-// through a 4-stage shared-memory ring; per stage
+// through a 3-stage shared-memory ring (two CTAs per SM); per stage
 //   A chunk: E_hi, E_lo, O_hi, O_lo (4 tiles of 128 x 8 TF32), laid out by the
 //     host in the canonical no-swizzle K-major core-matrix order and fetched
 //     by one cp.async.bulk on the stage's "full" mbarrier;
 //   B chunk: 16 converter warps (4 groups x 128 columns) fold, split and
 //     store their input rows in the same order, then arrive on the stage's
 //     "ready" mbarrier.  Each converter streams its own input elements into
-//     registers 4 chunks ahead (coalesced across the warp).
+//     registers 3 chunks ahead (coalesced across the warp).
 // A control warp owns TMEM; its lane 0 issues the bulk copies and six MMAs
 // per chunk (E and O accumulators, 128 TMEM columns each) and commits them to
 // the stage's "empty" mbarrier, which releases the stage.  The epilogue reads
@@ -56,13 +56,13 @@ namespace {
 constexpr int kCols = 128;                 // real columns per CTA = MMA N
 constexpr int kFold = 128;                 // MMA M
 constexpr int kKc = 8;                     // fold indices per chunk (TF32 k-step)
-constexpr int kStages = 4;
+constexpr int kStages = 3;
 constexpr int kThreads = 512;
 constexpr int kGroups = kThreads / 128;    // thread groups per column (2 fold indices each)
 static_assert(2 * kGroups == 8, "each group converts two fold indices of a chunk");
 constexpr int kTile = kFold * kKc * 4;     // one 128 x 8 TF32 operand tile, bytes
 constexpr int kAB = 4 * kTile;             // hi/lo x even/odd tiles of one chunk
-constexpr int kAhead = 4;                  // chunks of input prefetched into registers
+constexpr int kAhead = 3;                  // chunks of input prefetched into registers
 static_assert(kAhead == kStages, "the register ring and the stage ring share their index");
 constexpr uint32_t kTmemCols = 256;        // E accumulator [0,128), O [128,256)
 constexpr uint64_t kWaitNs = 1000000000ull;
@@ -228,7 +228,7 @@ struct TcArgs {
 };
 
 template <bool INV>
-__global__ void __launch_bounds__(kThreads + 64, 1) k_tc_vertical(const __grid_constant__ TcArgs a) {
+__global__ void __launch_bounds__(kThreads + 64, 2) k_tc_vertical(const __grid_constant__ TcArgs a) {
   using In = typename std::conditional<INV, float, double>::type;
   constexpr int SB = stage_bytes<INV>();
   extern __shared__ uint8_t tc_smem_raw[];
@@ -399,15 +399,11 @@ __global__ void __launch_bounds__(kThreads + 64, 1) k_tc_vertical(const __grid_c
     const uint32_t tl = tmem + ((uint32_t)(lq * 32) << 16);
     float* tt = reinterpret_cast<float*>(sm) + warp * (32 * 33);
     const int nrow = min(32, H - lq * 32);  // valid fold rows of this lane quarter
-    float e[32], o[32];
-    tc_ld32(tl + cc, e);
-    tc_ld32(tl + 128 + cc, o);
     const int cg = col0 + cc + lane;
-#pragma unroll
-    for (int pass = 0; pass < 2; ++pass) {  // rows 2i / i, then 2i+1 / N-i
-#pragma unroll
-      for (int q = 0; q < 32; ++q)
-        tt[lane * 33 + q] = INV ? (pass ? o[q] : e[q]) : (pass ? e[q] - o[q] : e[q] + o[q]);
+    // one 32-column accumulator block in registers at a time: E goes to the
+    // transpose tile first, then O is combined with it (forward: E + O and
+    // E - O from the same two values) or written after it (inverse)
+    auto store_rows = [&](int pass) {  // rows 2i / i (pass 0), 2i+1 / N-i (pass 1)
       __syncwarp();
       if (cg < a.ncols) {
         for (int r = 0; r < nrow; ++r) {
@@ -418,6 +414,28 @@ __global__ void __launch_bounds__(kThreads + 64, 1) k_tc_vertical(const __grid_c
         }
       }
       __syncwarp();
+    };
+    float v[32];
+    tc_ld32(tl + cc, v);
+#pragma unroll
+    for (int q = 0; q < 32; ++q) tt[lane * 33 + q] = v[q];
+    if (INV) store_rows(0);
+    tc_ld32(tl + 128 + cc, v);
+    if (INV) {
+#pragma unroll
+      for (int q = 0; q < 32; ++q) tt[lane * 33 + q] = v[q];
+      store_rows(1);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const float e = tt[lane * 33 + q];
+        tt[lane * 33 + q] = e + v[q];
+        v[q] = e - v[q];
+      }
+      store_rows(0);
+#pragma unroll
+      for (int q = 0; q < 32; ++q) tt[lane * 33 + q] = v[q];
+      store_rows(1);
     }
     if (grp == 0 && cval && (!INV || F.rows > N)) {
       const float x = ((red[t] + red[kCols + t]) + red[2 * kCols + t]) + red[3 * kCols + t];
