@@ -174,9 +174,19 @@ def kernel_work(name: str, g, launches_per_step: int, tc: bool = False) -> tuple
         # stage combinations, counted from the kernel's operations (FMA = 2
         # flops) per level and mode over the three fields: 42 at stage 1, 108
         # at stage 2.
+        # Bytes: every distinct field once.  Stage 1 reads A_q, A_w, A_theta
+        # and the state q0, w0, t0 and writes E1 (3) and the solve's R_q,
+        # R_theta, rhs_w; stage 2 reads A (3), q0, w0, t0, E1 (3), q1, w1,
+        # t1, t1p and writes R_q, R_theta, rhs_w.  A is FP32 in the mixed
+        # step (8 B), FP64 nodal otherwise.
+        a_b = 3 * (0.5 if tc else 1.0) * field64
+        if name == "vback_stage1":
+            b = a_b + 3 * field64 + 6 * field64
+        else:
+            b = a_b + 10 * field64 + 3 * field64
         if tc:
-            return (42.0 if name == "vback_stage1" else 108.0) * P * M, 12 * field64, col
-        return 3 * dct * M, 12 * field64, "fp64"
+            return (42.0 if name == "vback_stage1" else 108.0) * P * M, b, col
+        return 3 * dct * M, b, "fp64"
     if name == "shell_solve":
         n_in = len(np.unique(g.imex_shell_row[g.imex_shell_row >= 0]))
         return 4.0 * G * G * M, 2 * G * M * 16.0 + n_in * G * G * 8.0, "fp64"
@@ -207,13 +217,10 @@ def kernel_work(name: str, g, launches_per_step: int, tc: bool = False) -> tuple
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# dominant kernel class of the mixed step at 256^2 x 256 (2/3 rule), from one
-# single-pass ncu capture of a timed mixed step at that size
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
 # main kernel classes of the mixed step at 256^2 x 256 (2/3 rule), each from
-# a one-launch ncu capture of a mixed step at that size (profiles/)
-NCU_TRAFFIC_256 = {"corr_pre": 258424320, "vback_stage2": 880997888, "h2_row_products_f32": 451207424,
-                   "tau_solve": 225772800, "corr_sub_mid": 136062976, "vpost": 272108032}
+# a one-launch ncu --set full capture of a timed mixed step at that size
+NCU_TRAFFIC_256 = {"h2_row_products_f32": 448960256, "vback_stage2": 880899840, "corr_pre": 202028800,
+                   "corr_sub_last": 143561472, "corr_sub_mid": 103279104, "tau_solve": 218991360}
 NCU_TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, full size"
 
 
