@@ -456,15 +456,28 @@ __global__ void __launch_bounds__(128) k_h2r(HR k) {
     gyb = k.eta_y[(size_t)(xa + 1) * N + y];
   };
 
+  // L2 prefetch of field f's rows of this pair (one instruction per 128-byte
+  // line, no registers held): issued one field ahead, so the next load finds
+  // its lines in L2 instead of waiting on DRAM behind this field's FFTs
+  auto prefetch = [&](int f) {
+    const uintptr_t a0 = reinterpret_cast<uintptr_t>(k.x1 + xi(k, f, lev, pair, 0, cols));
+    const uintptr_t end = a0 + (uintptr_t)cols * sizeof(float4);
+    for (uintptr_t a = (a0 & ~uintptr_t(127)) + 128 * (uintptr_t)l; a < end; a += 128 * R1)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+  };
+
   float2 x[R2], y[R2], u[R2];
   if constexpr (FORM == HF_FLUX) {
     load(0, u);
+    prefetch(1);
+    prefetch(2);
     F::inv(u, Tg, tw_s, l);
     load(1, x);
     F::inv(x, Tg, tw_s, l);
     sfor<R2>([&](auto e) { Vg[decltype(e)::value * R1 + l] = x[decltype(e)::value]; });
     for (int f = 0; f < 3; ++f) {
       load(2 + f, x);
+      if (f < 2) prefetch(3 + f);
       F::inv(x, Tg, tw_s, l);
       // G = F(u f)
       sfor<R2>([&](auto e) {
