@@ -116,6 +116,15 @@ template <typename C> __device__ __forceinline__ C gneg(C a) { return gmk<C>(-a.
 template <typename C, typename T> __device__ __forceinline__ C gaxpy(T s, C a, C acc) {
   return gmk<C>(fma(s, a.x, acc.x), fma(s, a.y, acc.y));
 }
+// L2 prefetch of a CTA's columns (modes m0 .. m0 + TM - 1) of a [nlev][M]
+// field of esize-byte values: one instruction per level, issued a phase ahead
+// of the tile load so that the load finds L2 instead of waiting on DRAM
+__device__ __forceinline__ void tprefetch(const void* f, int nlev, int m0, int M, size_t esize) {
+  if (f == nullptr) return;
+  const char* base = static_cast<const char*>(f) + (size_t)m0 * esize;
+  for (int l = threadIdx.x; l < nlev; l += blockDim.x)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)l * M * esize));
+}
 // FP64 field columns <-> tiles of type C
 template <typename C>
 __device__ __forceinline__ void tloadp(C* b, const double2* __restrict__ src, int nlev, int m0, int M) {

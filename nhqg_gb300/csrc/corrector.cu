@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(NT) k_corr_pre(CK k, const double2* wp, const 
   const int PT = k.P * TM;
   void* dct_base = sm_raw + 2 * PT;  // after two tiles of the widest type
   const int m0 = blockIdx.x * TM;
+  col::tprefetch(tp, k.G, m0, k.M, sizeof(double2));  // theta, read after w's transform
   {
     CW* sw = reinterpret_cast<CW*>(sm_raw);
     CW *b0 = sw, *b1 = sw + PT;

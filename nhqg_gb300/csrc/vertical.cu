@@ -175,6 +175,20 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   const size_t Ms = (size_t)M;
   const T alpha = Pr::s(a.alpha), cE1 = Pr::s(a.c_E1), cE2 = Pr::s(a.c_E2);
   const T omega = Pr::s(a.omega), gdt = Pr::s(k.gdt), Ra = Pr::s(k.Ra);
+  // L2 prefetch of the CTA's columns of a field (the line holding modes m0,
+  // m0 + 1 at every level), one field group ahead of the phase that reads it,
+  // so that the phase's loads find L2 instead of waiting on DRAM
+  auto pf = [&](const void* f, int nlev, size_t esize) {
+    if (f == nullptr) return;
+    const char* base = static_cast<const char*>(f) + (size_t)m0 * esize;
+    for (int l = threadIdx.x; l < nlev; l += blockDim.x)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)l * Ms * esize));
+  };
+  if constexpr (MODE == VB_STAGE2) {
+    pf(a.w1, G, 16); pf(a.q0, P, 16); pf(a.E1q, P, 16); pf(a.q1, P, 16);
+  } else if constexpr (MODE == VB_STAGE1) {
+    pf(a.q0, P, 16); pf(AK == AK_F32_COEF ? (const void*)a.Awf : (const void*)nullptr, G, 8);
+  }
 
   // ------------------------------------------------------------- q
   if (MODE != VB_SOLVE) {
@@ -247,6 +261,13 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   }
 
   // ------------------------------------------------------------- w
+  if constexpr (MODE == VB_STAGE2) {
+    if constexpr (AK == AK_F32_COEF) pf(a.Awf, G, 8);
+    pf(a.t1, G, 16); pf(a.w0, G, 16); pf(a.E1w, G, 16);
+  } else if constexpr (MODE == VB_STAGE1) {
+    pf(a.w0, G, 16);
+    if constexpr (AK == AK_F32_COEF) pf(a.Atf, G, 8);
+  }
   if (MODE != VB_SOLVE) {
     if constexpr (AK == AK_F32_COEF) {  // E_w in the Galerkin basis
       col::tloadp(b2, a.Awf, G, m0, M);
@@ -305,6 +326,12 @@ __global__ void __launch_bounds__(NT) k_vback(VK k, VArgs a) {
   }
 
   // ------------------------------------------------------------- theta
+  if constexpr (MODE == VB_STAGE2) {
+    if constexpr (AK == AK_F32_COEF) pf(a.Atf, G, 8);
+    pf(a.t0, G, 16); pf(a.E1t, G, 16); pf(a.t1p, G, 16);
+  } else if constexpr (MODE == VB_STAGE1) {
+    pf(a.t0, G, 16);
+  }
   if (MODE != VB_SOLVE) {
     if constexpr (AK == AK_F64) {
       tload(b0, a.At, P, m0, M);
@@ -402,6 +429,8 @@ __global__ void __launch_bounds__(NT) k_vpost(VK k, const double2* Rq, const dou
   const int m0 = blockIdx.x * TM;
   const int M = k.M;
   const typename Pr::T gdt = Pr::s(k.gdt);
+  col::tprefetch(Rq, k.P, m0, M, sizeof(double2));
+  col::tprefetch(Rt, k.G, m0, M, sizeof(double2));
   col::tloadp(b0, wn, k.G, m0, M);
   __syncthreads();
   tstencil_w(k, b1, b0);  // w Chebyshev coefficients
