@@ -317,18 +317,23 @@ __device__ __forceinline__ void tscan(int len, bool reverse, Get get, Put put) {
     const int pos = r0 + t;                        // position along the scan
     const int n = reverse ? len - 1 - pos : pos;   // level
     const bool in = pos < len;
+    // warps of this round that hold at least one position (the others would
+    // only add zeros: they skip the shuffles and post zero totals)
+    const int nwa = min(NW, (len - r0 + 31) >> 5);
     C v[TM];
 #pragma unroll
     for (int mm = 0; mm < TM; ++mm) v[mm] = in ? get(n, mm) : gzero<C>();
     // class scan within the warp: positions of one class are 2 apart
+    if (warp < nwa) {
 #pragma unroll
-    for (int o = 2; o < 32; o <<= 1) {
+      for (int o = 2; o < 32; o <<= 1) {
 #pragma unroll
-      for (int mm = 0; mm < TM; ++mm) {
-        C u;
-        u.x = __shfl_up_sync(0xffffffffu, v[mm].x, o);
-        u.y = __shfl_up_sync(0xffffffffu, v[mm].y, o);
-        if (lane >= o) v[mm] = gadd(v[mm], u);
+        for (int mm = 0; mm < TM; ++mm) {
+          C u;
+          u.x = __shfl_up_sync(0xffffffffu, v[mm].x, o);
+          u.y = __shfl_up_sync(0xffffffffu, v[mm].y, o);
+          if (lane >= o) v[mm] = gadd(v[mm], u);
+        }
       }
     }
     // lanes 30 and 31 hold the warp's totals of the two position classes
@@ -340,9 +345,17 @@ __device__ __forceinline__ void tscan(int len, bool reverse, Get get, Put put) {
     if (t < 2 * TM) {  // exclusive prefix over the warps, and the carry into the next round
       const int c = t / TM, mm = t % TM;
       C acc = carry[c][mm];
-      for (int w = 0; w < NW; ++w) {
-        pref[w][c][mm] = acc;
-        acc = gadd(acc, red[w][c][mm]);
+      if (nwa == NW) {  // every warp holds positions: unrolled
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+          pref[w][c][mm] = acc;
+          acc = gadd(acc, red[w][c][mm]);
+        }
+      } else {  // a short column or the last round: the warps that hold positions
+        for (int w = 0; w < nwa; ++w) {
+          pref[w][c][mm] = acc;
+          acc = gadd(acc, red[w][c][mm]);
+        }
       }
       carry[c][mm] = acc;
     }
