@@ -586,6 +586,11 @@ int nhqg_ctx_create(const nhqg_grid_desc* g, nhqg_ctx** out) {
     // (NHQG_REG_FFT=0 selects the shared-memory FFT kernels)
     const char* e = getenv("NHQG_REG_FFT");
     p.reg_fft = !(e && e[0] == '0');
+    // NHQG_CORR_WINDOW_OVERLAP=<rows> overrides the corrector's window overlap
+    // (a tuning and test switch: every setting solves to FP64 round-off, small
+    // overlaps through the fallback to one global factorisation)
+    const char* ov = getenv("NHQG_CORR_WINDOW_OVERLAP");
+    p.corr_win_ov = (ov && ov[0]) ? atoi(ov) : -1;
   }
 
   // ---- work buffers ----

@@ -930,6 +930,7 @@ cudaError_t run_corrector(const Params& p, const Tables& t, Work& w, const CorrA
       ov = std::max(2, (int)std::ceil(std::log(1e-7) / std::log(r)) + 2);
     }
     k.win_ov = ov <= CV::kWinOvMax ? ov : 0;
+    if (p.corr_win_ov >= 0) k.win_ov = p.corr_win_ov <= CV::kWinOvMax ? p.corr_win_ov : 0;
   }
   const size_t tsm = (size_t)kTstepSmem(p.d.P) * sizeof(double);
   cudaFuncSetAttribute(k_corr_tstep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);

@@ -139,6 +139,9 @@ struct Params {
   // FP32 horizontal products with register-resident FFTs (horizontal_reg.cu)
   // where the transform length allows, else the shared-memory FFT kernels
   bool reg_fft;
+  // overlap rows of the corrector's windowed 1-D solve; -1: set from the decay
+  // of A^-1 (the default), 0: one global FP32 LU, > 24: windows off
+  int corr_win_ov;
   int scheme;  // NHQG_SCHEME_*
 };
 
