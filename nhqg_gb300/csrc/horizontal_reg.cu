@@ -276,6 +276,15 @@ __global__ void __launch_bounds__(128) k_h1r(HR k) {
   float2* Tg = T + (size_t)(warp * G + g) * F::TILE;
   const float kys = live ? k.ky_full[c] * k.scale : 0.f;
   const float sc = k.scale;
+  if (nphase == 2 && ncb > 0) {
+    // L2 prefetch of phase 1's columns (w, theta) while phase 0 runs: one
+    // instruction per row and field (the CTA's CB columns share a line or two)
+    for (int i = threadIdx.x; i < 2 * k.rows_in; i += blockDim.x) {
+      const int r = i >> 1;
+      const float2* f = (i & 1) ? k.th : k.w;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(f + (size_t)lev * plane + (size_t)r * k.cols_in + c0));
+    }
+  }
   for (int phase = 0; phase < nphase; ++phase) {
     if (phase > 0) __syncthreads();  // the previous phase's reads of the tile are done
     for (int i = threadIdx.x; i < k.rows_in * CB; i += blockDim.x) {
