@@ -106,12 +106,15 @@ def imex_step_many(states, grid: Grid, precision: str = "fp64", out=None) -> lis
     """``imex_step`` of each of a sequence of independent states held in host
     memory, with the host<->device copies overlapped with the steps: step k
     computes on the current stream while the input of step k+1 is uploaded
-    and the result of step k-1 downloaded on two copy streams (double-buffered
-    device states, ordered by CUDA events).  Inputs in pinned memory let the
-    copies run asynchronously.  Results go to ``out`` (a list of host State
-    tuples of pinned tensors, reused cyclically if shorter than ``states``) or
-    to new pinned tensors; returns the list of results, complete on return.
-    The band-limit status is checked once, after the last step."""
+    and the result of step k-1 downloaded on two copy streams (three device
+    states in rotation, ordered by CUDA events: the upload into a state waits
+    only for the download of the result it held three steps earlier, so the
+    two directions of the host link run at the same time).  Inputs in pinned
+    memory let the copies run asynchronously.  Results go to ``out`` (a list
+    of host State tuples of pinned tensors, reused cyclically if shorter than
+    ``states``) or to new pinned tensors; returns the list of results,
+    complete on return.  The band-limit status is checked once, after the
+    last step."""
     states = list(states)
     if not states:
         return []
@@ -121,18 +124,19 @@ def imex_step_many(states, grid: Grid, precision: str = "fp64", out=None) -> lis
     up, down = torch.cuda.Stream(), torch.cuda.Stream()
     dtypes = (torch.complex128, torch.complex128, torch.complex128, torch.float64)
     first = [torch.as_tensor(np.asarray(x)) if not isinstance(x, torch.Tensor) else x for x in states[0]]
+    nbuf = 3
     bufs = [State(*(torch.empty(t.shape, dtype=d, device="cuda") for t, d in zip(first, dtypes)))
-            for _ in range(2)]
+            for _ in range(nbuf)]
     if out is None:
         out = [tuple(torch.empty(t.shape, dtype=d, pin_memory=True) for t, d in zip(first, dtypes))
                for _ in range(len(states))]
-    ev_in = [torch.cuda.Event() for _ in range(2)]
-    ev_done = [torch.cuda.Event() for _ in range(2)]
-    ev_out = [torch.cuda.Event() for _ in range(2)]
+    ev_in = [torch.cuda.Event() for _ in range(nbuf)]
+    ev_done = [torch.cuda.Event() for _ in range(nbuf)]
+    ev_out = [torch.cuda.Event() for _ in range(nbuf)]
     results = []
     for k, st in enumerate(states):
-        b = k % 2
-        if k >= 2:
+        b = k % nbuf
+        if k >= nbuf:
             up.wait_event(ev_out[b])  # buffer b's previous result has left the device
         with torch.cuda.stream(up):
             for dst, src, d in zip(bufs[b], st, dtypes):

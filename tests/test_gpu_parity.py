@@ -205,13 +205,15 @@ def test_make_initial_state_reference_regression():
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_imex_step_many_matches_imex_step(precision):
     """The pipelined host-state stepping (copies on two streams overlapped with
-    the steps) returns exactly what imex_step returns for each input."""
+    the steps, three device states in rotation) returns exactly what
+    imex_step returns for each input; six inputs reuse every device state."""
     meta, arrays = fixtures.load_case("prod16")
     g = make_grid(NHQGConfig(**dict(meta["cfg"])))
     ins = []
     for label in ("r", "s0", "r1", "r5"):
         st = fixtures.state_from(arrays, label)
         ins.append(tuple(torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in st))
+    ins += ins[:2]
     got = S.imex_step_many(ins, g, precision=precision)
     assert len(got) == len(ins)
     for inp, res in zip(ins, got):
