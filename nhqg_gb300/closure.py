@@ -1,5 +1,5 @@
-"""Learned vertical-tail closure for q (spec extension 3; no reference
-counterpart).
+"""Learned vertical-tail closure for q (an extension of the step with no
+reference counterpart).
 
 The closure adds C_n = -s (r_n + i rho_n) q_n to the explicit q tendency on
 the first ``ncoef`` (<= 64) Chebyshev coefficients of every horizontal mode,

@@ -1,5 +1,5 @@
-// Learned vertical-tail closure for q (spec extension 3; no reference
-// counterpart).  Per horizontal mode column (compact band) the closure adds
+// Learned vertical-tail closure for q (an extension of the step with no
+// reference counterpart).  Per horizontal mode column (compact band) the closure adds
 //   C_n = -s * (r_n + i rho_n)(f) * q_n,   n < n_coef (<= 64),
 // to the explicit q tendency, where (r, rho) = MLP(f) is a complex
 // per-coefficient rate computed from phase-invariant features of the column:

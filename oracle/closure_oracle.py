@@ -1,7 +1,7 @@
 """NumPy restatement of the learned vertical-tail closure (test oracle).
 
 TEST INFRASTRUCTURE -- see ``oracle/__init__.py``.  The closure has no
-reference counterpart (spec extension); this file restates the model
+reference counterpart (an extension of the step); this file restates the model
 that ``nhqg_gb300/csrc/closure.cu`` implements so that the GPU features,
 forward pass and gradients can be checked, and it is itself pinned by
 central finite differences in ``tests/test_closure_oracle.py``.
