@@ -615,7 +615,7 @@ def run_ours(args, ws, rank, local):
                                 {"value": round(ws * args.steps / (ms_dct * 1e-3), 4), "unit": "steps/s",
                                  "ms_per_step": round(ms_dct / args.steps, 4)}),
         "rel_err_vs_plain": study_conv,
-        "precision_study_config3_start": study_lin,
+        "precision_study_linear_spinup": study_lin,
         "simulated_time_per_wall_hour": round(3600.0 * cfgd["dt"] * value / ws, 6),
         "gpu_launches": sum(n for n, _ in prof_mixed.values()),
         "roofline": dom,

@@ -94,7 +94,7 @@ def test_ensemble_recaptures_on_precision_change():
     ens.close()
 
 
-def test_ensemble_config4_size_classes():
+def test_ensemble_48_members_size_classes():
     """One member per size class of the 48-instance benchmark ensemble
     (64^2x32, 96^2x48 with radix-3 transforms, 128^2x64; L = 10 L_c,
     dt = 5e-5, Ra ~ U(40, 120), production recipe), each in FP64 and mixed

@@ -138,16 +138,16 @@ def test_tau_solve_nz256():
         assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) <= 1e-8
 
 
-CFG1 = dict(Nx=64, Nz=32, L=10 * L_C, Ra_tilde=100.0, sigma=1.0, nu_q=1.0, nu_w=1.0, nu_theta=1.0,
+CFG_64X32 = dict(Nx=64, Nz=32, L=10 * L_C, Ra_tilde=100.0, sigma=1.0, nu_q=1.0, nu_w=1.0, nu_theta=1.0,
             hyper_order=1, dt=5e-5, nonlinear_advection="flux", horizontal_dealiasing="23_rule",
             float_dtype="float64", thermal_closure="evolve_mean",
             mean_exchange_discretization="balanced_sbp2_pc", sbp_corrector_substeps=4)
 
 
-def test_config1_100_steps_mixed():
+def test_64x32_100_steps_mixed():
     """64^2 x 32 production recipe, 100 mixed steps vs the FP64 oracle."""
-    g = make_grid(NHQGConfig(**CFG1))
-    o = oracle.make_grid(OracleConfig(**CFG1))
+    g = make_grid(NHQGConfig(**CFG_64X32))
+    o = oracle.make_grid(OracleConfig(**CFG_64X32))
     s0 = theta_perturbation_state(g, seed=0)
     os_ = OracleState(*s0)
     for _ in range(100):
@@ -184,7 +184,7 @@ def _bf16(a):
     return b.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def test_config1_convecting_state_100_steps(monkeypatch):
+def test_64x32_convecting_state_100_steps_mixed(monkeypatch):
     """64^2 x 32 production recipe from a convecting state (seeded theta'
     of amplitude 1, 4000 mixed steps: t = 0.2, Nu - 1 ~ 4), where the
     advection term is O(1) of the tendency: 100 mixed steps within 1e-6 of
@@ -192,7 +192,7 @@ def test_config1_convecting_state_100_steps(monkeypatch):
     oracle steps with the product factors rounded to BF16 leave the 1e-6
     band, so the gate sees the precision of the products."""
     from nhqg_gb300.diagnostics import compute_diagnostics
-    g = make_grid(NHQGConfig(**CFG1))
+    g = make_grid(NHQGConfig(**CFG_64X32))
     s0 = S.to_device(theta_perturbation_state(g, seed=0, amplitude=1.0))
     S.step_inplace(s0, g, 4000, check=True, precision="mixed")
     d = compute_diagnostics(s0, g)
@@ -202,7 +202,7 @@ def test_config1_convecting_state_100_steps(monkeypatch):
     share = float(torch.linalg.norm(E.th_hat) / torch.linalg.norm(I.th_hat))
     assert share > 0.05, share  # the nonlinear term is a visible part of the theta tendency
     host = S.to_host(s0)
-    o = oracle.make_grid(OracleConfig(**CFG1))
+    o = oracle.make_grid(OracleConfig(**CFG_64X32))
     ref = OracleState(*host)
     for _ in range(100):
         ref = oracle.imex_step(ref, o)

@@ -161,8 +161,8 @@ def test_golden_seeded_trajectory(case):
     assert_state_close(_host(s), fixtures.state_from(arrays, "sN"), 1e-11, th_bar_abs=1e-16)
 
 
-# ---------------------------------------------------------------- benchmark configuration 1
-CFG1 = dict(Nx=64, Nz=32, L=10 * L_C, Ra_tilde=100.0, sigma=1.0, nu_q=1.0, nu_w=1.0, nu_theta=1.0,
+# ---------------------------------------------------------------- 64^2 x 32 production recipe
+CFG_64X32 = dict(Nx=64, Nz=32, L=10 * L_C, Ra_tilde=100.0, sigma=1.0, nu_q=1.0, nu_w=1.0, nu_theta=1.0,
             hyper_order=1, dt=5e-5, nonlinear_advection="flux", horizontal_dealiasing="23_rule",
             float_dtype="float64")
 
@@ -172,9 +172,9 @@ CFG1 = dict(Nx=64, Nz=32, L=10 * L_C, Ra_tilde=100.0, sigma=1.0, nu_q=1.0, nu_w=
     dict(thermal_closure="evolve_mean", mean_exchange_discretization="balanced_sbp2_pc",
          sbp_corrector_substeps=4),
 ])
-def test_config1_100_steps(recipe):
+def test_64x32_production_100_steps(recipe):
     """64^2 x 32, 100 steps: per-RHS <= 1e-12, 100-step <= 1e-9 vs the oracle."""
-    cfgd = dict(CFG1, **recipe)
+    cfgd = dict(CFG_64X32, **recipe)
     g = make_grid(NHQGConfig(**cfgd))
     o = oracle.make_grid(OracleConfig(**cfgd))
     s0 = theta_perturbation_state(g, seed=0)
